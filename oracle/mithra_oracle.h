@@ -1,0 +1,118 @@
+/*
+ * CPU restatement of the MITHRA FdTd time-marching loop, in plain C.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle that the CUDA path is checked against.
+ * Only tests/, __graft_entry__.smoke() and the CPU-baseline legs of bench.py may load it.
+ * The product library never links, loads or calls it.
+ *
+ * Layout follows the reference exactly so that its state can be compared with dumps of
+ * the reference itself: vector fields are arrays of N1N0*np records of 3 doubles, node
+ * m = N1N0*k + N1*i + j (src/solver.cpp:674, :2302-2315); particles are records of 11
+ * doubles  q, rnp[3], rnm[3], gb[3], e  (src/stdinclude.h:130-144).
+ *
+ * Every function states the reference lines it restates.  The arithmetic is written in
+ * the reference's order so that, compiled with -ffp-contract=off, it reproduces the
+ * reference's rounding.
+ */
+#ifndef MITHRA_ORACLE_H
+#define MITHRA_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MO_REC 11          /* doubles per particle record */
+#define MO_MAX_UND 64
+
+typedef struct {
+  int N0, N1, np, k0;       /* nodes along x, y, and along z in this domain */
+  int solver;               /* 0 = FD, 1 = NSFD */
+  int order;                /* Mur truncation order, 1 or 2 */
+  int space_charge;         /* 1: also advance the scalar potential */
+  double a[6];              /* uf_.a */
+  double nsfd_alpha, nsfd_beta;  /* uf_.af.alpha_, uf_.af.beta_ (= beta/alpha) */
+  double bB[5], cB[5], dB[5];
+  double eE[5], fE[5], gE[5];
+  double hC[17];
+  double dt, dx, dy, dz;
+} mo_field;
+
+typedef struct {
+  int type;                 /* 0 static */
+  double k, lu, rb, length, dist, theta;
+} mo_undulator;
+
+typedef struct {
+  int N0, N1, np, k0;
+  double xmin, xmax, ymin, ymax, zmin, zmax, zp0, zp1, Lz;
+  double dx, dy, dz;
+  double dtb;               /* ub_.dtb = c0 * bunch time step */
+  double r1, r2;            /* ub_.r1, ub_.r2 */
+  double gamma, beta, c0, dt_shift;  /* gamma_, beta_, c0_, dt_ */
+  int n_und;
+  mo_undulator und[MO_MAX_UND];
+} mo_push;
+
+typedef struct {
+  int N0, N1, np, k0;
+  double xmin, ymin, zmin, xmax, ymax;
+  double dx, dy, dz;
+  double dv, rc;            /* uc_.dv, uc_.rc (unused by the deposit itself) */
+  double zp0, zp1, Lz;
+} mo_deposit;
+
+typedef struct {
+  int N0, N1, np, k0;
+  int N;                    /* sampling planes */
+  int Nl, Nf;
+  double zmin, dz, zp0, zp1, gamma, beta, c0, pc;
+  const double* z;          /* N boosted plane positions */
+  const double* ep_re;      /* Nl*Nf twiddles cos(w j dt) */
+  const double* ep_im;      /* Nl*Nf twiddles sin(w j dt) */
+  double* fdt;              /* Nf * Nz * N1N0 * 4 ring buffer (state) */
+} mo_power;
+
+/* One FdTd::fieldUpdate without the MPI halo (src/fdtd.cpp:231-725): interior FD/NSFD update
+ * of A (J is read from anp1 in place), Mur faces, and for order 2 edges and corners. */
+void mo_field_update(const mo_field* f, double* anp1, const double* an, const double* anm1);
+
+/* The scalar-potential counterpart used with space charge (src/fdtdSC.cpp:260-1087):
+ * interior update with rho read from fnp1 in place, Mur faces, edges, corners. */
+void mo_scalar_update(const mo_field* f, double* fnp1, const double* fn, const double* fnm1);
+
+/* FdTd::fieldEvaluate applied to every interior node (src/fdtd.cpp:818-845) and the copies of
+ * planes k=1, np-2 into k=0, np-1 (src/fdtd.cpp:742-774).  With fn != NULL the space-charge
+ * electric field -grad(phi) is added as in src/fdtdSC.cpp:1110-1140. */
+void mo_eval_eb(const mo_field* f, const double* anp1, const double* an, const double* fn,
+                float* en, float* bn);
+
+/* One Solver::bunchUpdate over all particles (src/solver.cpp:1424-1576) with the static
+ * undulator field (src/solver.cpp:1798-1880, src/beam.cc:14-76).  Particles that cross a z
+ * face are appended again, as the single-rank self-exchange does (src/solver.cpp:1544-1568).
+ * Returns the new particle count (<= cap), or -1 when cap would be exceeded. */
+long mo_push_substep(const mo_push* p, double timeBunch, double* rec, long n, long cap,
+                     const float* en, const float* bn, long* n_transverse_out);
+
+/* FdTd::currentUpdate (src/fdtd.cpp:38-185): zigzag deposit into J (which must be zeroed
+ * first, src/fdtd.cpp:23-32).  With rho != NULL also the charge deposit of
+ * src/fdtdSC.cpp:140-161. */
+void mo_deposit_current(const mo_deposit* d, const double* rec, long n, double* J, double* rho);
+
+/* The particle erasure of FdTd::currentCommunicate / Solver::recycleParticles
+ * (src/fdtd.cpp:214-224, src/solver.cpp:493-503, :2292-2296).  Returns the new count. */
+long mo_erase_outside(double zmin, double Lz, double zp0, double zp1, double* rec, long n);
+
+/* Solver::powerSample for one FEL output (src/radiation.cpp:127-232).  nTime selects the ring
+ * slot.  Writes N*Nl powers into pG. */
+void mo_power_sample(const mo_power* p, unsigned nTime, const float* en, const float* bn, double* pG);
+
+/* Thread count used by the parallel loops (1 = serial, bitwise reproduction of the reference). */
+void mo_set_threads(int n);
+int mo_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,298 @@
+"""Python binding of the C oracle (oracle/mithra_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU-baseline
+legs of bench.py, never by the product package.
+
+The state layout is the reference's: vector fields are (N1N0*np, 3) float64 arrays in node
+order m = N1N0*k + N1*i + j, particles are (n, 11) float64 records
+q, rnp[3], rnm[3], gb[3], e.  `OracleRun.step()` performs one field step in the order of
+Solver::solve (src/solver.cpp:1300-1399).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD, "libmithra_oracle.so")
+MO_MAX_UND = 64
+_lock = threading.Lock()
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile the C restatement into oracle/_build/libmithra_oracle.so (gcc, OpenMP)."""
+    src = os.path.join(HERE, "mithra_oracle.c")
+    hdr = os.path.join(HERE, "mithra_oracle.h")
+    with _lock:
+        if (not force and os.path.exists(LIB_PATH)
+                and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(src), os.path.getmtime(hdr))):
+            return LIB_PATH
+        os.makedirs(BUILD, exist_ok=True)
+        tmp = LIB_PATH + ".tmp%d" % os.getpid()
+        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", src, "-o", tmp, "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_reference(ref_src: str = "/root/reference/src", jobs: int = 8) -> str | None:
+    """Build oracle/_ref/ref_harness from the reference sources when they are present."""
+    if not os.path.isdir(ref_src):
+        return None
+    repo = os.path.dirname(HERE)
+    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "REF_SRC=" + ref_src,
+                    "-j%d" % jobs], cwd=repo, check=True)
+    return os.path.join(HERE, "_ref", "ref_harness")
+
+
+class MoField(C.Structure):
+    _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("np", C.c_int), ("k0", C.c_int),
+                ("solver", C.c_int), ("order", C.c_int), ("space_charge", C.c_int),
+                ("a", C.c_double * 6), ("nsfd_alpha", C.c_double), ("nsfd_beta", C.c_double),
+                ("bB", C.c_double * 5), ("cB", C.c_double * 5), ("dB", C.c_double * 5),
+                ("eE", C.c_double * 5), ("fE", C.c_double * 5), ("gE", C.c_double * 5),
+                ("hC", C.c_double * 17),
+                ("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+
+
+class MoUndulator(C.Structure):
+    _fields_ = [("type", C.c_int), ("k", C.c_double), ("lu", C.c_double), ("rb", C.c_double),
+                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double)]
+
+
+class MoPush(C.Structure):
+    _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("np", C.c_int), ("k0", C.c_int),
+                ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double),
+                ("zmin", C.c_double), ("zmax", C.c_double), ("zp0", C.c_double), ("zp1", C.c_double),
+                ("Lz", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("dtb", C.c_double), ("r1", C.c_double), ("r2", C.c_double),
+                ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double), ("dt_shift", C.c_double),
+                ("n_und", C.c_int), ("und", MoUndulator * MO_MAX_UND)]
+
+
+class MoDeposit(C.Structure):
+    _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("np", C.c_int), ("k0", C.c_int),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
+                ("xmax", C.c_double), ("ymax", C.c_double),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("dv", C.c_double), ("rc", C.c_double),
+                ("zp0", C.c_double), ("zp1", C.c_double), ("Lz", C.c_double)]
+
+
+class MoPower(C.Structure):
+    _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("np", C.c_int), ("k0", C.c_int),
+                ("N", C.c_int), ("Nl", C.c_int), ("Nf", C.c_int),
+                ("zmin", C.c_double), ("dz", C.c_double), ("zp0", C.c_double), ("zp1", C.c_double),
+                ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double), ("pc", C.c_double),
+                ("z", C.POINTER(C.c_double)), ("ep_re", C.POINTER(C.c_double)),
+                ("ep_im", C.POINTER(C.c_double)), ("fdt", C.POINTER(C.c_double))]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build_oracle())
+        P = C.POINTER
+        d, f, l = P(C.c_double), P(C.c_float), C.c_long
+        _lib.mo_field_update.argtypes = [P(MoField), d, d, d]
+        _lib.mo_scalar_update.argtypes = [P(MoField), d, d, d]
+        _lib.mo_eval_eb.argtypes = [P(MoField), d, d, d, f, f]
+        _lib.mo_push_substep.argtypes = [P(MoPush), C.c_double, d, l, l, f, f, P(C.c_long)]
+        _lib.mo_push_substep.restype = l
+        _lib.mo_deposit_current.argtypes = [P(MoDeposit), d, l, d, d]
+        _lib.mo_erase_outside.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, d, l]
+        _lib.mo_erase_outside.restype = l
+        _lib.mo_power_sample.argtypes = [P(MoPower), C.c_uint, f, f, d]
+        _lib.mo_set_threads.argtypes = [C.c_int]
+    return _lib
+
+
+def set_threads(n: int) -> None:
+    lib().mo_set_threads(int(n))
+
+
+def dptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def fptr(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def read_meta(path: str) -> dict:
+    out = {}
+    with open(path) as fh:
+        for line in fh:
+            k, v = line.split()
+            out[k] = float(v)
+    return out
+
+
+def field_params(m: dict, solver: int, order: int, space_charge: int = 0) -> MoField:
+    f = MoField()
+    f.N0, f.N1, f.np, f.k0 = int(m["N0"]), int(m["N1"]), int(m["np"]), int(m.get("k0", 0))
+    f.solver, f.order, f.space_charge = solver, order, space_charge
+    for i in range(6):
+        f.a[i] = m["a%d" % i]
+    f.nsfd_alpha, f.nsfd_beta = m["nsfd_alpha"], m["nsfd_beta"]
+    for name in ("bB", "cB", "dB", "eE", "fE", "gE"):
+        arr = getattr(f, name)
+        for i in range(5):
+            arr[i] = m["%s%d" % (name, i)]
+    for i in range(17):
+        f.hC[i] = m["hC%d" % i]
+    f.dt, f.dx, f.dy, f.dz = m["dt"], m["dx"], m["dy"], m["dz"]
+    return f
+
+
+def push_params(m: dict) -> MoPush:
+    p = MoPush()
+    p.N0, p.N1, p.np, p.k0 = int(m["N0"]), int(m["N1"]), int(m["np"]), int(m.get("k0", 0))
+    for k in ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax", "zp0", "zp1", "dx", "dy", "dz"):
+        setattr(p, k, m[k])
+    p.Lz = m["Lz"]
+    p.dtb, p.r1, p.r2 = m["ub_dtb"], m["ub_r1"], m["ub_r2"]
+    p.gamma, p.beta, p.c0, p.dt_shift = m["gamma"], m["beta"], m["c0"], m["dt_shift"]
+    n = int(m.get("n_undulator", 0))
+    p.n_und = n
+    for u in range(n):
+        U = p.und[u]
+        U.type = int(m["und%d_type" % u])
+        U.k, U.lu, U.rb = m["und%d_k" % u], m["und%d_lu" % u], m["und%d_rb" % u]
+        U.length, U.dist, U.theta = m["und%d_length" % u], m["und%d_dist" % u], m["und%d_theta" % u]
+    return p
+
+
+def deposit_params(m: dict) -> MoDeposit:
+    d = MoDeposit()
+    d.N0, d.N1, d.np, d.k0 = int(m["N0"]), int(m["N1"]), int(m["np"]), int(m.get("k0", 0))
+    for k in ("xmin", "ymin", "zmin", "xmax", "ymax", "dx", "dy", "dz", "zp0", "zp1"):
+        setattr(d, k, m[k])
+    d.Lz = m["Lz"]
+    d.dv, d.rc = m.get("uc_dv", 0.0), m.get("uc_rc", 0.0)
+    return d
+
+
+class PowerSampler:
+    """State of Solver::powerSample for one FEL output (src/radiation.cpp:18-232)."""
+
+    def __init__(self, m: dict, jf: int = 0):
+        self.N = int(m["rp%d_N" % jf])
+        self.Nl = int(m["rp%d_Nl" % jf])
+        self.Nf = int(m["rp%d_Nf" % jf])
+        self.z = np.array([m["rp%d_z%d" % (jf, i)] for i in range(self.N)], dtype=np.float64)
+        w = np.array([m["rp%d_w%d" % (jf, i)] for i in range(self.Nl)], dtype=np.float64)
+        dt = m["dt"]
+        import math
+        re = np.empty((self.Nl, self.Nf))
+        im = np.empty((self.Nl, self.Nf))
+        for l in range(self.Nl):
+            for j in range(self.Nf):
+                arg = w[l] * j * dt
+                re[l, j] = math.cos(arg)
+                im[l, j] = math.sin(arg)
+        self.ep_re, self.ep_im = re.ravel().copy(), im.ravel().copy()
+        N1N0 = int(m["N0"]) * int(m["N1"])
+        self.fdt = np.zeros(self.Nf * self.N * N1N0 * 4)
+        p = MoPower()
+        p.N0, p.N1, p.np, p.k0 = int(m["N0"]), int(m["N1"]), int(m["np"]), int(m.get("k0", 0))
+        p.N, p.Nl, p.Nf = self.N, self.Nl, self.Nf
+        p.zmin, p.dz, p.zp0, p.zp1 = m["zmin"], m["dz"], m["zp0"], m["zp1"]
+        p.gamma, p.beta, p.c0, p.pc = m["gamma"], m["beta"], m["c0"], m["rp%d_pc" % jf]
+        p.z, p.ep_re, p.ep_im, p.fdt = dptr(self.z), dptr(self.ep_re), dptr(self.ep_im), dptr(self.fdt)
+        self.p = p
+
+    def sample(self, n_time: int, en, bn) -> np.ndarray:
+        out = np.zeros(self.N * self.Nl)
+        lib().mo_power_sample(C.byref(self.p), n_time, fptr(en), fptr(bn), dptr(out))
+        return out
+
+
+class OracleRun:
+    """One single-rank FdTd march on the CPU, state initialised from a meta dict and arrays."""
+
+    def __init__(self, meta: dict, an, anm1, anp1, particles, solver: int, order: int,
+                 cap_factor: float = 2.0):
+        self.m = dict(meta)
+        self.f = field_params(meta, solver, order)
+        self.p = push_params(meta)
+        self.d = deposit_params(meta)
+        nodes = int(meta["N0"]) * int(meta["N1"]) * int(meta["np"])
+        self.an = np.ascontiguousarray(an, dtype=np.float64).reshape(nodes * 3).copy()
+        self.anm1 = np.ascontiguousarray(anm1, dtype=np.float64).reshape(nodes * 3).copy()
+        self.anp1 = np.ascontiguousarray(anp1, dtype=np.float64).reshape(nodes * 3).copy()
+        self.en = np.zeros(nodes * 3, dtype=np.float32)
+        self.bn = np.zeros(nodes * 3, dtype=np.float32)
+        parts = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 11)
+        self.n = parts.shape[0]
+        self.cap = max(16, int(self.n * cap_factor) + 16)
+        self.rec = np.zeros((self.cap, 11))
+        self.rec[: self.n] = parts
+        self.time = meta["time"]
+        self.time_bunch = meta["timeBunch"]
+        self.n_time = int(meta["nTime"])
+        self.n_time_bunch = int(meta["nTimeBunch"])
+        self.n_update_bunch = meta["nUpdateBunch"]
+        self.dt = meta["dt"]
+        self.dtb_time = meta["dtb"]
+        self.power = PowerSampler(meta) if int(meta.get("n_fel", 0)) > 0 and "rp0_N" in meta else None
+        self.power_rows = []
+
+    @property
+    def particles(self):
+        return self.rec[: self.n]
+
+    def field_update(self):
+        lib().mo_field_update(C.byref(self.f), dptr(self.anp1), dptr(self.an), dptr(self.anm1))
+
+    def eval_eb(self):
+        lib().mo_eval_eb(C.byref(self.f), dptr(self.anp1), dptr(self.an), None, fptr(self.en), fptr(self.bn))
+
+    def push(self):
+        nt = C.c_long(0)
+        n = lib().mo_push_substep(C.byref(self.p), self.time_bunch, dptr(self.rec), self.n, self.cap,
+                                  fptr(self.en), fptr(self.bn), C.byref(nt))
+        if n < 0:
+            raise RuntimeError("particle capacity exceeded")
+        self.n = n
+
+    def erase(self):
+        m = self.m
+        self.n = lib().mo_erase_outside(m["zmin"], m["Lz"], m["zp0"], m["zp1"], dptr(self.rec), self.n)
+
+    def deposit(self):
+        self.anp1[:] = 0.0
+        lib().mo_deposit_current(C.byref(self.d), dptr(self.rec), self.n, dptr(self.anp1), None)
+
+    def step(self):
+        """One field step, src/solver.cpp:1300-1399 (diagnostic file writers omitted)."""
+        self.field_update()
+        self.eval_eb()
+        self.rec[: self.n, 4:7] = self.rec[: self.n, 1:4]
+        t = 0.0
+        while t < self.n_update_bunch:
+            self.push()
+            self.time_bunch += self.dtb_time
+            self.n_time_bunch += 1
+            t += 1.0
+        self.erase()
+        if self.power is not None:
+            pg = self.power.sample(self.n_time, self.en, self.bn)
+            m = self.m
+            zl = m["gamma"] * (self.power.z + m["beta"] * m["c0"] * (self.time_bunch + m["dt_shift"]))
+            self.power_rows.append((zl, pg))
+        self.anm1, self.an, self.anp1 = self.an, self.anp1, self.anm1
+        self.deposit()
+        self.erase()
+        self.time += self.dt
+        self.n_time += 1

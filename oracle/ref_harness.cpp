@@ -1,0 +1,317 @@
+/*
+ * Test harness around the UNMODIFIED reference MITHRA sources (compiled from the reference
+ * tree by oracle/Makefile.ref into oracle/_ref/).  Test infrastructure only: it produces
+ * golden vectors that pin the C restatement in oracle/ and the host set-up code.
+ *
+ * Every member of MITHRA::Solver is public (src/solver.h:20-345), so the harness drives
+ * the reference's own member functions in the order of Solver::solve
+ * (src/solver.cpp:1212-1418) and dumps internal state as raw little-endian arrays:
+ *   vec3 arrays : N1N0*np records of 3 doubles (the reference AoS layout, m = N1N0*k+N1*i+j)
+ *   particles   : records of 11 doubles  q, rnp[3], rnm[3], gb[3], e  (src/stdinclude.h:130-144)
+ *
+ * Modes
+ *   init    JOB OUT                 initialise (incl. the negative-time particle loop), dump state
+ *   run     JOB NSTEPS OUT EVERY    initialise, march NSTEPS field steps, dump every EVERY steps
+ *   field   JOB IN OUT              load an/anm1/anp1(=J), FdTd::fieldUpdate, evaluate E/B eagerly
+ *   push    JOB IN OUT              load an/anp1/particles/timeBunch, one Solver::bunchUpdate
+ *   deposit JOB IN OUT              load particles, currentReset + currentUpdate (+ currentCommunicate)
+ *   power   JOB IN OUT K            K calls of Solver::powerSample on loaded field pairs
+ */
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <list>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "classes.h"
+#include "datainput.h"
+#include "fdtd.h"
+#include "fdtdSC.h"
+#include "readdata.h"
+#include "solver.h"
+
+using namespace MITHRA;
+
+static std::string jp(const std::string& a, const std::string& b) { return a + "/" + b; }
+
+static void write_raw(const std::string& path, const void* p, size_t bytes) {
+  FILE* f = fopen(path.c_str(), "wb");
+  if (!f) { perror(path.c_str()); exit(2); }
+  if (bytes && fwrite(p, 1, bytes, f) != bytes) { perror("fwrite"); exit(2); }
+  fclose(f);
+}
+static std::vector<char> read_raw(const std::string& path) {
+  FILE* f = fopen(path.c_str(), "rb");
+  if (!f) { perror(path.c_str()); exit(2); }
+  fseek(f, 0, SEEK_END); long n = ftell(f); fseek(f, 0, SEEK_SET);
+  std::vector<char> b((size_t)n);
+  if (n && fread(b.data(), 1, (size_t)n, f) != (size_t)n) { perror("fread"); exit(2); }
+  fclose(f);
+  return b;
+}
+static void dump_vec3(const std::string& path, std::vector<FieldVector<double> >* v) {
+  write_raw(path, v->data(), v->size() * sizeof(FieldVector<double>));
+}
+static void load_vec3(const std::string& path, std::vector<FieldVector<double> >* v) {
+  std::vector<char> b = read_raw(path);
+  if (b.size() != v->size() * sizeof(FieldVector<double>)) { fprintf(stderr, "size mismatch %s\n", path.c_str()); exit(2); }
+  memcpy(v->data(), b.data(), b.size());
+}
+static void dump_scalar_field(const std::string& path, std::vector<double>* v) { write_raw(path, v->data(), v->size() * 8); }
+static void load_scalar_field(const std::string& path, std::vector<double>* v) {
+  std::vector<char> b = read_raw(path);
+  if (b.size() != v->size() * 8) { fprintf(stderr, "size mismatch %s\n", path.c_str()); exit(2); }
+  memcpy(v->data(), b.data(), b.size());
+}
+static void dump_particles(const std::string& path, std::list<Charge>& q) {
+  std::vector<double> b; b.reserve(q.size() * 11);
+  for (auto& c : q) {
+    b.push_back(c.q);
+    for (int d = 0; d < 3; d++) b.push_back(c.rnp[d]);
+    for (int d = 0; d < 3; d++) b.push_back(c.rnm[d]);
+    for (int d = 0; d < 3; d++) b.push_back(c.gb[d]);
+    b.push_back(c.e);
+  }
+  write_raw(path, b.data(), b.size() * 8);
+}
+static void load_particles(const std::string& path, std::list<Charge>& q) {
+  std::vector<char> raw = read_raw(path);
+  size_t n = raw.size() / (11 * 8);
+  const double* d = (const double*)raw.data();
+  q.clear();
+  for (size_t i = 0; i < n; i++) {
+    Charge c; const double* r = d + 11 * i;
+    c.q = r[0];
+    for (int k = 0; k < 3; k++) { c.rnp[k] = r[1 + k]; c.rnm[k] = r[4 + k]; c.gb[k] = r[7 + k]; }
+    c.e = r[10];
+    q.push_back(c);
+  }
+}
+
+static void meta_line(FILE* f, const char* k, double v) { fprintf(f, "%s %.17g\n", k, v); }
+
+static void dump_meta(Solver* s, const std::string& path) {
+  FILE* f = fopen(path.c_str(), "w");
+  meta_line(f, "N0", s->N0_); meta_line(f, "N1", s->N1_); meta_line(f, "N2", s->N2_); meta_line(f, "np", s->np_);
+  meta_line(f, "k0", s->k0_);
+  meta_line(f, "xmin", s->xmin_); meta_line(f, "xmax", s->xmax_);
+  meta_line(f, "ymin", s->ymin_); meta_line(f, "ymax", s->ymax_);
+  meta_line(f, "zmin", s->zmin_); meta_line(f, "zmax", s->zmax_);
+  meta_line(f, "zp0", s->zp_[0]); meta_line(f, "zp1", s->zp_[1]);
+  meta_line(f, "dx", s->mesh_.meshResolution_[0]); meta_line(f, "dy", s->mesh_.meshResolution_[1]);
+  meta_line(f, "dz", s->mesh_.meshResolution_[2]);
+  meta_line(f, "Lx", s->mesh_.meshLength_[0]); meta_line(f, "Ly", s->mesh_.meshLength_[1]);
+  meta_line(f, "Lz", s->mesh_.meshLength_[2]);
+  meta_line(f, "dt", s->mesh_.timeStep_); meta_line(f, "dtb", s->bunch_.timeStep_);
+  meta_line(f, "nUpdateBunch", s->nUpdateBunch_);
+  meta_line(f, "totalTime", s->mesh_.totalTime_);
+  meta_line(f, "time", s->time_); meta_line(f, "timeBunch", s->timeBunch_);
+  meta_line(f, "nTime", s->nTime_); meta_line(f, "nTimeBunch", s->nTimeBunch_);
+  meta_line(f, "gamma", s->gamma_); meta_line(f, "beta", s->beta_); meta_line(f, "dt_shift", s->dt_);
+  meta_line(f, "c0", s->c0_); meta_line(f, "m0", s->m0_); meta_line(f, "e0", s->e0_);
+  for (int i = 0; i < 6; i++) { char k[32]; snprintf(k, 32, "a%d", i); meta_line(f, k, s->uf_.a[i]); }
+  meta_line(f, "nsfd_alpha", s->uf_.af.alpha_); meta_line(f, "nsfd_beta", s->uf_.af.beta_);
+  const char* bn[4] = {"bB", "cB", "dB", 0};
+  const double* bv[3] = {s->uf_.bB, s->uf_.cB, s->uf_.dB};
+  for (int b = 0; b < 3; b++)
+    for (int i = 0; i < 5; i++) { char k[32]; snprintf(k, 32, "%s%d", bn[b], i); meta_line(f, k, bv[b][i]); }
+  const char* en[3] = {"eE", "fE", "gE"};
+  const double* ev[3] = {s->uf_.eE, s->uf_.fE, s->uf_.gE};
+  for (int b = 0; b < 3; b++)
+    for (int i = 0; i < 5; i++) { char k[32]; snprintf(k, 32, "%s%d", en[b], i); meta_line(f, k, ev[b][i]); }
+  for (int i = 0; i < 17; i++) { char k[32]; snprintf(k, 32, "hC%d", i); meta_line(f, k, s->uf_.hC[i]); }
+  meta_line(f, "uc_dv", s->uc_.dv); meta_line(f, "uc_rc", s->uc_.rc);
+  meta_line(f, "ub_dtb", s->ub_.dtb); meta_line(f, "ub_r1", s->ub_.r1); meta_line(f, "ub_r2", s->ub_.r2);
+  meta_line(f, "n_undulator", (double)s->undulator_.size());
+  for (size_t u = 0; u < s->undulator_.size(); u++) {
+    char k[64];
+    snprintf(k, 64, "und%zu_k", u); meta_line(f, k, s->undulator_[u].k_);
+    snprintf(k, 64, "und%zu_lu", u); meta_line(f, k, s->undulator_[u].lu_);
+    snprintf(k, 64, "und%zu_rb", u); meta_line(f, k, s->undulator_[u].rb_);
+    snprintf(k, 64, "und%zu_length", u); meta_line(f, k, s->undulator_[u].length_);
+    snprintf(k, 64, "und%zu_dist", u); meta_line(f, k, s->undulator_[u].dist_);
+    snprintf(k, 64, "und%zu_theta", u); meta_line(f, k, s->undulator_[u].theta_);
+    snprintf(k, 64, "und%zu_type", u); meta_line(f, k, (double)s->undulator_[u].type_);
+  }
+  meta_line(f, "n_particles", (double)s->chargeVectorn_.size());
+  meta_line(f, "n_fel", (double)s->FEL_.size());
+  for (size_t j = 0; j < s->FEL_.size(); j++) {
+    char k[64];
+    if (!s->FEL_[j].radiationPower_.sampling_) continue;
+    snprintf(k, 64, "rp%zu_N", j); meta_line(f, k, s->rp_[j].N);
+    snprintf(k, 64, "rp%zu_Nl", j); meta_line(f, k, s->rp_[j].Nl);
+    snprintf(k, 64, "rp%zu_Nf", j); meta_line(f, k, s->rp_[j].Nf);
+    snprintf(k, 64, "rp%zu_pc", j); meta_line(f, k, s->rp_[j].pc);
+    for (unsigned i = 0; i < s->rp_[j].Nl; i++) { snprintf(k, 64, "rp%zu_w%u", j, i); meta_line(f, k, s->rp_[j].w[i]); }
+    for (unsigned i = 0; i < s->rp_[j].N; i++) { snprintf(k, 64, "rp%zu_z%u", j, i); meta_line(f, k, s->FEL_[j].radiationPower_.z_[i]); }
+  }
+  fclose(f);
+}
+
+/* The per-step body of Solver::solve, src/solver.cpp:1300-1399, without the file writers other
+ * than the power sample (whose values are returned through rp_[].pG). */
+static void field_step(Solver* s, FILE* power_out) {
+  s->fieldUpdate();
+  for (auto it = s->chargeVectorn_.begin(); it != s->chargeVectorn_.end(); it++) it->rnm = it->rnp;
+  for (double t = 0.0; t < s->nUpdateBunch_; t += 1.0) {
+    s->bunchUpdate();
+    s->timeBunch_ += s->bunch_.timeStep_;
+    ++s->nTimeBunch_;
+  }
+  s->recycleParticles();
+  s->powerSample();
+  if (power_out) {
+    for (size_t jf = 0; jf < s->FEL_.size(); jf++) {
+      if (!s->FEL_[jf].radiationPower_.sampling_) continue;
+      for (unsigned k = 0; k < s->rp_[jf].N; k++) {
+        double zl = s->gamma_ * (s->FEL_[jf].radiationPower_.z_[k] + s->beta_ * s->c0_ * (s->timeBunch_ + s->dt_));
+        fwrite(&zl, 8, 1, power_out);
+        for (unsigned l = 0; l < s->rp_[jf].Nl; l++) fwrite(&s->rp_[jf].pG[k * s->rp_[jf].Nl + l], 8, 1, power_out);
+      }
+    }
+  }
+  s->fieldShift();
+  s->currentReset();
+  s->currentUpdate();
+  s->currentCommunicate();
+  s->timem1_ += s->mesh_.timeStep_;
+  s->time_ += s->mesh_.timeStep_;
+  s->timep1_ += s->mesh_.timeStep_;
+  ++s->nTime_;
+}
+
+/* The negative-time particle loop of Solver::solve, src/solver.cpp:1232-1291 (diagnostics off). */
+static void pre_loop(Solver* s) {
+  while (s->time_ < 0.0) {
+    for (auto it = s->chargeVectorn_.begin(); it != s->chargeVectorn_.end(); it++) it->rnm = it->rnp;
+    for (double t = 0.0; t < s->nUpdateBunch_; t += 1.0) {
+      s->bunchUpdate();
+      s->timeBunch_ += s->bunch_.timeStep_;
+      ++s->nTimeBunch_;
+    }
+    s->recycleParticles();
+    s->timem1_ += s->mesh_.timeStep_;
+    s->time_ += s->mesh_.timeStep_;
+    s->timep1_ += s->mesh_.timeStep_;
+    ++s->nTime_;
+  }
+}
+
+static void dump_state(Solver* s, const std::string& dir) {
+  mkdir(dir.c_str(), 0755);
+  dump_meta(s, jp(dir, "meta.txt"));
+  dump_vec3(jp(dir, "an.bin"), s->an_);
+  dump_vec3(jp(dir, "anm1.bin"), s->anm1_);
+  dump_vec3(jp(dir, "anp1.bin"), s->anp1_);
+  if (s->mesh_.spaceCharge_) {
+    dump_scalar_field(jp(dir, "fn.bin"), s->fn_);
+    dump_scalar_field(jp(dir, "fnm1.bin"), s->fnm1_);
+    dump_scalar_field(jp(dir, "fnp1.bin"), s->fnp1_);
+  }
+  dump_particles(jp(dir, "particles.bin"), s->chargeVectorn_);
+}
+
+int main(int argc, char** argv) {
+  if (argc < 4) { fprintf(stderr, "usage: %s MODE JOB OUT ...\n", argv[0]); return 2; }
+  std::string mode = argv[1];
+  int dummy_argc = 1;
+  MPI_Init(&dummy_argc, &argv);
+
+  /* Parse exactly as main does, src/mithra.cpp:48-75. */
+  std::list<std::string> jobFile = read_file(argv[2]);
+  cleanJobFile(jobFile);
+  Mesh mesh; mesh.initialize();
+  Bunch bunch; Seed seed;
+  std::vector<Undulator> undulator; std::vector<ExtField> extField; std::vector<FreeElectronLaser> FEL;
+  ParseDarius parser(jobFile, mesh, bunch, seed, undulator, extField, FEL);
+  parser.setJobParameters();
+
+  Solver* s;
+  if (mesh.spaceCharge_) s = new FdTdSC(mesh, bunch, seed, undulator, extField, FEL);
+  else s = new FdTd(mesh, bunch, seed, undulator, extField, FEL);
+  s->initialize();
+
+  if (mode == "init") {
+    pre_loop(s);
+    dump_state(s, argv[3]);
+  } else if (mode == "run") {
+    int nsteps = atoi(argv[3]);
+    std::string out = argv[4];
+    int every = argc > 5 ? atoi(argv[5]) : nsteps;
+    mkdir(out.c_str(), 0755);
+    pre_loop(s);
+    dump_state(s, jp(out, "step0"));
+    FILE* pw = fopen(jp(out, "power.bin").c_str(), "wb");
+    for (int n = 1; n <= nsteps; n++) {
+      field_step(s, pw);
+      if (n % every == 0 || n == nsteps) dump_state(s, jp(out, "step" + std::to_string(n)));
+    }
+    fclose(pw);
+  } else if (mode == "field") {
+    std::string in = argv[3], out = argv[4];
+    mkdir(out.c_str(), 0755);
+    load_vec3(jp(in, "an.bin"), s->an_);
+    load_vec3(jp(in, "anm1.bin"), s->anm1_);
+    load_vec3(jp(in, "anp1.bin"), s->anp1_);
+    if (mesh.spaceCharge_) {
+      load_scalar_field(jp(in, "fn.bin"), s->fn_);
+      load_scalar_field(jp(in, "fnm1.bin"), s->fnm1_);
+      load_scalar_field(jp(in, "fnp1.bin"), s->fnp1_);
+    }
+    s->fieldUpdate();
+    for (int k = 2; k < s->np_ - 2; k++)
+      for (int i = 1; i < s->N0_ - 1; i++)
+        for (int j = 1; j < s->N1_ - 1; j++) s->fieldEvaluate((long)s->N1N0_ * k + s->N1_ * i + j);
+    dump_vec3(jp(out, "anp1.bin"), s->anp1_);
+    if (mesh.spaceCharge_) dump_scalar_field(jp(out, "fnp1.bin"), s->fnp1_);
+    write_raw(jp(out, "en.bin"), s->en_.data(), s->en_.size() * 12);
+    write_raw(jp(out, "bn.bin"), s->bn_.data(), s->bn_.size() * 12);
+  } else if (mode == "push") {
+    std::string in = argv[3], out = argv[4];
+    mkdir(out.c_str(), 0755);
+    load_vec3(jp(in, "an.bin"), s->an_);
+    load_vec3(jp(in, "anp1.bin"), s->anp1_);
+    if (mesh.spaceCharge_) load_scalar_field(jp(in, "fn.bin"), s->fn_);
+    load_particles(jp(in, "particles.bin"), s->chargeVectorn_);
+    std::vector<char> tb = read_raw(jp(in, "timebunch.bin"));
+    memcpy(&s->timeBunch_, tb.data(), 8);
+    std::fill(s->pic_.begin(), s->pic_.end(), false);
+    s->bunchUpdate();
+    dump_particles(jp(out, "particles.bin"), s->chargeVectorn_);
+  } else if (mode == "deposit") {
+    std::string in = argv[3], out = argv[4];
+    mkdir(out.c_str(), 0755);
+    load_particles(jp(in, "particles.bin"), s->chargeVectorn_);
+    s->currentReset();
+    s->currentUpdate();
+    dump_vec3(jp(out, "anp1.bin"), s->anp1_);
+    if (mesh.spaceCharge_) dump_scalar_field(jp(out, "fnp1.bin"), s->fnp1_);
+    s->currentCommunicate();
+    dump_particles(jp(out, "particles.bin"), s->chargeVectorn_);
+  } else if (mode == "power") {
+    std::string in = argv[3], out = argv[4];
+    int K = atoi(argv[5]);
+    mkdir(out.c_str(), 0755);
+    FILE* pw = fopen(jp(out, "power.bin").c_str(), "wb");
+    for (int t = 0; t < K; t++) {
+      load_vec3(jp(in, "an_" + std::to_string(t) + ".bin"), s->an_);
+      load_vec3(jp(in, "anp1_" + std::to_string(t) + ".bin"), s->anp1_);
+      std::fill(s->pic_.begin(), s->pic_.end(), false);
+      s->powerSample();
+      for (size_t jf = 0; jf < s->FEL_.size(); jf++) {
+        if (!s->FEL_[jf].radiationPower_.sampling_) continue;
+        fwrite(s->rp_[jf].pG.data(), 8, s->rp_[jf].pG.size(), pw);
+      }
+      ++s->nTime_;
+    }
+    fclose(pw);
+  } else {
+    fprintf(stderr, "unknown mode %s\n", mode.c_str());
+    return 2;
+  }
+  MPI_Finalize();
+  return 0;
+}
