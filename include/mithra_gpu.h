@@ -1,0 +1,195 @@
+/*
+ * mithra_gpu.h : C ABI of the GB300 FdTd/FdTdSC time-marching library (libmithra_gb300.so).
+ *
+ * The reference selects its solver at src/mithra.cpp:86-93 and drives it through the virtual
+ * interface of MITHRA::Solver (src/solver.h:139-178) plus the non-virtual Solver::solve and
+ * Solver::bunchUpdate (src/solver.h:75-78).  This ABI is what that interface needs from a
+ * device: an opaque context that owns all device memory, entry points for each stage of one
+ * field step, and a fused multi-step march.  Plain pointers and sizes only; no C++ types cross
+ * it and no pointer passed in is retained after a call returns.
+ *
+ * Host buffers use the reference's own layouts:
+ *   vector fields : N1N0*N2 records of 3 doubles, node m = N1N0*k + N1*i + j (src/solver.cpp:674)
+ *   E and B       : N1N0*N2 records of 3 floats (src/solver.h:244-245)
+ *   particles     : records of 11 doubles  q, rnp[3], rnm[3], gb[3], e  (src/stdinclude.h:130-144,
+ *                   the MPI_CHARGE datatype of src/solver.cpp:55)
+ *
+ * Every call returns MITHRA_OK (0) or a negative status; mithra_gpu_last_error() gives the text.
+ * A context is used by one host thread at a time and owns one CUDA stream.
+ */
+#ifndef MITHRA_GPU_H
+#define MITHRA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MITHRA_OK 0
+#define MITHRA_ERR_ARG (-1)        /* invalid argument or size */
+#define MITHRA_ERR_CUDA (-2)       /* CUDA runtime failure */
+#define MITHRA_ERR_CAPACITY (-3)   /* particle capacity exceeded */
+#define MITHRA_ERR_STATE (-4)      /* call out of order (e.g. no particles uploaded) */
+#define MITHRA_ERR_NONFINITE (-5)  /* NaN or Inf detected in the state */
+#define MITHRA_ERR_PARSE (-6)      /* job file could not be parsed */
+
+#define MITHRA_PRECISION_FP64 0    /* plain form: FP64 throughout, E/B stored as float */
+#define MITHRA_PRECISION_FP32 1    /* mixed form: FP32 fields/particles, FP64 phase and frames */
+
+#define MITHRA_MAX_UNDULATORS 64
+#define MITHRA_MAX_POWER_OUTPUTS 8
+
+typedef struct mithra_ctx mithra_ctx;
+
+/* Mesh, solver and field-update coefficients: the values Solver::initializeMesh and
+ * Solver::initializeField compute (src/solver.cpp:601-842). */
+typedef struct {
+  int32_t N0, N1, N2;          /* nodes along x, y, z */
+  int32_t solver;              /* 0 = FD, 1 = NSFD (src/stdinclude.h:40) */
+  int32_t truncation_order;    /* Mur order, 1 or 2 */
+  int32_t space_charge;        /* 1 selects the FdTdSC path */
+  double a[6];                 /* uf_.a */
+  double nsfd_alpha, nsfd_beta;/* uf_.af.alpha_, uf_.af.beta_ */
+  double bB[5], cB[5], dB[5];  /* Mur face coefficients */
+  double eE[5], fE[5], gE[5];  /* Mur edge coefficients */
+  double hC[17];               /* Mur corner coefficients */
+  double dt, dx, dy, dz;       /* field time step and boosted mesh resolution */
+  double xmin, xmax, ymin, ymax, zmin, zmax;
+  double zp0, zp1;             /* z range owned by the (single) domain, src/solver.cpp:676-683 */
+  double Lz;                   /* boosted mesh length along z */
+} mithra_grid_desc;
+
+/* Particle-update constants: Solver::initializeBunchUpdate and the frame parameters
+ * (src/solver.cpp:1050-1059, :191-213, :322). */
+typedef struct {
+  double dtb;                  /* ub_.dtb = c0 * bunch time step */
+  double bunch_time_step;      /* bunch_.timeStep_ (the timeBunch increment) */
+  double r1, r2;               /* ub_.r1, ub_.r2 */
+  double gamma, beta, c0;      /* moving-frame gamma_, beta_, c0_ */
+  double dt_shift;             /* dt_ */
+  double n_update_bunch;       /* nUpdateBunch_ (the substep loop runs while t < this) */
+} mithra_push_desc;
+
+/* One undulator module after Solver::setSimulationParameters (sorted, rb shifted). */
+typedef struct {
+  int32_t type;                /* 0 static, 1 optical */
+  double k, lu, rb, length, dist, theta;
+} mithra_undulator_desc;
+
+/* One radiation-power output (src/radiation.cpp:18-121). */
+typedef struct {
+  int32_t N;                   /* sampling planes */
+  int32_t Nl;                  /* frequencies */
+  int32_t Nf;                  /* DFT length (ring slots) */
+  double pc;                   /* power constant */
+  const double* z;             /* N boosted plane positions */
+  const double* twiddle_re;    /* Nl*Nf values cos(w_l * j * dt) */
+  const double* twiddle_im;    /* Nl*Nf values sin(w_l * j * dt) */
+} mithra_power_desc;
+
+/* Time state of Solver (src/solver.h:253-268). */
+typedef struct {
+  double time, time_bunch;
+  int64_t n_time, n_time_bunch;
+} mithra_time_state;
+
+/* ---- context ---------------------------------------------------------------------------- */
+
+/* Replaces `new FdTd(...)` / `new FdTdSC(...)` (src/mithra.cpp:86-90) once the host has run the
+ * reference's initialisation.  `particle_capacity` bounds the particle count including the
+ * copies the single-domain z-face exchange appends (src/solver.cpp:1551-1568). */
+int mithra_gpu_create(const mithra_grid_desc* grid, const mithra_push_desc* push, int precision,
+                      int device, size_t particle_capacity, mithra_ctx** out);
+int mithra_gpu_destroy(mithra_ctx* ctx);
+int mithra_gpu_last_error(const mithra_ctx* ctx, char* buf, size_t len);
+int mithra_gpu_synchronize(mithra_ctx* ctx);
+
+/* Undulator modules, replacing the parsed std::vector<Undulator> (src/solver.h:224). */
+int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und, int n);
+/* Radiation-power outputs, replacing Solver::initializePowerSample's rp_ (src/radiation.cpp:18-121). */
+int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outputs, int n);
+
+/* ---- state transfer --------------------------------------------------------------------- */
+
+/* Fields anp1_ (which holds J between steps), an_, anm1_ (src/solver.h:231-233); any may be NULL. */
+int mithra_gpu_upload_fields(mithra_ctx* ctx, const double* anp1, const double* an, const double* anm1);
+int mithra_gpu_download_fields(mithra_ctx* ctx, double* anp1, double* an, double* anm1);
+/* Scalar potential fnp1_ (rho between steps), fn_, fnm1_ (src/solver.h:236-238), FdTdSC only. */
+int mithra_gpu_upload_scalar(mithra_ctx* ctx, const double* fnp1, const double* fn, const double* fnm1);
+int mithra_gpu_download_scalar(mithra_ctx* ctx, double* fnp1, double* fn, double* fnm1);
+/* E and B as evaluated by the last field step (src/solver.h:244-245). */
+int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn);
+/* chargeVectorn_ (src/solver.h:271) as 11-double records. */
+int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n);
+int mithra_gpu_download_particles(mithra_ctx* ctx, double* rec, size_t cap, size_t* n);
+int mithra_gpu_particle_count(mithra_ctx* ctx, size_t* n);
+int mithra_gpu_set_time(mithra_ctx* ctx, const mithra_time_state* t);
+int mithra_gpu_get_time(mithra_ctx* ctx, mithra_time_state* t);
+
+/* ---- stages of one field step (each replaces one reference member function) ------------- */
+
+/* FdTd::fieldUpdate / FdTdSC::fieldUpdate without the MPI halo, plus the eager equivalent of
+ * the lazy FdTd::fieldEvaluate (src/fdtd.cpp:231-800, :818-845). */
+int mithra_gpu_field_update(mithra_ctx* ctx);
+/* `rnm = rnp` for all particles (src/solver.cpp:1311-1312). */
+int mithra_gpu_save_positions(mithra_ctx* ctx);
+/* One Solver::bunchUpdate (src/solver.cpp:1424-1576) followed by timeBunch_ += bunch time step
+ * and ++nTimeBunch_ (src/solver.cpp:1319-1320). */
+int mithra_gpu_bunch_update(mithra_ctx* ctx);
+/* Solver::recycleParticles (src/solver.cpp:493-503). */
+int mithra_gpu_recycle(mithra_ctx* ctx);
+/* Solver::powerSample (src/radiation.cpp:127-232); the row is appended to the device row log. */
+int mithra_gpu_power_sample(mithra_ctx* ctx);
+/* FdTd::fieldShift (src/fdtd.cpp:806-812). */
+int mithra_gpu_field_shift(mithra_ctx* ctx);
+/* FdTd::currentReset + currentUpdate + currentCommunicate (src/fdtd.cpp:23-225). */
+int mithra_gpu_current_update(mithra_ctx* ctx);
+/* time_ += dt, ++nTime_ (src/solver.cpp:1396-1399). */
+int mithra_gpu_advance_time(mithra_ctx* ctx);
+
+/* ---- fused march ------------------------------------------------------------------------ */
+
+/* `nsteps` iterations of the body of Solver::solve's main loop (src/solver.cpp:1300-1414),
+ * replayed from CUDA graphs with no host synchronisation between steps. */
+int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps);
+/* The negative-time particle loop of Solver::solve (src/solver.cpp:1232-1291): field-free
+ * substeps while time_ < 0. */
+int mithra_gpu_run_prelude(mithra_ctx* ctx);
+
+/* Power rows recorded since the last call (or since creation): for each row and output, per
+ * plane the lab-frame z followed by Nl powers, as written to power-sampling files
+ * (src/radiation.cpp:222-229).  `*n_values` returns the number of doubles written. */
+int mithra_gpu_power_rows(mithra_ctx* ctx, double* out, size_t cap_values, size_t* n_values);
+
+/* Per-kernel device time accumulated since the last reset (CUDA events on the context stream).
+ * names/ms are filled for up to `cap` kernels; returns the count through *n. */
+int mithra_gpu_kernel_times(mithra_ctx* ctx, char* names, size_t name_len, double* ms, int cap, int* n);
+int mithra_gpu_enable_timing(mithra_ctx* ctx, int on);
+
+/* ---- job-file level entry points (host initialisation of the reference, then a context) --- */
+
+/* Parses a MITHRA job file (src/readdata.cpp:10-53, src/datainput.cpp:18-751) and runs the
+ * reference's FP64 initialisation (Solver::initialize, src/solver.cpp:547-595) on the host.
+ * The setup object holds the descriptors above, the initial fields and the particles. */
+typedef struct mithra_setup mithra_setup;
+int mithra_setup_from_job(const char* job_path, mithra_setup** out, char* err, size_t err_len);
+int mithra_setup_destroy(mithra_setup* s);
+int mithra_setup_grid(const mithra_setup* s, mithra_grid_desc* grid);
+int mithra_setup_push(const mithra_setup* s, mithra_push_desc* push);
+int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, int cap, int* n);
+int mithra_setup_time(const mithra_setup* s, mithra_time_state* t);
+int mithra_setup_particles(const mithra_setup* s, double* rec, size_t cap, size_t* n);
+int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double* anm1);
+int mithra_setup_total_time(const mithra_setup* s, double* total_time);
+/* Writes `key value` lines (the derived scalars of the initialisation) into buf. */
+int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed);
+/* Creates a context from a setup and uploads its state; the power outputs are configured. */
+int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int device,
+                                 double capacity_factor, mithra_ctx** out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,448 @@
+"""GB300-native FdTd/FdTdSC time-marching loop of MITHRA.
+
+The compute path is libmithra_gb300.so (hand-written sm_103a CUDA kernels behind the C ABI of
+include/mithra_gpu.h).  This module binds that ABI with ctypes and mirrors the reference's
+solver interface (src/solver.h:20-345, src/fdtd.h:15-66):
+
+    job = Setup.from_job("run.job")            # parse + FP64 initialisation (host)
+    s = FdTd(job)                              # `new FdTd(...)`, src/mithra.cpp:86-90
+    s.solve()                                  # Solver::solve, src/solver.cpp:1212-1418
+
+Importing never falls back to a CPU implementation: if the library is missing it is built
+with nvcc, and if that is impossible the import raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+__all__ = ["Setup", "Context", "FdTd", "FdTdSC", "MithraError", "lib", "FP64", "FP32"]
+
+FP64 = 0
+FP32 = 1
+MAX_UND = 64
+
+
+class MithraError(RuntimeError):
+    pass
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("N0", C.c_int32), ("N1", C.c_int32), ("N2", C.c_int32), ("solver", C.c_int32),
+                ("truncation_order", C.c_int32), ("space_charge", C.c_int32),
+                ("a", C.c_double * 6), ("nsfd_alpha", C.c_double), ("nsfd_beta", C.c_double),
+                ("bB", C.c_double * 5), ("cB", C.c_double * 5), ("dB", C.c_double * 5),
+                ("eE", C.c_double * 5), ("fE", C.c_double * 5), ("gE", C.c_double * 5),
+                ("hC", C.c_double * 17),
+                ("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("xmin", C.c_double), ("xmax", C.c_double), ("ymin", C.c_double), ("ymax", C.c_double),
+                ("zmin", C.c_double), ("zmax", C.c_double), ("zp0", C.c_double), ("zp1", C.c_double),
+                ("Lz", C.c_double)]
+
+
+class PushDesc(C.Structure):
+    _fields_ = [("dtb", C.c_double), ("bunch_time_step", C.c_double), ("r1", C.c_double), ("r2", C.c_double),
+                ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double), ("dt_shift", C.c_double),
+                ("n_update_bunch", C.c_double)]
+
+
+class UndulatorDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("k", C.c_double), ("lu", C.c_double), ("rb", C.c_double),
+                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double)]
+
+
+class PowerDesc(C.Structure):
+    _fields_ = [("N", C.c_int32), ("Nl", C.c_int32), ("Nf", C.c_int32), ("pc", C.c_double),
+                ("z", C.POINTER(C.c_double)), ("twiddle_re", C.POINTER(C.c_double)),
+                ("twiddle_im", C.POINTER(C.c_double))]
+
+
+class TimeState(C.Structure):
+    _fields_ = [("time", C.c_double), ("time_bunch", C.c_double), ("n_time", C.c_int64),
+                ("n_time_bunch", C.c_int64)]
+
+
+_lib = None
+_P = C.POINTER
+_dp, _fp, _vp = _P(C.c_double), _P(C.c_float), C.c_void_p
+
+_SIGS = {
+    "mithra_gpu_create": [_P(GridDesc), _P(PushDesc), C.c_int, C.c_int, C.c_size_t, _P(_vp)],
+    "mithra_gpu_destroy": [_vp],
+    "mithra_gpu_last_error": [_vp, C.c_char_p, C.c_size_t],
+    "mithra_gpu_synchronize": [_vp],
+    "mithra_gpu_set_undulators": [_vp, _P(UndulatorDesc), C.c_int],
+    "mithra_gpu_set_power": [_vp, _P(PowerDesc), C.c_int],
+    "mithra_gpu_upload_fields": [_vp, _dp, _dp, _dp],
+    "mithra_gpu_download_fields": [_vp, _dp, _dp, _dp],
+    "mithra_gpu_upload_scalar": [_vp, _dp, _dp, _dp],
+    "mithra_gpu_download_scalar": [_vp, _dp, _dp, _dp],
+    "mithra_gpu_download_eb": [_vp, _fp, _fp],
+    "mithra_gpu_upload_particles": [_vp, _dp, C.c_size_t],
+    "mithra_gpu_download_particles": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
+    "mithra_gpu_particle_count": [_vp, _P(C.c_size_t)],
+    "mithra_gpu_set_time": [_vp, _P(TimeState)],
+    "mithra_gpu_get_time": [_vp, _P(TimeState)],
+    "mithra_gpu_field_update": [_vp],
+    "mithra_gpu_save_positions": [_vp],
+    "mithra_gpu_bunch_update": [_vp],
+    "mithra_gpu_recycle": [_vp],
+    "mithra_gpu_power_sample": [_vp],
+    "mithra_gpu_field_shift": [_vp],
+    "mithra_gpu_current_update": [_vp],
+    "mithra_gpu_advance_time": [_vp],
+    "mithra_gpu_run": [_vp, C.c_int64],
+    "mithra_gpu_run_prelude": [_vp],
+    "mithra_gpu_power_rows": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
+    "mithra_gpu_kernel_times": [_vp, C.c_char_p, C.c_size_t, _dp, C.c_int, _P(C.c_int)],
+    "mithra_gpu_enable_timing": [_vp, C.c_int],
+    "mithra_setup_from_job": [C.c_char_p, _P(_vp), C.c_char_p, C.c_size_t],
+    "mithra_setup_destroy": [_vp],
+    "mithra_setup_grid": [_vp, _P(GridDesc)],
+    "mithra_setup_push": [_vp, _P(PushDesc)],
+    "mithra_setup_undulators": [_vp, _P(UndulatorDesc), C.c_int, _P(C.c_int)],
+    "mithra_setup_time": [_vp, _P(TimeState)],
+    "mithra_setup_particles": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_fields": [_vp, _dp, _dp, _dp],
+    "mithra_setup_total_time": [_vp, _dp],
+    "mithra_setup_meta": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_gpu_create_from_setup": [_vp, C.c_int, C.c_int, C.c_double, _P(_vp)],
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Loads libmithra_gb300.so, building it first when it is absent or stale."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = C.CDLL(path)
+        for name, args in _SIGS.items():
+            fn = getattr(_lib, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+    return _lib
+
+
+def dptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous, "float64 C-contiguous array expected"
+    return a.ctypes.data_as(_dp)
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous, "float32 C-contiguous array expected"
+    return a.ctypes.data_as(_fp)
+
+
+class Setup:
+    """Parsed job plus the reference's FP64 host initialisation (Solver::initialize)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_job(cls, path: str) -> "Setup":
+        h = _vp()
+        err = C.create_string_buffer(1024)
+        r = lib().mithra_setup_from_job(os.fsencode(path), C.byref(h), err, len(err))
+        if r != 0:
+            raise MithraError("job %s: %s (status %d)" % (path, err.value.decode(errors="replace"), r))
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mithra_setup_destroy(self._h)
+            self._h = None
+
+    def grid(self) -> GridDesc:
+        g = GridDesc()
+        lib().mithra_setup_grid(self._h, C.byref(g))
+        return g
+
+    def push(self) -> PushDesc:
+        p = PushDesc()
+        lib().mithra_setup_push(self._h, C.byref(p))
+        return p
+
+    def undulators(self):
+        arr = (UndulatorDesc * MAX_UND)()
+        n = C.c_int()
+        lib().mithra_setup_undulators(self._h, arr, MAX_UND, C.byref(n))
+        return [arr[i] for i in range(n.value)]
+
+    def time(self) -> TimeState:
+        t = TimeState()
+        lib().mithra_setup_time(self._h, C.byref(t))
+        return t
+
+    def total_time(self) -> float:
+        v = C.c_double()
+        lib().mithra_setup_total_time(self._h, C.byref(v))
+        return v.value
+
+    def particles(self) -> np.ndarray:
+        n = C.c_size_t()
+        lib().mithra_setup_particles(self._h, None, 0, C.byref(n))
+        out = np.zeros((n.value, 11))
+        lib().mithra_setup_particles(self._h, dptr(out), n.value, C.byref(n))
+        return out
+
+    def fields(self):
+        g = self.grid()
+        n = g.N0 * g.N1 * g.N2 * 3
+        anp1, an, anm1 = np.zeros(n), np.zeros(n), np.zeros(n)
+        lib().mithra_setup_fields(self._h, dptr(anp1), dptr(an), dptr(anm1))
+        return anp1, an, anm1
+
+    def meta(self) -> dict:
+        need = C.c_size_t()
+        lib().mithra_setup_meta(self._h, None, 0, C.byref(need))
+        buf = C.create_string_buffer(need.value)
+        lib().mithra_setup_meta(self._h, buf, need.value, C.byref(need))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            k, v = line.split()
+            out[k] = float(v)
+        return out
+
+
+class Context:
+    """One GPU domain: owns every device buffer of a FdTd/FdTdSC solve."""
+
+    def __init__(self, handle, grid: GridDesc):
+        self._h = handle
+        self.grid = grid
+        self.nodes = grid.N0 * grid.N1 * grid.N2
+
+    @classmethod
+    def create(cls, grid: GridDesc, push: PushDesc, precision: int = FP64, device: int = 0,
+               capacity: int = 1 << 20) -> "Context":
+        h = _vp()
+        r = lib().mithra_gpu_create(C.byref(grid), C.byref(push), precision, device, capacity, C.byref(h))
+        if r != 0:
+            raise MithraError("mithra_gpu_create failed with status %d" % r)
+        return cls(h, grid)
+
+    @classmethod
+    def from_setup(cls, setup: Setup, precision: int = FP64, device: int = 0,
+                   capacity_factor: float = 1.25) -> "Context":
+        h = _vp()
+        r = lib().mithra_gpu_create_from_setup(setup._h, precision, device, capacity_factor, C.byref(h))
+        if r != 0:
+            raise MithraError("mithra_gpu_create_from_setup failed with status %d" % r)
+        return cls(h, setup.grid())
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.mithra_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _ck(self, r, what):
+        if r != 0:
+            buf = C.create_string_buffer(1024)
+            lib().mithra_gpu_last_error(self._h, buf, len(buf))
+            raise MithraError("%s: %s (status %d)" % (what, buf.value.decode(errors="replace"), r))
+
+    def call(self, name, *args):
+        self._ck(getattr(lib(), name)(self._h, *args), name)
+
+    def set_undulators(self, und):
+        arr = (UndulatorDesc * max(1, len(und)))(*und)
+        self.call("mithra_gpu_set_undulators", arr, len(und))
+
+    def set_power(self, outputs):
+        """outputs: list of dicts with N, Nl, Nf, pc, z, tw_re, tw_im (numpy float64)."""
+        self._power_keep = []
+        descs = (PowerDesc * max(1, len(outputs)))()
+        for i, o in enumerate(outputs):
+            z = np.ascontiguousarray(o["z"], dtype=np.float64)
+            re = np.ascontiguousarray(o["tw_re"], dtype=np.float64)
+            im = np.ascontiguousarray(o["tw_im"], dtype=np.float64)
+            self._power_keep += [z, re, im]
+            descs[i] = PowerDesc(int(o["N"]), int(o["Nl"]), int(o["Nf"]), float(o["pc"]), dptr(z), dptr(re), dptr(im))
+        self.call("mithra_gpu_set_power", descs, len(outputs))
+
+    def upload_fields(self, anp1=None, an=None, anm1=None):
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        a, b, c = conv(anp1), conv(an), conv(anm1)
+        self.call("mithra_gpu_upload_fields", dptr(a), dptr(b), dptr(c))
+
+    def download_fields(self):
+        n = self.nodes * 3
+        anp1, an, anm1 = np.empty(n), np.empty(n), np.empty(n)
+        self.call("mithra_gpu_download_fields", dptr(anp1), dptr(an), dptr(anm1))
+        return anp1, an, anm1
+
+    def upload_scalar(self, fnp1=None, fn=None, fnm1=None):
+        conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+        self.call("mithra_gpu_upload_scalar", dptr(conv(fnp1)), dptr(conv(fn)), dptr(conv(fnm1)))
+
+    def download_scalar(self):
+        n = self.nodes
+        a, b, c = np.empty(n), np.empty(n), np.empty(n)
+        self.call("mithra_gpu_download_scalar", dptr(a), dptr(b), dptr(c))
+        return a, b, c
+
+    def download_eb(self):
+        en = np.empty(self.nodes * 3, dtype=np.float32)
+        bn = np.empty(self.nodes * 3, dtype=np.float32)
+        self.call("mithra_gpu_download_eb", fptr(en), fptr(bn))
+        return en, bn
+
+    def upload_particles(self, rec):
+        rec = np.ascontiguousarray(rec, dtype=np.float64).reshape(-1, 11)
+        self.call("mithra_gpu_upload_particles", dptr(rec), rec.shape[0])
+
+    def particle_count(self) -> int:
+        n = C.c_size_t()
+        self.call("mithra_gpu_particle_count", C.byref(n))
+        return n.value
+
+    def download_particles(self) -> np.ndarray:
+        cap = self.particle_count()
+        out = np.zeros((max(cap, 1), 11))
+        n = C.c_size_t()
+        self.call("mithra_gpu_download_particles", dptr(out), cap, C.byref(n))
+        return out[: n.value]
+
+    def set_time(self, t: TimeState):
+        self.call("mithra_gpu_set_time", C.byref(t))
+
+    def get_time(self) -> TimeState:
+        t = TimeState()
+        self.call("mithra_gpu_get_time", C.byref(t))
+        return t
+
+    def power_rows(self) -> np.ndarray:
+        n = C.c_size_t()
+        self.call("mithra_gpu_power_rows", None, 0, C.byref(n))
+        out = np.zeros(n.value)
+        self.call("mithra_gpu_power_rows", dptr(out), n.value, C.byref(n))
+        return out
+
+    def enable_timing(self, on: bool = True):
+        self.call("mithra_gpu_enable_timing", 1 if on else 0)
+
+    def kernel_times(self) -> dict:
+        n = C.c_int()
+        self.call("mithra_gpu_kernel_times", None, 0, None, 0, C.byref(n))
+        cnt = n.value
+        names = C.create_string_buffer(64 * max(cnt, 1))
+        ms = np.zeros(2 * max(cnt, 1))
+        self.call("mithra_gpu_kernel_times", names, 64, dptr(ms), cnt, C.byref(n))
+        out = {}
+        for i in range(cnt):
+            nm = names.raw[64 * i: 64 * (i + 1)].split(b"\0", 1)[0].decode()
+            out[nm] = (ms[2 * i], int(ms[2 * i + 1]))
+        return out
+
+    # Stages, one per reference member function.
+    def field_update(self):
+        self.call("mithra_gpu_field_update")
+
+    def save_positions(self):
+        self.call("mithra_gpu_save_positions")
+
+    def bunch_update(self):
+        self.call("mithra_gpu_bunch_update")
+
+    def recycle(self):
+        self.call("mithra_gpu_recycle")
+
+    def power_sample(self):
+        self.call("mithra_gpu_power_sample")
+
+    def field_shift(self):
+        self.call("mithra_gpu_field_shift")
+
+    def current_update(self):
+        self.call("mithra_gpu_current_update")
+
+    def advance_time(self):
+        self.call("mithra_gpu_advance_time")
+
+    def run(self, nsteps: int):
+        self.call("mithra_gpu_run", int(nsteps))
+
+    def run_prelude(self):
+        self.call("mithra_gpu_run_prelude")
+
+    def synchronize(self):
+        self.call("mithra_gpu_synchronize")
+
+
+class FdTd:
+    """Drop-in for the reference's FdTd (src/fdtd.h:15-66) driven by a GPU context.
+
+    The member functions keep the reference's names; `solve()` marches to mesh.totalTime_ like
+    Solver::solve and returns the power rows (z_lab, P...) that the reference writes to its
+    power-sampling files."""
+
+    precision = FP64
+
+    def __init__(self, setup: Setup, precision: int | None = None, device: int = 0, capacity_factor: float = 1.25):
+        self.setup = setup
+        self.meta = setup.meta()
+        self.ctx = Context.from_setup(setup, self.precision if precision is None else precision, device, capacity_factor)
+
+    def currentReset(self):  # noqa: N802 - reference name
+        pass  # folded into currentUpdate, as the reference calls them back to back
+
+    def currentUpdate(self):  # noqa: N802
+        self.ctx.current_update()
+
+    def currentCommunicate(self):  # noqa: N802
+        pass  # one domain: nothing to exchange; the erasure is part of currentUpdate
+
+    def fieldUpdate(self):  # noqa: N802
+        self.ctx.field_update()
+
+    def fieldShift(self):  # noqa: N802
+        self.ctx.field_shift()
+
+    def bunchUpdate(self):  # noqa: N802
+        self.ctx.bunch_update()
+
+    def powerSample(self):  # noqa: N802
+        self.ctx.power_sample()
+
+    def steps_to_total_time(self) -> int:
+        t = self.ctx.get_time()
+        total = self.setup.total_time()
+        time, dt, n = t.time, self.meta["dt"], 0
+        while time < total:
+            time += dt
+            n += 1
+        return n
+
+    def solve(self, max_steps: int | None = None):
+        self.ctx.run_prelude()
+        n = self.steps_to_total_time()
+        if max_steps is not None:
+            n = min(n, max_steps)
+        self.ctx.run(n)
+        return self.ctx.power_rows()
+
+
+class FdTdSC(FdTd):
+    """Drop-in for FdTdSC (src/fdtdSC.h): the same loop with the scalar potential."""

@@ -1,0 +1,122 @@
+// Internal definition of the library context shared by the translation units of the CUDA part.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/mithra_gpu.h"
+#include "device_common.cuh"
+
+namespace mithra {
+
+struct PowerOut {
+  PowerDev dev{};
+  double *z = nullptr, *dzr = nullptr, *tw_re = nullptr, *tw_im = nullptr, *fdt = nullptr,
+         *partial = nullptr, *rows = nullptr;
+  int *plane_k = nullptr, *plane_slot = nullptr;
+};
+
+struct KernelTimer {
+  std::string name;
+  double ms = 0.0;
+  long long launches = 0;
+};
+
+// Device buffers of the mixed-precision form (allocated only when it is selected).
+struct Fp32State {
+  float* A[3] = {nullptr, nullptr, nullptr};
+  float* F[3] = {nullptr, nullptr, nullptr};
+  ParticlesF32 pt{};
+};
+
+}  // namespace mithra
+
+struct mithra_ctx {
+  int device = 0;
+  int precision = MITHRA_PRECISION_FP64;
+  cudaStream_t stream = nullptr;
+  mithra::GridDev g{};
+  mithra::PushDev P{};
+  mithra_grid_desc grid_desc{};
+  mithra_push_desc push_desc{};
+  std::vector<mithra::UndDev> und_host;
+  mithra::UndDev* und_dev = nullptr;
+  double* A[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of A (SoA)
+  double* F[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of phi
+  mithra::ParticlesDev<double> pt{};
+  mithra::Fp32State f32{};
+  float* E = nullptr;  // 3 components, cstride apart
+  float* B = nullptr;
+  int idx[3] = {0, 1, 2};  // buffer index of np1, n, nm1
+  size_t capacity = 0;
+  mithra::StateDev* st = nullptr;
+  mithra::StateDev* st_host = nullptr;  // pinned mirror
+  std::vector<mithra::PowerOut> power;
+  long long row_cap = 0;
+  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  bool timing = false;
+  std::vector<mithra::KernelTimer> timers;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  bool particles_loaded = false;
+  std::string err;
+  int sm_count = 152;
+  long long st_host_rows();
+};
+
+namespace mithra {
+
+int fail(mithra_ctx* c, int code, const char* fmt, ...);
+int grid_stride_blocks(const mithra_ctx* ctx, long long work, int block);
+int timer_begin(mithra_ctx* ctx, const char* name, int* slot, cudaEvent_t* a, cudaEvent_t* b);
+int timer_end(mithra_ctx* ctx, int slot, cudaEvent_t a, cudaEvent_t b);
+int harvest_timers(mithra_ctx* ctx);
+void invalidate_graphs(mithra_ctx* ctx);
+
+#define CK(call)                                                                                        \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess) return ::mithra::fail(ctx, MITHRA_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
+}
+
+inline long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+// Launches one kernel through `fn` on ctx->stream; in timing mode it is bracketed by CUDA
+// events recorded on the same stream and accumulated under `name`.
+template <typename Fn>
+int timed(mithra_ctx* ctx, const char* name, Fn fn) {
+  int slot = 0;
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (ctx->timing) {
+    int r = timer_begin(ctx, name, &slot, &a, &b);
+    if (r) return r;
+  }
+  fn();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "launch %s: %s", name, cudaGetErrorString(e));
+  if (ctx->timing) return timer_end(ctx, slot, a, b);
+  return MITHRA_OK;
+}
+
+// Mixed-precision form (fp32_form.cu).
+int fp32_alloc(mithra_ctx* ctx);
+void fp32_free(mithra_ctx* ctx);
+float* fp32_field(mithra_ctx* ctx, int level);   // level 0 = np1, 1 = n, 2 = nm1
+float* fp32_scalar(mithra_ctx* ctx, int level);
+int fp32_records_to_soa(mithra_ctx* ctx, const double* staging, long long n);
+int fp32_soa_to_records(mithra_ctx* ctx, double* staging, long long slots, long long* n_out);
+int fp32_field_update(mithra_ctx* ctx);
+int fp32_eval_eb(mithra_ctx* ctx);
+int fp32_push(mithra_ctx* ctx, int save_rnm);
+int fp32_save_positions(mithra_ctx* ctx);
+int fp32_erase(mithra_ctx* ctx);
+int fp32_current(mithra_ctx* ctx);
+
+}  // namespace mithra

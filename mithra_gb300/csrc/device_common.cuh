@@ -1,0 +1,132 @@
+// Shared device-side definitions of the GB300 FdTd library.
+//
+// Device layout (both precision forms):
+//   * every scalar field component is its own array of N2 planes of N0 rows of P1 values
+//     (P1 = N1 rounded up to a multiple of 8), node (k, i, j) at k*plane + i*P1 + j;
+//     the three components of A (and of E, B) are `cstride` apart.  SoA keeps each stencil
+//     load a coalesced row segment; the padded pitch keeps rows 16-byte aligned for vector
+//     and bulk-tensor copies.
+//   * particles are structure-of-arrays (position, momentum, previous position, charge, entry
+//     flag), plus a status byte (bit 0: erased) and a crossing byte written by the push.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mithra {
+
+constexpr int kMaxUndulators = 64;
+constexpr double kPI = 3.1415926535;  // src/stdinclude.h:43 (truncated value kept for parity)
+constexpr double kEM = 9.109e-31;     // src/stdinclude.h:51
+constexpr double kEC = 1.602e-19;     // src/stdinclude.h:50
+
+struct GridDev {
+  int N0, N1, N2, P1;
+  long long plane;    // N0 * P1
+  long long cstride;  // distance between components
+  int solver, order, space_charge;
+  double a[6];
+  double nsfd_alpha, nsfd_beta;
+  double bB[5], cB[5], dB[5], eE[5], fE[5], gE[5], hC[17];
+  double dt, dx, dy, dz;
+  double xmin, xmax, ymin, ymax, zmin, zmax, zp0, zp1, Lz;
+};
+
+__host__ __device__ inline long long node_index(const GridDev& g, int k, int i, int j) {
+  return (long long)k * g.plane + (long long)i * g.P1 + j;
+}
+
+struct UndDev {
+  int type;
+  double k, lu, rb, length, dist, theta;
+  // Per-module constants of Solver::undulatorField (src/solver.cpp:1805-1812), computed on
+  // the host with the reference's expressions so that they are bit-identical.
+  double b0, ku, ct, st, ul;  // ul = length * lu
+  double r0_prev, r0_next;    // gap to the previous / next module (src/beam.cc:35, :60)
+  int has_prev, has_next;
+};
+
+struct PushDev {
+  double dtb, r1, r2, gamma, beta, c0, dt_shift, bunch_time_step;
+  int n_und;
+  double und0_dist;
+};
+
+// Device-resident time and bookkeeping state of one context.  The kernels advance it
+// themselves so that a captured step graph can be replayed without host involvement.
+struct StateDev {
+  double time, time_bunch;
+  long long n_time, n_time_bunch;
+  long long n_particles;     // particle slots in use (erased ones included)
+  long long capacity;
+  unsigned long long n_cross;       // particles that crossed a z face in the last substep
+  unsigned long long n_transverse;  // particles outside the transverse domain (diagnostic)
+  int overflow;                     // set when appended copies would exceed the capacity
+  int nonfinite;
+  long long n_power_rows;
+  long long power_row_cap;
+};
+
+template <typename T>
+struct ParticlesDev {
+  T *x, *y, *z;        // rnp
+  T *gx, *gy, *gz;     // gb
+  T *mx, *my, *mz;     // rnm
+  T *q, *e;
+  uint8_t* status;     // bit 0: erased
+  int8_t* cross;       // 0 none, 1 below zp0, 2 at/above zp1
+};
+
+// Particles of the mixed-precision form: integer cell coordinates packed into one 64-bit word
+// (21 bits per axis, biased by 2^20, so positions far outside the mesh stay representable), the
+// FP32 offset inside the cell in units of the cell size, FP32 gamma*beta.  The previous position
+// is kept in the same form for the deposit.
+struct ParticlesF32 {
+  long long* cell;
+  float *fx, *fy, *fz;
+  float *gx, *gy, *gz;
+  long long* mcell;
+  float *mfx, *mfy, *mfz;
+  float* q;
+  uint8_t* e;
+  uint8_t* status;
+  int8_t* cross;
+};
+
+constexpr long long kCellBias = 1LL << 20;
+__host__ __device__ __forceinline__ long long pack_cell(int i, int j, int k) {
+  return ((long long)(i + kCellBias) << 42) | ((long long)(j + kCellBias) << 21) | (long long)(k + kCellBias);
+}
+__host__ __device__ __forceinline__ void unpack_cell(long long c, int& i, int& j, int& k) {
+  i = (int)((c >> 42) & 0x1FFFFF) - (int)kCellBias;
+  j = (int)((c >> 21) & 0x1FFFFF) - (int)kCellBias;
+  k = (int)(c & 0x1FFFFF) - (int)kCellBias;
+}
+
+// One radiation-power output on the device (see power_kernels.cuh).
+struct PowerDev {
+  int N, Nl, Nf;
+  int nz;                   // planes owned by this domain
+  double pc;                // power constant (src/radiation.cpp:106)
+  double gamma, beta, c0, dt_shift;
+  const double* z;          // N boosted plane positions
+  const int* plane_k;       // N: cell index of the plane, or -1 when outside [zp0, zp1)
+  const double* plane_dzr;  // N: fractional position inside that cell
+  const int* plane_slot;    // N: compressed index kz of each owned plane
+  const double* tw_re;      // Nl*Nf twiddles cos(w_l j dt)
+  const double* tw_im;      // Nl*Nf twiddles sin(w_l j dt)
+  double* fdt;              // ring buffer: Nf slots x 4 values x nz planes x nodes
+  double* partial;          // (blocks) x Nl
+  double* rows;             // row log: row_cap rows of N*(1+Nl) doubles
+  int nodes_i, nodes_j;     // N0-4, N1-4
+  int blocks_per_plane;
+  long long row_cap;
+};
+
+// pmod, src/stdinclude.cpp:88-93.
+__device__ __forceinline__ double pmod_d(double a, double b) {
+  double x = fmod(a, b);
+  x += (x < 0.0) ? b : 0.0;
+  return x;
+}
+
+}  // namespace mithra

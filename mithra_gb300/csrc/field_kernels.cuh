@@ -1,0 +1,255 @@
+// Field kernels: the leapfrog potential update with Mur absorbing boundaries and the E/B
+// evaluation, for one rank that owns the whole z range.
+//
+// Dependency order inside one FdTd::fieldUpdate (src/fdtd.cpp:231-725): interior nodes
+// (J/rho read in place from anp1/fnp1), then the six faces (which read interior anp1), then
+// the twelve edges (which read face anp1), then the eight corners (which read edge anp1).
+// Each stage is one launch; within a stage every node is independent.
+#pragma once
+#include "device_common.cuh"
+
+namespace mithra {
+
+template <typename T>
+struct PotentialArgs {
+  T* np1;        // anp1 (holds J on entry) or fnp1 (holds rho)
+  const T* n;    // an / fn
+  const T* nm1;  // anm1 / fnm1
+  int ncomp;     // 3 for A, 1 for phi
+  double asrc;   // a[4] for J, a[5] for rho
+};
+
+// Interior update, AdvanceField::advanceMagneticPotentialFD/NSFD and the scalar variants
+// (src/database.cpp:44-134) called from src/fdtd.cpp:270-303.  One thread per node, looping
+// over the components; FP64 FMAs are allowed (the result agrees with the reference to a few
+// ulp per step).
+template <typename T, bool NSFD>
+__global__ void __launch_bounds__(256) k_potential_interior(GridDev g, PotentialArgs<T> p) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + 1;
+  if (j > g.N1 - 2 || i > g.N0 - 2) return;
+  const long long m = node_index(g, k, i, j);
+  const long long sI = g.P1, sK = g.plane;
+  const T a0 = (T)g.a[0], a1 = (T)g.a[1], a2 = (T)g.a[2], a3 = (T)g.a[3], as = (T)p.asrc;
+  for (int c = 0; c < p.ncomp; c++) {
+    const T* an = p.n + c * g.cstride;
+    const T* am = p.nm1 + c * g.cstride;
+    T* ap = p.np1 + c * g.cstride;
+    T v;
+    if (NSFD) {
+      const T al = (T)g.nsfd_alpha, be = (T)g.nsfd_beta;
+      T sx = an[m + sI] + an[m - sI] + be * (an[m + sI + sK] + an[m + sI - sK] + an[m - sI + sK] + an[m - sI - sK]);
+      T sy = an[m + 1] + an[m - 1] + be * (an[m + 1 + sK] + an[m + 1 - sK] + an[m - 1 + sK] + an[m - 1 - sK]);
+      v = a0 * an[m] - am[m] + al * (a1 * sx + a2 * sy) + a3 * (an[m + sK] + an[m - sK]) + as * ap[m];
+    } else {
+      v = a0 * an[m] - am[m] + a1 * (an[m + sI] + an[m - sI]) + a2 * (an[m + 1] + an[m - 1]) +
+          a3 * (an[m + sK] + an[m - sK]) + as * ap[m];
+    }
+    ap[m] = v;
+  }
+}
+
+// Mur faces, AdvanceField::advanceBoundaryF/S (src/database.cpp:137-176) with the argument
+// pattern of src/fdtd.cpp:377-472: `in` points into the domain, o1/o2 along the face.
+template <typename T>
+__device__ __forceinline__ T face_value(const double* B, const T* np1, const T* n, const T* nm1,
+                                        long long m, long long in, long long o1, long long o2) {
+  return (T)B[0] * (nm1[m] + np1[m + in]) + (T)B[1] * nm1[m + in] + (T)B[2] * (n[m] + n[m + in]) +
+         (T)B[3] * (n[m + in + o1] + n[m + in - o1] + n[m + o1] + n[m - o1]) +
+         (T)B[4] * (n[m + in + o2] + n[m + in - o2] + n[m + o2] + n[m - o2]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_potential_faces(GridDev g, PotentialArgs<T> p) {
+  const long long nx = (long long)(g.N1 - 2) * (g.N2 - 2);
+  const long long ny = (long long)(g.N0 - 2) * (g.N2 - 2);
+  const long long nz = (long long)(g.N0 - 2) * (g.N1 - 2);
+  const long long total = 2 * (nx + ny + nz);
+  const long long sI = g.P1, sK = g.plane;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long m, in, o1, o2;
+    const double* B;
+    long long u = t;
+    if (u < 2 * nx) {  // x faces: j in [1,N1-2], k in [1,N2-2]
+      int side = u >= nx; u -= side * nx;
+      int j = 1 + (int)(u % (g.N1 - 2)), k = 1 + (int)(u / (g.N1 - 2));
+      m = node_index(g, k, side ? g.N0 - 1 : 0, j);
+      in = side ? -sI : sI; o1 = 1; o2 = sK; B = g.bB;
+    } else if ((u -= 2 * nx) < 2 * ny) {  // y faces: i in [1,N0-2], k in [1,N2-2]
+      int side = u >= ny; u -= side * ny;
+      int i = 1 + (int)(u % (g.N0 - 2)), k = 1 + (int)(u / (g.N0 - 2));
+      m = node_index(g, k, i, side ? g.N1 - 1 : 0);
+      in = side ? -1 : 1; o1 = sI; o2 = sK; B = g.cB;
+    } else {  // z faces: i in [1,N0-2], j in [1,N1-2]
+      u -= 2 * ny;
+      int side = u >= nz; u -= side * nz;
+      int j = 1 + (int)(u % (g.N1 - 2)), i = 1 + (int)(u / (g.N1 - 2));
+      m = node_index(g, side ? g.N2 - 1 : 0, i, j);
+      in = side ? -sK : sK; o1 = sI; o2 = 1; B = g.dB;
+    }
+    for (int c = 0; c < p.ncomp; c++) {
+      const long long off = c * g.cstride;
+      p.np1[off + m] = face_value<T>(B, p.np1 + off, p.n + off, p.nm1 + off, m, in, o1, o2);
+    }
+  }
+}
+
+// Mur edges, AdvanceField::advanceEdgeF/S (src/database.cpp:179-229) with the argument
+// pattern of src/fdtd.cpp:480-645: a, b point into the domain, t runs along the edge.
+template <typename T>
+__device__ __forceinline__ T edge_value(const double* E, const T* np1, const T* n, const T* nm1,
+                                        long long m, long long a, long long b, long long t) {
+  return (T)E[0] * (np1[m + a] + nm1[m + b]) + (T)E[1] * (nm1[m + a] + np1[m + b]) +
+         (T)E[2] * (nm1[m] + np1[m + a + b]) + (T)E[3] * (n[m] + n[m + a] + n[m + b] + n[m + a + b]) +
+         (T)E[4] * (n[m - t] + n[m + a - t] + n[m + b - t] + n[m + a + b - t] + n[m + t] + n[m + a + t] +
+                    n[m + b + t] + n[m + a + b + t]) -
+         nm1[m + a + b];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_potential_edges(GridDev g, PotentialArgs<T> p) {
+  const long long ez = g.N2 - 2, ex = g.N0 - 2, ey = g.N1 - 2;
+  const long long total = 4 * (ez + ex + ey);
+  const long long sI = g.P1, sK = g.plane;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    long long u = t, m, a, b, tt;
+    const double* E;
+    if (u < 4 * ez) {  // edges along z (eE), src/fdtd.cpp:480-522
+      int which = (int)(u / ez); int k = 1 + (int)(u % ez);
+      int hi_i = which & 1, hi_j = which >> 1;
+      m = node_index(g, k, hi_i ? g.N0 - 1 : 0, hi_j ? g.N1 - 1 : 0);
+      a = hi_i ? -sI : sI; b = hi_j ? -1 : 1; tt = sK; E = g.eE;
+    } else if ((u -= 4 * ez) < 4 * ex) {  // edges along x (fE), src/fdtd.cpp:527-579
+      int which = (int)(u / ex); int i = 1 + (int)(u % ex);
+      int hi_j = which & 1, hi_k = which >> 1;
+      m = node_index(g, hi_k ? g.N2 - 1 : 0, i, hi_j ? g.N1 - 1 : 0);
+      a = hi_j ? -1 : 1; b = hi_k ? -sK : sK; tt = sI; E = g.fE;
+    } else {  // edges along y (gE), src/fdtd.cpp:584-645
+      u -= 4 * ex;
+      int which = (int)(u / ey); int j = 1 + (int)(u % ey);
+      int hi_i = which & 1, hi_k = which >> 1;
+      m = node_index(g, hi_k ? g.N2 - 1 : 0, hi_i ? g.N0 - 1 : 0, j);
+      a = hi_k ? -sK : sK; b = hi_i ? -sI : sI; tt = 1; E = g.gE;
+    }
+    for (int c = 0; c < p.ncomp; c++) {
+      const long long off = c * g.cstride;
+      p.np1[off + m] = edge_value<T>(E, p.np1 + off, p.n + off, p.nm1 + off, m, a, b, tt);
+    }
+  }
+}
+
+// Mur corners, AdvanceField::advanceCornerF/S (src/database.cpp:232-288), src/fdtd.cpp:647-725.
+template <typename T>
+__global__ void k_potential_corners(GridDev g, PotentialArgs<T> p) {
+  const int t = threadIdx.x;
+  if (t >= 8 * p.ncomp) return;
+  const int c = t / 8, w = t % 8;
+  const int hi_i = w & 1, hi_j = (w >> 1) & 1, hi_k = w >> 2;
+  const long long off = c * g.cstride;
+  const T* np1 = p.np1 + off;
+  const T* n = p.n + off;
+  const T* nm1 = p.nm1 + off;
+  const long long m = node_index(g, hi_k ? g.N2 - 1 : 0, hi_i ? g.N0 - 1 : 0, hi_j ? g.N1 - 1 : 0);
+  const long long a = hi_i ? -(long long)g.P1 : g.P1, b = hi_j ? -1 : 1, cc = hi_k ? -g.plane : g.plane;
+  const double* h = g.hC;
+  const long long P1 = m + a, P2 = m + b, P3 = m + cc, P4 = m + a + b, P5 = m + cc + a, P6 = m + cc + b,
+                  P7 = m + a + b + cc;
+  T s = n[m] * (T)h[16] + nm1[m] * (T)h[8] + np1[P1] * (T)h[1] + n[P1] * (T)h[16] + nm1[P1] * (T)h[9] +
+        np1[P2] * (T)h[2] + n[P2] * (T)h[16] + nm1[P2] * (T)h[10] + np1[P3] * (T)h[3] + n[P3] * (T)h[16] +
+        nm1[P3] * (T)h[11] + np1[P4] * (T)h[4] + n[P4] * (T)h[16] + nm1[P4] * (T)h[12] + np1[P5] * (T)h[5] +
+        n[P5] * (T)h[16] + nm1[P5] * (T)h[13] + np1[P6] * (T)h[6] + n[P6] * (T)h[16] + nm1[P6] * (T)h[14] +
+        np1[P7] * (T)h[7] + n[P7] * (T)h[16] + nm1[P7] * (T)h[15];
+  p.np1[off + m] = -s / (T)h[0];
+}
+
+// E and B at every interior node, the eager form of FdTd::fieldEvaluate (src/fdtd.cpp:818-845;
+// with space charge src/fdtdSC.cpp:1110-1140), plus the copies into planes k = 0 and N2-1
+// (src/fdtd.cpp:755-772).  E is rounded to float twice as FieldVector<float>::dv and ::mdv do
+// (src/fieldvector.h:87-107); B once.
+template <typename T>
+struct EBArgs {
+  const T* anp1;
+  const T* an;
+  const T* fn;  // scalar potential phi^n, or nullptr without space charge
+  float* E;     // 3 components, cstride apart
+  float* B;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_lo, int k_hi) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + k_lo;
+  if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
+  const long long m = node_index(g, k, i, j);
+  const long long cs = g.cstride, sI = g.P1, sK = g.plane;
+  const double rmdt = -1.0 / g.dt;
+  const double rdx2 = 1.0 / (2.0 * g.dx), rdy2 = 1.0 / (2.0 * g.dy), rdz2 = 1.0 / (2.0 * g.dz);
+  const T *A1 = p.anp1, *A0 = p.an;
+  float e[3], b[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float ef = (float)((double)A1[c * cs + m] * rmdt);
+    ef = (float)((double)ef - (double)A0[c * cs + m] * rmdt);
+    e[c] = ef;
+  }
+  if (p.fn) {
+    e[0] = (float)((double)e[0] - ((double)p.fn[m + sI] - (double)p.fn[m - sI]) * rdx2);
+    e[1] = (float)((double)e[1] - ((double)p.fn[m + 1] - (double)p.fn[m - 1]) * rdy2);
+    e[2] = (float)((double)e[2] - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
+  }
+  const T *X0 = A0, *Y0 = A0 + cs, *Z0 = A0 + 2 * cs, *X1 = A1, *Y1 = A1 + cs, *Z1 = A1 + 2 * cs;
+  double bx = 0.5 * (((double)Z0[m + 1] - Z0[m - 1]) * rdy2 - ((double)Y0[m + sK] - Y0[m - sK]) * rdz2 +
+                     ((double)Z1[m + 1] - Z1[m - 1]) * rdy2 - ((double)Y1[m + sK] - Y1[m - sK]) * rdz2);
+  double by = 0.5 * (((double)X0[m + sK] - X0[m - sK]) * rdz2 - ((double)Z0[m + sI] - Z0[m - sI]) * rdx2 +
+                     ((double)X1[m + sK] - X1[m - sK]) * rdz2 - ((double)Z1[m + sI] - Z1[m - sI]) * rdx2);
+  double bz = 0.5 * (((double)Y0[m + sI] - Y0[m - sI]) * rdx2 - ((double)X0[m + 1] - X0[m - 1]) * rdy2 +
+                     ((double)Y1[m + sI] - Y1[m - sI]) * rdx2 - ((double)X1[m + 1] - X1[m - 1]) * rdy2);
+  b[0] = (float)bx; b[1] = (float)by; b[2] = (float)bz;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    p.E[c * cs + m] = e[c];
+    p.B[c * cs + m] = b[c];
+  }
+  if (k == 1) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = e[c]; p.B[c * cs + m - sK] = b[c]; }
+  }
+  if (k == g.N2 - 2) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = e[c]; p.B[c * cs + m + sK] = b[c]; }
+  }
+}
+
+// Layout conversion between the reference's AoS records (m = N1N0*k + N1*i + j, `ncomp`
+// values per node) and the padded SoA device layout.
+template <typename Tdev, typename Thost>
+__global__ void k_aos_to_soa(GridDev g, const Thost* __restrict__ src, Tdev* __restrict__ dst, int ncomp) {
+  const long long total = (long long)g.N0 * g.N1 * g.N2;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(r % g.N1);
+    const long long ki = r / g.N1;
+    const int i = (int)(ki % g.N0), k = (int)(ki / g.N0);
+    const long long m = node_index(g, k, i, j);
+    for (int c = 0; c < ncomp; c++) dst[c * g.cstride + m] = (Tdev)src[r * ncomp + c];
+  }
+}
+
+template <typename Tdev, typename Thost>
+__global__ void k_soa_to_aos(GridDev g, const Tdev* __restrict__ src, Thost* __restrict__ dst, int ncomp) {
+  const long long total = (long long)g.N0 * g.N1 * g.N2;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(r % g.N1);
+    const long long ki = r / g.N1;
+    const int i = (int)(ki % g.N0), k = (int)(ki / g.N0);
+    const long long m = node_index(g, k, i, j);
+    for (int c = 0; c < ncomp; c++) dst[r * ncomp + c] = (Thost)src[c * g.cstride + m];
+  }
+}
+
+}  // namespace mithra

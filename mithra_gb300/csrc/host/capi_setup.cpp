@@ -1,0 +1,169 @@
+// C ABI of the host initialisation (mithra_setup_*) and the job-level context constructor.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <exception>
+
+#include "mithra_gpu.h"
+#include "setup.h"
+
+struct mithra_setup {
+  mithra::host::Setup s;
+};
+
+using mithra::host::Setup;
+
+extern "C" {
+
+int mithra_setup_from_job(const char* job_path, mithra_setup** out, char* err, size_t err_len) {
+  if (!job_path || !out) return MITHRA_ERR_ARG;
+  *out = nullptr;
+  mithra_setup* h = new mithra_setup();
+  try {
+    h->s.job = mithra::host::parse_job_file(job_path);
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    delete h;
+    return MITHRA_ERR_PARSE;
+  }
+  try {
+    h->s.initialize();
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    delete h;
+    return MITHRA_ERR_ARG;
+  }
+  *out = h;
+  return MITHRA_OK;
+}
+
+int mithra_setup_destroy(mithra_setup* s) {
+  if (!s) return MITHRA_ERR_ARG;
+  delete s;
+  return MITHRA_OK;
+}
+
+int mithra_setup_grid(const mithra_setup* s, mithra_grid_desc* g) {
+  if (!s || !g) return MITHRA_ERR_ARG;
+  s->s.fill_grid(g);
+  return MITHRA_OK;
+}
+
+int mithra_setup_push(const mithra_setup* s, mithra_push_desc* p) {
+  if (!s || !p) return MITHRA_ERR_ARG;
+  s->s.fill_push(p);
+  return MITHRA_OK;
+}
+
+int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, int cap, int* n) {
+  if (!s || !n) return MITHRA_ERR_ARG;
+  const auto& U = s->s.job.undulators;
+  *n = (int)U.size();
+  for (int u = 0; u < std::min<int>(cap, (int)U.size()); u++) {
+    und[u].type = U[u].type == mithra::host::STATIC ? 0 : 1;
+    und[u].k = U[u].k;
+    und[u].lu = U[u].lu;
+    und[u].rb = U[u].rb;
+    und[u].length = (double)U[u].length;
+    und[u].dist = U[u].dist;
+    und[u].theta = U[u].theta;
+  }
+  return MITHRA_OK;
+}
+
+int mithra_setup_time(const mithra_setup* s, mithra_time_state* t) {
+  if (!s || !t) return MITHRA_ERR_ARG;
+  t->time = s->s.time;
+  t->time_bunch = s->s.timeBunch;
+  t->n_time = s->s.nTime;
+  t->n_time_bunch = s->s.nTimeBunch;
+  return MITHRA_OK;
+}
+
+int mithra_setup_total_time(const mithra_setup* s, double* total_time) {
+  if (!s || !total_time) return MITHRA_ERR_ARG;
+  *total_time = s->s.job.mesh.totalTime;
+  return MITHRA_OK;
+}
+
+int mithra_setup_particles(const mithra_setup* s, double* rec, size_t cap, size_t* n) {
+  if (!s || !n) return MITHRA_ERR_ARG;
+  const auto& C = s->s.charges;
+  *n = C.size();
+  if (!rec) return MITHRA_OK;
+  for (size_t i = 0; i < std::min(cap, C.size()); i++) {
+    double* r = rec + 11 * i;
+    r[0] = C[i].q;
+    for (int d = 0; d < 3; d++) { r[1 + d] = C[i].rnp[d]; r[4 + d] = C[i].rnm[d]; r[7 + d] = C[i].gb[d]; }
+    r[10] = C[i].e;
+  }
+  return cap < C.size() ? MITHRA_ERR_CAPACITY : MITHRA_OK;
+}
+
+int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double* anm1) {
+  if (!s) return MITHRA_ERR_ARG;
+  const size_t n = (size_t)s->s.N1N0 * s->s.np * 3;
+  if (anp1) memset(anp1, 0, n * sizeof(double));
+  if (an) {
+    if (s->s.an.empty()) memset(an, 0, n * sizeof(double));
+    else memcpy(an, s->s.an.data(), n * sizeof(double));
+  }
+  if (anm1) {
+    if (s->s.anm1.empty()) memset(anm1, 0, n * sizeof(double));
+    else memcpy(anm1, s->s.anm1.data(), n * sizeof(double));
+  }
+  return MITHRA_OK;
+}
+
+int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
+  if (!s) return MITHRA_ERR_ARG;
+  const std::string m = s->s.meta();
+  if (needed) *needed = m.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < m.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, m.c_str(), m.size() + 1);
+  return MITHRA_OK;
+}
+
+int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int device, double capacity_factor,
+                                 mithra_ctx** out) {
+  if (!s || !out) return MITHRA_ERR_ARG;
+  const Setup& S = s->s;
+  mithra_grid_desc g;
+  mithra_push_desc p;
+  S.fill_grid(&g);
+  S.fill_push(&p);
+  if (capacity_factor < 1.0) capacity_factor = 1.0;
+  const size_t cap = (size_t)std::ceil(S.charges.size() * capacity_factor) + 1024;
+  int r = mithra_gpu_create(&g, &p, precision, device, cap, out);
+  if (r) return r;
+  mithra_ctx* ctx = *out;
+  auto bail = [&](int code) { mithra_gpu_destroy(ctx); *out = nullptr; return code; };
+  std::vector<mithra_undulator_desc> und(S.job.undulators.size());
+  int nu = 0;
+  if ((r = mithra_setup_undulators(s, und.data(), (int)und.size(), &nu))) return bail(r);
+  if ((r = mithra_gpu_set_undulators(ctx, und.data(), nu))) return bail(r);
+  std::vector<mithra_power_desc> pw;
+  for (const auto& pc : S.power) {
+    mithra_power_desc d;
+    d.N = pc.N; d.Nl = pc.Nl; d.Nf = pc.Nf; d.pc = pc.pc;
+    d.z = pc.z.data(); d.twiddle_re = pc.tw_re.data(); d.twiddle_im = pc.tw_im.data();
+    pw.push_back(d);
+  }
+  if ((r = mithra_gpu_set_power(ctx, pw.data(), (int)pw.size()))) return bail(r);
+  const size_t nf = (size_t)S.N1N0 * S.np * 3;
+  std::vector<double> a1(nf, 0.0);
+  const double* an = S.an.empty() ? a1.data() : S.an.data();
+  const double* anm1 = S.anm1.empty() ? a1.data() : S.anm1.data();
+  if ((r = mithra_gpu_upload_fields(ctx, a1.data(), an, anm1))) return bail(r);
+  std::vector<double> rec(S.charges.size() * 11);
+  size_t n = 0;
+  if ((r = mithra_setup_particles(s, rec.data(), S.charges.size(), &n))) return bail(r);
+  if ((r = mithra_gpu_upload_particles(ctx, rec.data(), n))) return bail(r);
+  mithra_time_state t;
+  mithra_setup_time(s, &t);
+  if ((r = mithra_gpu_set_time(ctx, &t))) return bail(r);
+  return MITHRA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,565 @@
+// Job-file reader and parser.  Same grammar and value conversions as the reference:
+//   * read_file/cleanJobFile (src/readdata.cpp:10-53): '#' starts a comment, every space and
+//     tab inside a line is removed, empty lines are dropped;
+//   * parameterName/stringValue/doubleValue/intValue/boolValue/vectorDoubleValue
+//     (src/readdata.cpp:56-160): atof-based conversions;
+//   * ParseDarius (src/datainput.cpp:18-751): groups MESH, BUNCH, FIELD, UNDULATOR,
+//     EXTERNAL-FIELD, FEL-OUTPUT; an unknown group or key is an error.
+// Where the reference prints and calls exit(1), this parser throws std::runtime_error with the
+// same message.
+#include <cmath>
+#include <cstdlib>
+#include <fstream>
+#include <stdexcept>
+
+#include "params.h"
+
+namespace mithra {
+namespace host {
+namespace {
+
+[[noreturn]] void die(const std::string& msg) { throw std::runtime_error(msg); }
+
+std::string name_of(const std::string& line) { return line.substr(0, line.find('=')); }
+
+std::string string_of(const std::string& line) {
+  std::string v = line.substr(line.find('=') + 1);
+  if (v.compare(0, 1, "\"") == 0) {
+    v.erase(v.find('"'), 1);
+    size_t q = v.find('"');
+    if (q != std::string::npos) v.erase(q, 1);
+  }
+  return v;
+}
+
+double double_of(const std::string& line) { return std::atof(line.substr(line.find('=') + 1).c_str()); }
+
+int int_of(const std::string& line) { return (int)std::atof(line.substr(line.find('=') + 1).c_str()); }
+
+bool bool_of(const std::string& line) {
+  std::string v = line.substr(line.find('=') + 1);
+  if (v == "true") return true;
+  if (v == "false") return false;
+  die("boolValue(std::string line) got unexpected input. Input should be \"true\" or \"false\" ");
+}
+
+// "(a,b,c)" -> {atof(a), atof(b), atof(c)}: the first character is dropped and the last one
+// replaced by a comma, then the string is cut at commas.
+std::vector<double> vector_of(const std::string& line) {
+  std::string v = line.substr(line.find('=') + 1);
+  std::vector<double> out;
+  if (v.empty()) return out;
+  v.erase(0, 1);
+  if (v.empty()) return out;
+  v.replace(v.size() - 1, 1, ",");
+  size_t c;
+  while ((c = v.find(',')) < v.size()) {
+    out.push_back(std::atof(v.substr(0, c).c_str()));
+    v.erase(0, c + 1);
+  }
+  return out;
+}
+
+std::vector<unsigned> uvector_of(const std::string& line) {
+  std::string v = line.substr(line.find('=') + 1);
+  std::vector<unsigned> out;
+  if (v.empty()) return out;
+  v.erase(0, 1);
+  if (v.empty()) return out;
+  v.replace(v.size() - 1, 1, ",");
+  size_t c;
+  while ((c = v.find(',')) < v.size()) {
+    out.push_back((unsigned)std::atoi(v.substr(0, c).c_str()));
+    v.erase(0, c + 1);
+  }
+  return out;
+}
+
+Vec3 vec3(const std::vector<double>& v) {
+  if (v.size() != 3) die("A field-vector with other than three parameters is not accepted.");
+  return {v[0], v[1], v[2]};
+}
+
+double norm2(const Vec3& v) { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; }
+
+struct Cursor {
+  const std::vector<std::string>& L;
+  size_t i = 0;
+  explicit Cursor(const std::vector<std::string>& l) : L(l) {}
+  const std::string& cur() const {
+    if (i >= L.size()) die("unexpected end of the job file");
+    return L[i];
+  }
+  void next() { ++i; }
+  void open(const char* what) {
+    next();
+    if (cur() != "{") die(std::string("The ") + what + " directory is empty");
+    next();
+  }
+};
+
+// Signal::initialize, src/classes.cpp:512-555.
+Signal make_signal(const std::string& type, double l0, double s, double l, double cep, unsigned nR,
+                   const std::vector<double>& sigmaInvG) {
+  Signal sg;
+  if (type == "neumann") sg.type = NEUMANN;
+  else if (type == "gaussian") sg.type = GAUSSIAN;
+  else if (type == "secant-hyperbolic") sg.type = SECANT;
+  else if (type == "flat-top") sg.type = FLATTOP;
+  else if (type == "inverse-gaussian") sg.type = INVGAUSSIAN;
+  else die(type + " is an unknown signal type for the given set of parameters.");
+  sg.t0 = l0;
+  sg.s = s;
+  sg.f0 = 1 / l;
+  sg.cep = cep * PI / 180;
+  sg.nR = nR;
+  sg.sigmaInvG = sigmaInvG;
+  if (sg.s == 0.0) die(" Variance of signal is set to zero. ");
+  if (sg.type == INVGAUSSIAN && sg.sigmaInvG.size() >= 2 && sg.sigmaInvG[0] * sg.sigmaInvG[1] == 0.0)
+    die(" sigma of the inverse-gaussian signal is set to zero. ");
+  return sg;
+}
+
+SeedType seed_type(const std::string& type) {
+  if (type == "plane-wave") return PLANEWAVE;
+  if (type == "truncated-plane-wave") return PLANEWAVETRUNCATED;
+  if (type == "gaussian-beam") return GAUSSIANBEAM;
+  if (type == "super-gaussian-beam") return SUPERGAUSSIANBEAM;
+  if (type == "standing-plane-wave") return STANDINGPLANEWAVE;
+  if (type == "standing-truncated-plane-wave") return STANDINGPLANEWAVETRUNCATED;
+  if (type == "standing-gaussian-beam") return STANDINGGAUSSIANBEAM;
+  if (type == "standing-super-gaussian-beam") return STANDINGSUPERGAUSSIANBEAM;
+  die(type + " is an unknown type.");
+}
+
+// Seed::initialize / Undulator::initialize / ExtField::initialize (src/classes.cpp:640-735,
+// :1003-1075, :1163-1260).  `ext` selects the ExtField variant, which normalises direction and
+// polarisation by sqrt(norm()) (src/classes.cpp:1197, :1210); the super-Gaussian branch divides
+// radius[0] twice (src/classes.cpp:733-734), both kept as in the reference.
+void init_beam(Beam& b, const std::string& type, const std::vector<double>& position,
+               const std::vector<double>& direction, const std::vector<double>& polarization, double a0,
+               const std::vector<double>& radius, const std::vector<int>& order, const Signal& signal, bool ext) {
+  b.seedType = seed_type(type);
+  b.position = vec3(position);
+  b.polarization = vec3(polarization);
+  b.direction = vec3(direction);
+  if (ext) {
+    double n = std::sqrt(norm2(b.direction));
+    if (n == 0.0) die("The direction vector has length zero.");
+    double vl = std::sqrt(n);
+    for (auto& x : b.direction) x /= vl;
+    n = std::sqrt(norm2(b.polarization));
+    if (n == 0.0) die("The polarization vector has length zero.");
+    vl = std::sqrt(n);
+    for (auto& x : b.polarization) x /= vl;
+  } else {
+    if (norm2(b.direction) == 0.0) die("The direction vector has length zero.");
+    double vl = std::sqrt(norm2(b.direction));
+    for (auto& x : b.direction) x /= vl;
+    if (norm2(b.polarization) == 0.0) die("The polarization vector has length zero.");
+    vl = std::sqrt(norm2(b.polarization));
+    for (auto& x : b.polarization) x /= vl;
+  }
+  const double pd = b.polarization[0] * b.direction[0] + b.polarization[1] * b.direction[1] +
+                    b.polarization[2] * b.direction[2];
+  if (std::fabs(pd) > 1.0e-50) die("Polarization is not normal to the direction.");
+  b.a0 = a0;
+  b.radius = radius;
+  if ((b.seedType == GAUSSIANBEAM || b.seedType == STANDINGGAUSSIANBEAM || b.seedType == SUPERGAUSSIANBEAM ||
+       b.seedType == STANDINGSUPERGAUSSIANBEAM) && b.radius[0] * b.radius[1] == 0.0)
+    die("One of the radii of the Gaussian beam is set to zero.");
+  b.signal = signal;
+  if (b.seedType == SUPERGAUSSIANBEAM || b.seedType == STANDINGSUPERGAUSSIANBEAM) {
+    b.order = order;
+    double d1 = 0.0, d2 = 0.0;
+    for (int i = -b.order[0]; i <= b.order[0]; i++) d1 += std::exp(-i * i);
+    for (int i = -b.order[1]; i <= b.order[1]; i++) d2 += std::exp(-i * i);
+    b.radius[0] /= b.order[0] + std::sqrt(1.0 - std::log(d1));
+    b.radius[0] /= b.order[0] + std::sqrt(1.0 - std::log(d2));
+    b.a0 /= d1 * d2;
+  }
+}
+
+struct BeamKeys {
+  std::string type, signalType;
+  std::vector<double> position{0, 0, 0}, direction{0, 0, 0}, polarization{0, 0, 0}, sigmaInvG{0, 0};
+  double a0 = 0.0, offset = 0.0, pulseLength = 0.0, wavelength = 0.0, cep = 0.0;
+  unsigned nR = 2;
+  std::vector<double> radius{0.0, 0.0};
+  std::vector<int> order{0, 0};
+  // Returns false when `n` is not one of the shared beam keys.
+  bool take(const std::string& n, const std::string& line, const char* type_key) {
+    if (n == type_key) type = string_of(line);
+    else if (n == "position") position = vector_of(line);
+    else if (n == "direction") direction = vector_of(line);
+    else if (n == "polarization") polarization = vector_of(line);
+    else if (n == "strength-parameter") a0 = double_of(line);
+    else if (n == "radius-parallel") radius[0] = double_of(line);
+    else if (n == "radius-perpendicular") radius[1] = double_of(line);
+    else if (n == "order-parallel") order[0] = (int)double_of(line);
+    else if (n == "order-perpendicular") order[1] = (int)double_of(line);
+    else if (n == "signal-type") signalType = string_of(line);
+    else if (n == "offset") offset = double_of(line);
+    else if (n == "pulse-length") pulseLength = double_of(line);
+    else if (n == "wavelength") wavelength = double_of(line);
+    else if (n == "rising-cycles") nR = (unsigned)int_of(line);
+    else if (n == "CEP") cep = double_of(line);
+    else if (n == "sigma-inverse-gaussian") sigmaInvG = vector_of(line);
+    else return false;
+    return true;
+  }
+  Signal signal() const {
+    if (signalType == "neumann" || signalType == "gaussian" || signalType == "secant-hyperbolic" ||
+        signalType == "flat-top" || signalType == "inverse-gaussian")
+      return make_signal(signalType, offset, pulseLength, wavelength, cep, nR, sigmaInvG);
+    die(signalType + " is an unknown signal type.");
+  }
+};
+
+void read_mesh(Cursor& c, Job& J) {
+  c.open("solver");
+  Mesh& m = J.mesh;
+  do {
+    const std::string& l = c.cur();
+    const std::string n = name_of(l);
+    if (n == "length-scale") {
+      const std::string v = string_of(l);
+      if (v == "METER") m.lengthScale = 1.0;
+      else if (v == "DECIMETER") m.lengthScale = 1.0e-1;
+      else if (v == "CENTIMETER") m.lengthScale = 1.0e-2;
+      else if (v == "MILLIMETER") m.lengthScale = 1.0e-3;
+      else if (v == "MICROMETER") m.lengthScale = 1.0e-6;
+      else if (v == "NANOMETER") m.lengthScale = 1.0e-9;
+      else if (v == "ANGSTROM") m.lengthScale = 1.0e-10;
+      else m.lengthScale = double_of(l);
+    } else if (n == "mesh-lengths") m.meshLength = vec3(vector_of(l));
+    else if (n == "mesh-resolution") m.meshResolution = vec3(vector_of(l));
+    else if (n == "mesh-center") m.meshCenter = vec3(vector_of(l));
+    else if (n == "total-time") m.totalTime = double_of(l);
+    else if (n == "total-distance") m.totalDist = double_of(l);
+    else if (n == "bunch-time-step") J.bunch.timeStep = double_of(l);
+    else if (n == "mesh-truncation-order") {
+      m.truncationOrder = int_of(l);
+      if (m.truncationOrder != 1 && m.truncationOrder != 2) die("Mesh truncation order can not be different from one or two.");
+    } else if (n == "time-scale") {
+      const std::string v = string_of(l);
+      if (v == "SECOND") m.timeScale = 1.0;
+      else if (v == "MILLISECOND") m.timeScale = 1.0e-3;
+      else if (v == "MICROSECOND") m.timeScale = 1.0e-6;
+      else if (v == "NANOSECOND") m.timeScale = 1.0e-9;
+      else if (v == "PICOSECOND") m.timeScale = 1.0e-12;
+      else if (v == "FEMTOSECOND") m.timeScale = 1.0e-15;
+      else if (v == "ATTOSECOND") m.timeScale = 1.0e-18;
+      else m.timeScale = double_of(l);
+    } else if (n == "space-charge") m.spaceCharge = bool_of(l);
+    else if (n == "optimize-bunch-position") m.optimizePosition = bool_of(l);
+    else if (n == "initial-time-back-shift") {
+      m.timeShift = double_of(l);
+      if (m.timeShift < 0.0) die("The shift back in time should always be positive.");
+    } else if (n == "solver") {
+      const std::string v = string_of(l);
+      if (v == "FD") m.solver = FD;
+      else if (v == "NSFD") m.solver = NSFD;
+      else die("The solver type is not among the accepted solvers.");
+    } else if (n == "lorentz-factor") m.gamma = double_of(l);
+    else die(n + " is not defined in solver group.");
+    c.next();
+  } while (c.cur() != "}");
+}
+
+void read_bunch(Cursor& c, Job& J) {
+  c.open("bunch");
+  do {
+    const std::string& g = c.cur();
+    if (g == "bunch-initialization") {
+      c.open("bunch-initialization");
+      BunchInit b;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "type") b.type = string_of(l);
+        else if (n == "distribution") b.distribution = string_of(l);
+        else if (n == "generator") {
+          b.generator = string_of(l);
+          if (b.generator != "halton" && b.generator != "random") die("The inserted generator is not accepted !!!");
+        } else if (n == "charge") b.cloudCharge = double_of(l);
+        else if (n == "number-of-particles") b.numberOfParticles = (unsigned)int_of(l);
+        else if (n == "gamma") b.initialGamma = double_of(l);
+        else if (n == "direction") b.initialDirection = vec3(vector_of(l));
+        else if (n == "position") b.position.push_back(vec3(vector_of(l)));
+        else if (n == "numbers") {
+          auto v = uvector_of(l);
+          if (v.size() != 3) die("A field-vector with other than three parameters is not accepted.");
+          b.numbers = {v[0], v[1], v[2]};
+        } else if (n == "lattice-constants") b.latticeConstants = vec3(vector_of(l));
+        else if (n == "sigma-position") b.sigmaPosition = vec3(vector_of(l));
+        else if (n == "sigma-momentum") b.sigmaGammaBeta = vec3(vector_of(l));
+        else if (n == "transverse-truncation") b.tranTrun = double_of(l);
+        else if (n == "longitudinal-truncation") b.longTrun = double_of(l);
+        else if (n == "file-name") b.fileName = string_of(l);
+        else if (n == "bunching-factor") b.bF = double_of(l);
+        else if (n == "bunching-factor-phase") b.bFP = double_of(l);
+        else if (n == "shot-noise") b.shotNoise = bool_of(l);
+        else die(n + " is not defined in bunch-initialization group.");
+        c.next();
+      } while (c.cur() != "}");
+      J.bunch.inits.push_back(b);
+    } else if (g == "bunch-sampling" || g == "bunch-visualization" || g == "bunch-profile") {
+      const std::string grp = g;
+      c.open(grp.c_str());
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "sample") {
+          bool v = bool_of(l);
+          if (grp == "bunch-sampling") J.bunch.sampling = v;
+          else if (grp == "bunch-visualization") J.bunch.vtk = v;
+          else J.bunch.profile = v;
+        } else if (n == "directory" || n == "base-name") {
+        } else if (n == "rhythm") {
+          double v = double_of(l);
+          if (grp == "bunch-sampling") J.bunch.rhythm = v;
+          else if (grp == "bunch-visualization") J.bunch.vtkRhythm = v;
+          else J.bunch.profileRhythm = v;
+        } else if (n == "time" && grp == "bunch-profile") J.bunch.profileTime.push_back(double_of(l));
+        else die(n + " is not defined in the " + grp + " group.");
+        c.next();
+      } while (c.cur() != "}");
+    } else {
+      die(name_of(g) + " is not defined in the bunch-profile group.");
+    }
+    c.next();
+  } while (c.cur() != "}");
+}
+
+void read_field(Cursor& c, Job& J) {
+  c.open("seed");
+  do {
+    const std::string& g = c.cur();
+    if (g == "field-initialization") {
+      c.open("seed-initialization");
+      BeamKeys k;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (!k.take(n, l, "type")) die(n + " is not defined in seed-initialization group.");
+        c.next();
+      } while (c.cur() != "}");
+      Signal s = k.signal();
+      init_beam(J.seed, k.type, k.position, k.direction, k.polarization, k.a0, k.radius, k.order, s, false);
+    } else if (g == "field-sampling" || g == "field-visualization" || g == "field-profile") {
+      // Diagnostics outside the time-marching path: accepted and validated, not produced.
+      const std::string grp = g;
+      c.open(grp.c_str());
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        static const char* keys[] = {"sample", "type", "field", "directory", "base-name", "rhythm", "position",
+                                     "line-begin", "line-end", "number-of-points", "plane", "time"};
+        bool ok = false;
+        for (const char* kk : keys) ok |= (n == kk);
+        if (!ok) die(n + " is not defined in " + grp + " group.");
+        if (n == "sample") {
+          bool v = bool_of(l);
+          if (grp == "field-sampling") J.seed.sampling = v;
+          if (grp == "field-profile") J.seed.profile = v;
+        }
+        c.next();
+      } while (c.cur() != "}");
+    }
+    c.next();
+  } while (c.cur() != "}");
+}
+
+void read_undulator(Cursor& c, Job& J) {
+  c.open("undulator");
+  do {
+    if (c.cur() == "static-undulator") {
+      c.open("static undulator");
+      Undulator u;
+      u.type = STATIC;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "undulator-parameter") u.k = double_of(l);
+        else if (n == "period") u.lu = double_of(l);
+        else if (n == "polarization-angle") u.theta = PI / 180.0 * double_of(l);
+        else if (n == "length") u.length = (unsigned)int_of(l);
+        else if (n == "distance-to-bunch-head") u.dist = double_of(l);
+        else if (n == "offset") u.rb = double_of(l);
+        else die(n + " is not defined in the static-undulator group.");
+        c.next();
+      } while (c.cur() != "}");
+      J.undulators.push_back(u);
+    }
+    if (c.cur() == "static-undulator-array") {
+      c.open("static undulator");
+      Undulator u;
+      double k = u.k, lu = u.lu, theta = u.theta, gap = 0.0, taper = 0.0, d = 0.0;
+      unsigned len = u.length, N = 1;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "undulator-parameter") k = double_of(l);
+        else if (n == "period") lu = double_of(l);
+        else if (n == "polarization-angle") theta = PI / 180.0 * double_of(l);
+        else if (n == "length") len = (unsigned)int_of(l);
+        else if (n == "gap") gap = double_of(l);
+        else if (n == "number") N = (unsigned)int_of(l);
+        else if (n == "tapering-parameter") taper = double_of(l);
+        else if (n == "distance-to-bunch-head") d = double_of(l);
+        else die(n + " is not defined in the static-undulator-array group.");
+        c.next();
+      } while (c.cur() != "}");
+      for (unsigned i = 0; i < N; i++) {  // src/datainput.cpp:487-502
+        u.type = STATIC;
+        u.k = k + i * taper;
+        u.lu = lu;
+        u.theta = theta;
+        u.length = len;
+        u.rb = i * (len * lu + gap);
+        u.dist = d;
+        J.undulators.push_back(u);
+      }
+    } else if (c.cur() == "optical-undulator") {
+      c.open("optical undulator");
+      Undulator u;
+      u.type = OPTICAL;
+      BeamKeys k;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (k.take(n, l, "beam-type")) {
+        } else if (n == "distance-to-bunch-head") u.dist = double_of(l);
+        else die(n + " is not defined in the optical-undulator group.");
+        c.next();
+      } while (c.cur() != "}");
+      Signal s = k.signal();
+      init_beam(u, k.type, k.position, k.direction, k.polarization, k.a0, k.radius, k.order, s, false);
+      u.lu = k.wavelength;  // Undulator::initialize sets lu_ = wavelength (src/classes.cpp:1059)
+      J.undulators.push_back(u);
+    }
+    c.next();
+  } while (c.cur() != "}");
+}
+
+void read_ext_field(Cursor& c, Job& J) {
+  c.open("EXTERNAL-FIELD");
+  do {
+    if (c.cur() == "electromagnetic-wave") {
+      c.open("electromagnetic-field");
+      BeamKeys k;
+      Signal defaults;
+      k.offset = defaults.t0;
+      k.pulseLength = defaults.s;
+      k.wavelength = 1 / defaults.f0;
+      k.cep = defaults.cep;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (!k.take(n, l, "beam-type")) die(n + " is not defined in the electromagnetic external field group.");
+        c.next();
+      } while (c.cur() != "}");
+      Signal s = k.signal();
+      ExtField e;
+      init_beam(e, k.type, k.position, k.direction, k.polarization, k.a0, k.radius, k.order, s, true);
+      J.extFields.push_back(e);
+    }
+    c.next();
+  } while (c.cur() != "}");
+}
+
+void read_fel(Cursor& c, Job& J) {
+  c.open("FEL-OUTPUT");
+  do {
+    if (c.cur() == "radiation-power") {
+      c.open("radiation-power");
+      FEL f;
+      RadiationPower& r = f.radiationPower;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "sample") r.sampling = bool_of(l);
+        else if (n == "plane-position") r.z.push_back(double_of(l));
+        else if (n == "directory") r.directory = string_of(l);
+        else if (n == "base-name") r.basename = string_of(l);
+        else if (n == "line-begin") r.lineBegin = double_of(l);
+        else if (n == "line-end") r.lineEnd = double_of(l);
+        else if (n == "number-of-points") r.res = (unsigned)int_of(l);
+        else if (n == "normalized-frequency") r.lambda.push_back(double_of(l));
+        else if (n == "minimum-normalized-frequency") r.lambdaMin = double_of(l);
+        else if (n == "maximum-normalized-frequency") r.lambdaMax = double_of(l);
+        else if (n == "number-of-frequency-points") r.lambdaRes = (unsigned)int_of(l);
+        else if (n == "type") {
+          const std::string v = string_of(l);
+          if (v == "at-point") r.samplingType = ATPOINT;
+          else if (v == "over-line") r.samplingType = OVERLINE;
+          else die(v + " is an unknown sampling type.");
+        } else die(n + " is not defined in radiation-power group.");
+        c.next();
+      } while (c.cur() != "}");
+      J.fel.push_back(f);
+    }
+    // Power visualisation, radiation energy and lab-frame screens are diagnostics outside the
+    // time-marching path.  Their groups are accepted; the radiation-energy group, which the
+    // reference parses into the radiation-power fields (src/datainput.cpp:706-717), adds an
+    // output entry the same way.
+    static const char* other[] = {"power-visualization", "radiation-energy", "bunch-profile-lab-frame"};
+    for (const char* grp : other) {
+      if (c.cur() != grp) continue;
+      c.open(grp);
+      FEL f;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (std::string(grp) == "radiation-energy" && n == "sample") f.radiationPower.sampling = bool_of(l);
+        c.next();
+      } while (c.cur() != "}");
+      // Only radiation-power entries are sampled here; mark the others as not sampling power.
+      f.radiationPower.sampling = false;
+      J.fel.push_back(f);
+    }
+    c.next();
+  } while (c.cur() != "}");
+}
+
+}  // namespace
+
+Job parse_job_text(const std::vector<std::string>& raw) {
+  std::vector<std::string> lines;
+  for (std::string s : raw) {
+    size_t h = s.find('#');
+    if (h != std::string::npos) s.erase(h);
+    std::string t;
+    for (char ch : s)
+      if (ch != ' ' && ch != '\t' && ch != '\r') t.push_back(ch);
+    if (!t.empty()) lines.push_back(t);
+  }
+  Job J;
+  if (lines.empty()) die("the job file is empty");
+  Cursor c(lines);
+  do {
+    const std::string& g = c.cur();
+    if (g == "MESH") read_mesh(c, J);
+    else if (g == "BUNCH") read_bunch(c, J);
+    else if (g == "FIELD") read_field(c, J);
+    else if (g == "UNDULATOR") read_undulator(c, J);
+    else if (g == "EXTERNAL-FIELD") read_ext_field(c, J);
+    else if (g == "FEL-OUTPUT") read_fel(c, J);
+    else die(g + " is not a defined group.");
+    c.next();
+  } while (c.i < lines.size());
+  return J;
+}
+
+Job parse_job_file(const std::string& path) {
+  std::ifstream f(path);
+  if (!f.is_open()) die("Unable to open file");
+  std::vector<std::string> raw;
+  std::string line;
+  while (std::getline(f, line)) raw.push_back(line);
+  return parse_job_text(raw);
+}
+
+}  // namespace host
+}  // namespace mithra

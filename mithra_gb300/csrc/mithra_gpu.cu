@@ -1,0 +1,836 @@
+// Context, stage orchestration and C ABI of the GB300 FdTd library (see include/mithra_gpu.h).
+//
+// One context = one domain on one GPU, one CUDA stream.  All device state (three time levels of
+// A and phi, E/B, particles, power ring buffers, the time state) stays resident; a field step is
+// a fixed sequence of kernels that is captured once per buffer rotation into a CUDA graph and
+// replayed, so a march of many steps needs no host round trip.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mithra_gpu.h"
+#include "ctx.h"
+#include "field_kernels.cuh"
+#include "particle_kernels.cuh"
+#include "power_kernels.cuh"
+
+using namespace mithra;
+
+namespace mithra {
+
+int fail(mithra_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int grid_stride_blocks(const mithra_ctx* ctx, long long work, int block) {
+  long long b = (work + block - 1) / block;
+  long long cap = (long long)ctx->sm_count * 16;
+  return (int)std::max<long long>(1, std::min(b, cap));
+}
+
+int timer_begin(mithra_ctx* ctx, const char* name, int* slot, cudaEvent_t* a, cudaEvent_t* b) {
+  *slot = -1;
+  for (size_t i = 0; i < ctx->timers.size(); i++)
+    if (ctx->timers[i].name == name) *slot = (int)i;
+  if (*slot < 0) {
+    ctx->timers.push_back({name, 0.0, 0});
+    *slot = (int)ctx->timers.size() - 1;
+  }
+  if (ctx->ev_pool.size() >= 2) {
+    *a = ctx->ev_pool.back(); ctx->ev_pool.pop_back();
+    *b = ctx->ev_pool.back(); ctx->ev_pool.pop_back();
+  } else {
+    CK(cudaEventCreate(a));
+    CK(cudaEventCreate(b));
+  }
+  CK(cudaEventRecord(*a, ctx->stream));
+  return MITHRA_OK;
+}
+
+int timer_end(mithra_ctx* ctx, int slot, cudaEvent_t a, cudaEvent_t b) {
+  CK(cudaEventRecord(b, ctx->stream));
+  ctx->pending.push_back({slot, {a, b}});
+  return MITHRA_OK;
+}
+
+int harvest_timers(mithra_ctx* ctx) {
+  if (ctx->pending.empty()) return MITHRA_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (auto& pe : ctx->pending) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, pe.second.first, pe.second.second));
+    ctx->timers[pe.first].ms += ms;
+    ctx->timers[pe.first].launches += 1;
+    ctx->ev_pool.push_back(pe.second.first);
+    ctx->ev_pool.push_back(pe.second.second);
+  }
+  ctx->pending.clear();
+  return MITHRA_OK;
+}
+
+void invalidate_graphs(mithra_ctx* ctx) {
+  for (auto& gr : ctx->graph)
+    if (gr) { cudaGraphExecDestroy(gr); gr = nullptr; }
+}
+
+}  // namespace mithra
+
+namespace {
+
+constexpr int kPowerBlock = 128;
+
+// ---- stages (each one reference member function) ---------------------------------------------
+
+int run_potential(mithra_ctx* ctx, PotentialArgs<double> p, bool vector) {
+  const GridDev& g = ctx->g;
+  dim3 blk(32, 8), grd((g.N1 - 2 + 31) / 32, (g.N0 - 2 + 7) / 8, g.N2 - 2);
+  const long long nfaces = 2LL * ((long long)(g.N1 - 2) * (g.N2 - 2) + (long long)(g.N0 - 2) * (g.N2 - 2) +
+                                  (long long)(g.N0 - 2) * (g.N1 - 2));
+  const long long nedges = 4LL * ((g.N2 - 2) + (g.N0 - 2) + (g.N1 - 2));
+  int r;
+  if (g.solver == 1)
+    r = timed(ctx, vector ? "potential_interior_nsfd" : "scalar_interior_nsfd",
+              [&] { k_potential_interior<double, true><<<grd, blk, 0, ctx->stream>>>(g, p); });
+  else
+    r = timed(ctx, vector ? "potential_interior_fd" : "scalar_interior_fd",
+              [&] { k_potential_interior<double, false><<<grd, blk, 0, ctx->stream>>>(g, p); });
+  if (r) return r;
+  r = timed(ctx, vector ? "potential_faces" : "scalar_faces", [&] {
+    k_potential_faces<double><<<grid_stride_blocks(ctx, nfaces, 256), 256, 0, ctx->stream>>>(g, p);
+  });
+  if (r) return r;
+  if (g.order == 2) {
+    r = timed(ctx, vector ? "potential_edges" : "scalar_edges", [&] {
+      k_potential_edges<double><<<grid_stride_blocks(ctx, nedges, 256), 256, 0, ctx->stream>>>(g, p);
+    });
+    if (r) return r;
+    r = timed(ctx, vector ? "potential_corners" : "scalar_corners",
+              [&] { k_potential_corners<double><<<1, 32, 0, ctx->stream>>>(g, p); });
+    if (r) return r;
+  }
+  return MITHRA_OK;
+}
+
+int stage_eval_eb(mithra_ctx* ctx) {
+  const GridDev& g = ctx->g;
+  const double* fn = g.space_charge ? ctx->F[ctx->idx[1]] : nullptr;
+  EBArgs<double> eb{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], fn, ctx->E, ctx->B};
+  dim3 blk(32, 8), grd((g.N1 - 2 + 31) / 32, (g.N0 - 2 + 7) / 8, g.N2 - 2);
+  return timed(ctx, "eval_eb", [&] { k_eval_eb<double><<<grd, blk, 0, ctx->stream>>>(g, eb, 1, g.N2 - 2); });
+}
+
+int stage_field_update(mithra_ctx* ctx) {
+  if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_field_update(ctx);
+  const GridDev& g = ctx->g;
+  int r;
+  PotentialArgs<double> pa{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], ctx->A[ctx->idx[2]], 3, g.a[4]};
+  if ((r = run_potential(ctx, pa, true))) return r;
+  if (g.space_charge) {
+    PotentialArgs<double> pf{ctx->F[ctx->idx[0]], ctx->F[ctx->idx[1]], ctx->F[ctx->idx[2]], 1, g.a[5]};
+    if ((r = run_potential(ctx, pf, false))) return r;
+  }
+  return stage_eval_eb(ctx);
+}
+
+int stage_push(mithra_ctx* ctx, int save_rnm) {
+  if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_push(ctx, save_rnm);
+  int r = timed(ctx, "push", [&] {
+    k_push_fp64<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(
+        ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E, ctx->B, ctx->st, save_rnm);
+  });
+  if (r) return r;
+  return timed(ctx, "substep_end", [&] {
+    k_substep_end<double><<<1, 1024, 0, ctx->stream>>>(ctx->pt, ctx->st, ctx->P.bunch_time_step);
+  });
+}
+
+int stage_save_positions(mithra_ctx* ctx) {
+  if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_save_positions(ctx);
+  return timed(ctx, "save_positions", [&] {
+    k_save_positions<double><<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(ctx->pt, ctx->st);
+  });
+}
+
+int stage_erase(mithra_ctx* ctx) {
+  if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_erase(ctx);
+  return timed(ctx, "erase", [&] {
+    k_erase_outside<double><<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(ctx->g, ctx->pt, ctx->st);
+  });
+}
+
+int stage_power(mithra_ctx* ctx) {
+  for (size_t o = 0; o < ctx->power.size(); o++) {
+    PowerOut& po = ctx->power[o];
+    const int blocks = po.dev.N * po.dev.blocks_per_plane;
+    const size_t shm = (size_t)kPowerBlock * po.dev.Nl * sizeof(double);
+    int r = timed(ctx, "power_sample", [&] {
+      k_power_sample<kPowerBlock><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E, ctx->B, ctx->st);
+    });
+    if (r) return r;
+    const int last = (o + 1 == ctx->power.size());
+    r = timed(ctx, "power_finish", [&] { k_power_finish<<<1, 256, 0, ctx->stream>>>(po.dev, ctx->st, last); });
+    if (r) return r;
+  }
+  return MITHRA_OK;
+}
+
+void rotate(mithra_ctx* ctx) {
+  const int np1 = ctx->idx[0], n = ctx->idx[1], nm1 = ctx->idx[2];
+  ctx->idx[0] = nm1;
+  ctx->idx[1] = np1;
+  ctx->idx[2] = n;
+}
+
+int stage_current(mithra_ctx* ctx) {
+  if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_current(ctx);
+  const GridDev& g = ctx->g;
+  double* J = ctx->A[ctx->idx[0]];
+  CK(cudaMemsetAsync(J, 0, (size_t)3 * g.cstride * sizeof(double), ctx->stream));
+  double* rho = nullptr;
+  if (g.space_charge) {
+    rho = ctx->F[ctx->idx[0]];
+    CK(cudaMemsetAsync(rho, 0, (size_t)g.cstride * sizeof(double), ctx->stream));
+  }
+  return timed(ctx, "deposit", [&] {
+    k_deposit_fp64<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(g, ctx->pt, ctx->st, J, rho);
+  });
+}
+
+int stage_advance_time(mithra_ctx* ctx) {
+  return timed(ctx, "advance_time", [&] { k_advance_time<<<1, 32, 0, ctx->stream>>>(ctx->st, ctx->g.dt); });
+}
+
+// Number of iterations of `for (Double t = 0.0; t < nUpdateBunch_; t += 1.0)` (src/solver.cpp:1316).
+int n_substeps(const mithra_ctx* ctx) {
+  int n = 0;
+  for (double t = 0.0; t < ctx->push_desc.n_update_bunch; t += 1.0) n++;
+  return n;
+}
+
+// The body of the main loop of Solver::solve (src/solver.cpp:1300-1399), diagnostics other
+// than the power sample omitted.  Ends with the buffer rotation of FdTd::fieldShift.
+int enqueue_step(mithra_ctx* ctx) {
+  int r;
+  if ((r = stage_field_update(ctx))) return r;
+  const int ns = n_substeps(ctx);
+  for (int s = 0; s < ns; s++)
+    if ((r = stage_push(ctx, s == 0))) return r;
+  if (ns == 0 && (r = stage_save_positions(ctx))) return r;
+  if ((r = stage_erase(ctx))) return r;
+  if ((r = stage_power(ctx))) return r;
+  rotate(ctx);
+  if ((r = stage_current(ctx))) return r;
+  return stage_advance_time(ctx);
+}
+
+int ensure_rows(mithra_ctx* ctx, long long extra) {
+  if (ctx->power.empty()) return MITHRA_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  const long long need = ctx->st_host_rows() + extra;
+  if (need <= ctx->row_cap) return MITHRA_OK;
+  long long cap = std::max(need, 2 * ctx->row_cap + 64);
+  for (auto& po : ctx->power) {
+    const long long rowlen = (long long)po.dev.N * (1 + po.dev.Nl);
+    double* nr = nullptr;
+    CK(dalloc(&nr, (size_t)(cap * rowlen)));
+    if (po.rows) {
+      CK(cudaMemcpyAsync(nr, po.rows, (size_t)(ctx->row_cap * rowlen) * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      CK(cudaFree(po.rows));
+    }
+    po.rows = nr;
+    po.dev.rows = nr;
+    po.dev.row_cap = cap;
+  }
+  ctx->row_cap = cap;
+  invalidate_graphs(ctx);
+  return MITHRA_OK;
+}
+
+int check_state(mithra_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->st_host->overflow)
+    return fail(ctx, MITHRA_ERR_CAPACITY, "particle capacity %lld exceeded by z-face copies", ctx->st_host->capacity);
+  return MITHRA_OK;
+}
+
+}  // namespace
+
+long long mithra_ctx::st_host_rows() {
+  if (cudaMemcpyAsync(st_host, st, sizeof(StateDev), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return 0;
+  cudaStreamSynchronize(stream);
+  return st_host->n_power_rows;
+}
+
+// ---- C ABI ----------------------------------------------------------------------------------
+
+extern "C" {
+
+int mithra_gpu_last_error(const mithra_ctx* ctx, char* buf, size_t len) {
+  if (!ctx || !buf || !len) return MITHRA_ERR_ARG;
+  snprintf(buf, len, "%s", ctx->err.c_str());
+  return MITHRA_OK;
+}
+
+int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, int precision, int device,
+                      size_t particle_capacity, mithra_ctx** out) {
+  if (!gd || !pd || !out) return MITHRA_ERR_ARG;
+  *out = nullptr;
+  if (gd->N0 < 4 || gd->N1 < 4 || gd->N2 < 4) return MITHRA_ERR_ARG;
+  if (gd->solver != 0 && gd->solver != 1) return MITHRA_ERR_ARG;
+  if (gd->truncation_order != 1 && gd->truncation_order != 2) return MITHRA_ERR_ARG;
+  if (precision != MITHRA_PRECISION_FP64 && precision != MITHRA_PRECISION_FP32) return MITHRA_ERR_ARG;
+  mithra_ctx* ctx = new mithra_ctx();
+  ctx->device = device;
+  ctx->precision = precision;
+  ctx->grid_desc = *gd;
+  ctx->push_desc = *pd;
+  int rc = [&]() -> int {
+    CK(cudaSetDevice(device));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    ctx->sm_count = sms;
+    CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    GridDev& g = ctx->g;
+    g.N0 = gd->N0; g.N1 = gd->N1; g.N2 = gd->N2;
+    g.P1 = (int)round_up(gd->N1, 8);
+    g.plane = (long long)g.N0 * g.P1;
+    g.cstride = round_up((long long)g.N2 * g.plane, 64);
+    g.solver = gd->solver; g.order = gd->truncation_order; g.space_charge = gd->space_charge;
+    memcpy(g.a, gd->a, sizeof g.a);
+    g.nsfd_alpha = gd->nsfd_alpha; g.nsfd_beta = gd->nsfd_beta;
+    memcpy(g.bB, gd->bB, sizeof g.bB); memcpy(g.cB, gd->cB, sizeof g.cB); memcpy(g.dB, gd->dB, sizeof g.dB);
+    memcpy(g.eE, gd->eE, sizeof g.eE); memcpy(g.fE, gd->fE, sizeof g.fE); memcpy(g.gE, gd->gE, sizeof g.gE);
+    memcpy(g.hC, gd->hC, sizeof g.hC);
+    g.dt = gd->dt; g.dx = gd->dx; g.dy = gd->dy; g.dz = gd->dz;
+    g.xmin = gd->xmin; g.xmax = gd->xmax; g.ymin = gd->ymin; g.ymax = gd->ymax;
+    g.zmin = gd->zmin; g.zmax = gd->zmax; g.zp0 = gd->zp0; g.zp1 = gd->zp1; g.Lz = gd->Lz;
+    PushDev& P = ctx->P;
+    P.dtb = pd->dtb; P.r1 = pd->r1; P.r2 = pd->r2; P.gamma = pd->gamma; P.beta = pd->beta; P.c0 = pd->c0;
+    P.dt_shift = pd->dt_shift; P.bunch_time_step = pd->bunch_time_step; P.n_und = 0; P.und0_dist = 0.0;
+    CK(dalloc(&ctx->und_dev, kMaxUndulators));
+    const size_t nf = (size_t)3 * g.cstride;
+    ctx->capacity = std::max<size_t>(particle_capacity, 1);
+    if (precision == MITHRA_PRECISION_FP64) {
+      for (int b = 0; b < 3; b++) {
+        CK(dalloc(&ctx->A[b], nf));
+        CK(cudaMemsetAsync(ctx->A[b], 0, nf * sizeof(double), ctx->stream));
+        if (g.space_charge) {
+          CK(dalloc(&ctx->F[b], (size_t)g.cstride));
+          CK(cudaMemsetAsync(ctx->F[b], 0, (size_t)g.cstride * sizeof(double), ctx->stream));
+        }
+      }
+      ParticlesDev<double>& pt = ctx->pt;
+      const size_t c = ctx->capacity;
+      CK(dalloc(&pt.x, c)); CK(dalloc(&pt.y, c)); CK(dalloc(&pt.z, c));
+      CK(dalloc(&pt.gx, c)); CK(dalloc(&pt.gy, c)); CK(dalloc(&pt.gz, c));
+      CK(dalloc(&pt.mx, c)); CK(dalloc(&pt.my, c)); CK(dalloc(&pt.mz, c));
+      CK(dalloc(&pt.q, c)); CK(dalloc(&pt.e, c));
+      CK(dalloc(&pt.status, c)); CK(dalloc(&pt.cross, c));
+    } else {
+      int r = fp32_alloc(ctx);
+      if (r) return r;
+    }
+    CK(dalloc(&ctx->E, nf));
+    CK(dalloc(&ctx->B, nf));
+    CK(cudaMemsetAsync(ctx->E, 0, nf * sizeof(float), ctx->stream));
+    CK(cudaMemsetAsync(ctx->B, 0, nf * sizeof(float), ctx->stream));
+    CK(dalloc(&ctx->st, 1));
+    CK(cudaMallocHost((void**)&ctx->st_host, sizeof(StateDev)));
+    memset(ctx->st_host, 0, sizeof(StateDev));
+    ctx->st_host->capacity = (long long)ctx->capacity;
+    CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return MITHRA_OK;
+  }();
+  if (rc) {
+    char msg[512];
+    snprintf(msg, sizeof msg, "%s", ctx->err.c_str());
+    mithra_gpu_destroy(ctx);
+    fprintf(stderr, "mithra_gpu_create: %s\n", msg);
+    return rc;
+  }
+  *out = ctx;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_destroy(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  invalidate_graphs(ctx);
+  for (int b = 0; b < 3; b++) { cudaFree(ctx->A[b]); cudaFree(ctx->F[b]); }
+  ParticlesDev<double>& pt = ctx->pt;
+  void* ps[] = {pt.x, pt.y, pt.z, pt.gx, pt.gy, pt.gz, pt.mx, pt.my, pt.mz, pt.q, pt.e, pt.status, pt.cross};
+  for (void* p : ps) cudaFree(p);
+  fp32_free(ctx);
+  cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev);
+  if (ctx->st_host) cudaFreeHost(ctx->st_host);
+  for (auto& po : ctx->power) {
+    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
+    for (void* q : qs) cudaFree(q);
+  }
+  for (auto& pe : ctx->pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_synchronize(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return check_state(ctx);
+}
+
+int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und, int n) {
+  if (!ctx || n < 0 || n > MITHRA_MAX_UNDULATORS || (n && !und)) return MITHRA_ERR_ARG;
+  ctx->und_host.assign(n, UndDev{});
+  const double c0 = ctx->P.c0;
+  for (int u = 0; u < n; u++) {
+    UndDev& U = ctx->und_host[u];
+    U.type = und[u].type; U.k = und[u].k; U.lu = und[u].lu; U.rb = und[u].rb;
+    U.length = und[u].length; U.dist = und[u].dist; U.theta = und[u].theta;
+    // Solver::undulatorField, src/solver.cpp:1805-1812 (same expressions, evaluated once here).
+    U.b0 = (U.lu != 0.0) ? kEM * c0 * 2 * kPI / U.lu * U.k / kEC : 0.0;
+    U.ku = (U.lu != 0.0) ? 2 * kPI / U.lu : 0.0;
+    U.ct = cos(U.theta);
+    U.st = sin(U.theta);
+    U.ul = U.length * U.lu;
+    U.has_prev = u > 0;
+    U.has_next = u + 1 < n;
+    if (u > 0) U.r0_prev = und[u - 1].rb + und[u - 1].length * und[u - 1].lu - U.rb;  // src/beam.cc:35
+    if (u + 1 < n) U.r0_next = und[u + 1].rb - U.rb - U.length * U.lu;                  // src/beam.cc:60
+  }
+  ctx->P.n_und = n;
+  ctx->P.und0_dist = n ? und[0].dist : 0.0;
+  if (n) CK(cudaMemcpyAsync(ctx->und_dev, ctx->und_host.data(), n * sizeof(UndDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  invalidate_graphs(ctx);
+  return MITHRA_OK;
+}
+
+int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) {
+  if (!ctx || n < 0 || n > MITHRA_MAX_POWER_OUTPUTS || (n && !outs)) return MITHRA_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (auto& po : ctx->power) {
+    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
+    for (void* q : qs) cudaFree(q);
+  }
+  ctx->power.clear();
+  ctx->row_cap = 0;
+  const GridDev& g = ctx->g;
+  for (int o = 0; o < n; o++) {
+    const mithra_power_desc& d = outs[o];
+    if (d.N <= 0 || d.Nl < 0 || d.Nf <= 0 || !d.z || (d.Nl && (!d.twiddle_re || !d.twiddle_im))) return MITHRA_ERR_ARG;
+    PowerOut po;
+    std::vector<int> pk(d.N), ps(d.N);
+    std::vector<double> pz(d.N);
+    int nz = 0;
+    for (int k = 0; k < d.N; k++) {
+      // src/radiation.cpp:51-53 and :162-167
+      if (d.z[k] < g.zp1 && d.z[k] >= g.zp0) {
+        double c;
+        pz[k] = modf((d.z[k] - g.zmin) / g.dz, &c);
+        pk[k] = (int)c;
+        ps[k] = nz++;
+      } else {
+        pk[k] = -1; ps[k] = 0; pz[k] = 0.0;
+      }
+    }
+    PowerDev& pw = po.dev;
+    pw.N = d.N; pw.Nl = d.Nl; pw.Nf = d.Nf; pw.nz = std::max(nz, 1); pw.pc = d.pc;
+    pw.gamma = ctx->P.gamma; pw.beta = ctx->P.beta; pw.c0 = ctx->P.c0; pw.dt_shift = ctx->P.dt_shift;
+    pw.nodes_i = g.N0 - 4; pw.nodes_j = g.N1 - 4;
+    const long long nodes = (long long)pw.nodes_i * pw.nodes_j;
+    pw.blocks_per_plane = (int)std::max<long long>(1, (nodes + kPowerBlock - 1) / kPowerBlock);
+    CK(dalloc(&po.z, d.N)); CK(dalloc(&po.dzr, d.N)); CK(dalloc(&po.plane_k, d.N)); CK(dalloc(&po.plane_slot, d.N));
+    CK(dalloc(&po.tw_re, (size_t)d.Nl * d.Nf)); CK(dalloc(&po.tw_im, (size_t)d.Nl * d.Nf));
+    const size_t fdt_n = (size_t)d.Nf * 4 * pw.nz * (size_t)std::max<long long>(nodes, 1);
+    CK(dalloc(&po.fdt, fdt_n));
+    CK(cudaMemsetAsync(po.fdt, 0, fdt_n * sizeof(double), ctx->stream));
+    CK(dalloc(&po.partial, (size_t)d.N * pw.blocks_per_plane * std::max(d.Nl, 1)));
+    CK(cudaMemcpyAsync(po.z, d.z, d.N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(po.dzr, pz.data(), d.N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(po.plane_k, pk.data(), d.N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(po.plane_slot, ps.data(), d.N * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    if (d.Nl) {
+      CK(cudaMemcpyAsync(po.tw_re, d.twiddle_re, (size_t)d.Nl * d.Nf * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(po.tw_im, d.twiddle_im, (size_t)d.Nl * d.Nf * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    pw.z = po.z; pw.plane_k = po.plane_k; pw.plane_dzr = po.dzr; pw.plane_slot = po.plane_slot;
+    pw.tw_re = po.tw_re; pw.tw_im = po.tw_im; pw.fdt = po.fdt; pw.partial = po.partial;
+    pw.rows = nullptr; pw.row_cap = 0;
+    ctx->power.push_back(po);
+  }
+  // Reset the row log.
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->st_host->n_power_rows = 0;
+  CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+  invalidate_graphs(ctx);
+  return ensure_rows(ctx, 256);
+}
+
+int mithra_gpu_upload_fields(mithra_ctx* ctx, const double* anp1, const double* an, const double* anm1) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  const GridDev& g = ctx->g;
+  const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
+  double* staging = nullptr;
+  CK(dalloc(&staging, n));
+  const double* src[3] = {anp1, an, anm1};
+  for (int l = 0; l < 3; l++) {
+    if (!src[l]) continue;
+    CK(cudaMemcpyAsync(staging, src[l], n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_aos_to_soa<double, double><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, staging, ctx->A[ctx->idx[l]], 3);
+    else
+      k_aos_to_soa<float, double><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, staging, fp32_field(ctx, l), 3);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaFree(staging));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_download_fields(mithra_ctx* ctx, double* anp1, double* an, double* anm1) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  const GridDev& g = ctx->g;
+  const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
+  double* staging = nullptr;
+  CK(dalloc(&staging, n));
+  double* dst[3] = {anp1, an, anm1};
+  for (int l = 0; l < 3; l++) {
+    if (!dst[l]) continue;
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_soa_to_aos<double, double><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, ctx->A[ctx->idx[l]], staging, 3);
+    else
+      k_soa_to_aos<float, double><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, fp32_field(ctx, l), staging, 3);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  CK(cudaFree(staging));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_upload_scalar(mithra_ctx* ctx, const double* fnp1, const double* fn, const double* fnm1) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (!ctx->g.space_charge) return fail(ctx, MITHRA_ERR_STATE, "context has no scalar potential");
+  const GridDev& g = ctx->g;
+  const size_t n = (size_t)g.N0 * g.N1 * g.N2;
+  double* staging = nullptr;
+  CK(dalloc(&staging, n));
+  const double* src[3] = {fnp1, fn, fnm1};
+  for (int l = 0; l < 3; l++) {
+    if (!src[l]) continue;
+    CK(cudaMemcpyAsync(staging, src[l], n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_aos_to_soa<double, double><<<grid_stride_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g, staging, ctx->F[ctx->idx[l]], 1);
+    else
+      k_aos_to_soa<float, double><<<grid_stride_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g, staging, fp32_scalar(ctx, l), 1);
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaFree(staging));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_download_scalar(mithra_ctx* ctx, double* fnp1, double* fn, double* fnm1) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (!ctx->g.space_charge) return fail(ctx, MITHRA_ERR_STATE, "context has no scalar potential");
+  const GridDev& g = ctx->g;
+  const size_t n = (size_t)g.N0 * g.N1 * g.N2;
+  double* staging = nullptr;
+  CK(dalloc(&staging, n));
+  double* dst[3] = {fnp1, fn, fnm1};
+  for (int l = 0; l < 3; l++) {
+    if (!dst[l]) continue;
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_soa_to_aos<double, double><<<grid_stride_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g, ctx->F[ctx->idx[l]], staging, 1);
+    else
+      k_soa_to_aos<float, double><<<grid_stride_blocks(ctx, n, 256), 256, 0, ctx->stream>>>(g, fp32_scalar(ctx, l), staging, 1);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  CK(cudaFree(staging));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  const GridDev& g = ctx->g;
+  const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
+  float* staging = nullptr;
+  CK(dalloc(&staging, n));
+  float* dst[2] = {en, bn};
+  const float* srcs[2] = {ctx->E, ctx->B};
+  for (int l = 0; l < 2; l++) {
+    if (!dst[l]) continue;
+    k_soa_to_aos<float, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs[l], staging, 3);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  CK(cudaFree(staging));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
+  if (!ctx || (n && !rec)) return MITHRA_ERR_ARG;
+  if (n > ctx->capacity) return fail(ctx, MITHRA_ERR_CAPACITY, "%zu particles exceed capacity %zu", n, ctx->capacity);
+  double* staging = nullptr;
+  CK(dalloc(&staging, n * 11));
+  if (n) CK(cudaMemcpyAsync(staging, rec, n * 11 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->precision == MITHRA_PRECISION_FP64) {
+    k_records_to_soa<<<grid_stride_blocks(ctx, (long long)n, 256), 256, 0, ctx->stream>>>(staging, (long long)n, ctx->pt);
+    CK(cudaGetLastError());
+  } else {
+    int r = fp32_records_to_soa(ctx, staging, (long long)n);
+    if (r) return r;
+  }
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->st_host->n_particles = (long long)n;
+  ctx->st_host->n_cross = 0;
+  ctx->st_host->overflow = 0;
+  CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaFree(staging));
+  ctx->particles_loaded = true;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_particle_count(mithra_ctx* ctx, size_t* n) {
+  if (!ctx || !n) return MITHRA_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  *n = (size_t)ctx->st_host->n_particles;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_download_particles(mithra_ctx* ctx, double* rec, size_t cap, size_t* n) {
+  if (!ctx || !n || (cap && !rec)) return MITHRA_ERR_ARG;
+  size_t slots = 0;
+  int r = mithra_gpu_particle_count(ctx, &slots);
+  if (r) return r;
+  double* staging = nullptr;
+  long long* dn = nullptr;
+  CK(dalloc(&staging, std::max<size_t>(slots, 1) * 11));
+  CK(dalloc(&dn, 1));
+  if (ctx->precision == MITHRA_PRECISION_FP64) {
+    k_soa_to_records<<<1, 1024, 0, ctx->stream>>>(ctx->pt, ctx->st, staging, (long long)slots, dn);
+    CK(cudaGetLastError());
+  } else {
+    r = fp32_soa_to_records(ctx, staging, (long long)slots, dn);
+    if (r) return r;
+  }
+  long long live = 0;
+  CK(cudaMemcpyAsync(&live, dn, sizeof live, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const size_t take = std::min<size_t>((size_t)live, cap);
+  if (take) CK(cudaMemcpyAsync(rec, staging, take * 11 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaFree(staging));
+  CK(cudaFree(dn));
+  *n = (size_t)live;
+  if ((size_t)live > cap) return fail(ctx, MITHRA_ERR_CAPACITY, "buffer holds %zu of %lld particles", cap, live);
+  return MITHRA_OK;
+}
+
+int mithra_gpu_set_time(mithra_ctx* ctx, const mithra_time_state* t) {
+  if (!ctx || !t) return MITHRA_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->st_host->time = t->time;
+  ctx->st_host->time_bunch = t->time_bunch;
+  ctx->st_host->n_time = t->n_time;
+  ctx->st_host->n_time_bunch = t->n_time_bunch;
+  CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_get_time(mithra_ctx* ctx, mithra_time_state* t) {
+  if (!ctx || !t) return MITHRA_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  t->time = ctx->st_host->time;
+  t->time_bunch = ctx->st_host->time_bunch;
+  t->n_time = ctx->st_host->n_time;
+  t->n_time_bunch = ctx->st_host->n_time_bunch;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_field_update(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  int r = stage_field_update(ctx);
+  if (r) return r;
+  return harvest_timers(ctx);
+}
+
+int mithra_gpu_save_positions(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  return stage_save_positions(ctx);
+}
+
+int mithra_gpu_bunch_update(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
+  int r = stage_push(ctx, 0);
+  if (r) return r;
+  if ((r = harvest_timers(ctx))) return r;
+  return check_state(ctx);
+}
+
+int mithra_gpu_recycle(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  return stage_erase(ctx);
+}
+
+int mithra_gpu_power_sample(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  int r = ensure_rows(ctx, 1);
+  if (r) return r;
+  return stage_power(ctx);
+}
+
+int mithra_gpu_field_shift(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  rotate(ctx);
+  return MITHRA_OK;
+}
+
+int mithra_gpu_current_update(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  int r = stage_current(ctx);
+  if (r) return r;
+  return stage_erase(ctx);
+}
+
+int mithra_gpu_advance_time(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  return stage_advance_time(ctx);
+}
+
+int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
+  if (!ctx || nsteps < 0) return MITHRA_ERR_ARG;
+  if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
+  int r = ensure_rows(ctx, nsteps);
+  if (r) return r;
+  if (ctx->timing) {
+    for (int64_t s = 0; s < nsteps; s++) {
+      if ((r = enqueue_step(ctx))) return r;
+      if ((r = harvest_timers(ctx))) return r;
+    }
+    return check_state(ctx);
+  }
+  for (int64_t s = 0; s < nsteps; s++) {
+    const int key = ctx->idx[0];
+    if (!ctx->graph[key]) {
+      cudaGraph_t graph;
+      const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
+      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      r = enqueue_step(ctx);
+      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+      if (r) return r;
+      if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      CK(cudaGraphInstantiate(&ctx->graph[key], graph, 0));
+      CK(cudaGraphDestroy(graph));
+      // enqueue_step rotated the indices while recording; restore them for the launch below.
+      ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
+    }
+    CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
+    rotate(ctx);
+  }
+  return check_state(ctx);
+}
+
+int mithra_gpu_run_prelude(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
+  mithra_time_state t;
+  int r = mithra_gpu_get_time(ctx, &t);
+  if (r) return r;
+  if (!(t.time < 0.0)) return MITHRA_OK;
+  // No field update happens before time zero, so the lazily evaluated E/B of the reference are
+  // those of the initial potentials throughout the prelude.
+  if ((r = stage_eval_eb(ctx))) return r;
+  const int ns = n_substeps(ctx);
+  while (t.time < 0.0) {
+    for (int s = 0; s < ns; s++)
+      if ((r = stage_push(ctx, s == 0))) return r;
+    if (ns == 0 && (r = stage_save_positions(ctx))) return r;
+    if ((r = stage_erase(ctx))) return r;
+    if ((r = stage_advance_time(ctx))) return r;
+    if ((r = harvest_timers(ctx))) return r;
+    if ((r = mithra_gpu_get_time(ctx, &t))) return r;
+  }
+  return check_state(ctx);
+}
+
+int mithra_gpu_power_rows(mithra_ctx* ctx, double* out, size_t cap_values, size_t* n_values) {
+  if (!ctx || !n_values) return MITHRA_ERR_ARG;
+  CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const long long rows = std::min(ctx->st_host->n_power_rows, ctx->row_cap);
+  size_t per_row = 0;
+  for (auto& po : ctx->power) per_row += (size_t)po.dev.N * (1 + po.dev.Nl);
+  const size_t need = per_row * (size_t)rows;
+  *n_values = need;
+  if (!out) return MITHRA_OK;
+  if (cap_values < need) return fail(ctx, MITHRA_ERR_ARG, "power row buffer too small (%zu < %zu)", cap_values, need);
+  std::vector<double> tmp;
+  size_t w = 0;
+  for (long long r = 0; r < rows; r++)
+    for (auto& po : ctx->power) {
+      const size_t rowlen = (size_t)po.dev.N * (1 + po.dev.Nl);
+      CK(cudaMemcpyAsync(out + w, po.rows + r * rowlen, rowlen * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      w += rowlen;
+    }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->st_host->n_power_rows = 0;
+  CK(cudaMemcpyAsync(&ctx->st->n_power_rows, &ctx->st_host->n_power_rows, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_enable_timing(mithra_ctx* ctx, int on) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  int r = harvest_timers(ctx);
+  if (r) return r;
+  ctx->timing = on != 0;
+  for (auto& t : ctx->timers) { t.ms = 0.0; t.launches = 0; }
+  return MITHRA_OK;
+}
+
+int mithra_gpu_kernel_times(mithra_ctx* ctx, char* names, size_t name_len, double* ms, int cap, int* n) {
+  if (!ctx || !n) return MITHRA_ERR_ARG;
+  int r = harvest_timers(ctx);
+  if (r) return r;
+  *n = (int)ctx->timers.size();
+  for (int i = 0; i < std::min(cap, *n); i++) {
+    if (names) snprintf(names + (size_t)i * name_len, name_len, "%s", ctx->timers[i].name.c_str());
+    if (ms) {
+      ms[2 * i] = ctx->timers[i].ms;
+      ms[2 * i + 1] = (double)ctx->timers[i].launches;
+    }
+  }
+  return MITHRA_OK;
+}
+
+}  // extern "C"

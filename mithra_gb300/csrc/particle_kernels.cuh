@@ -1,0 +1,359 @@
+// Particle kernels of the FP64 form: the bunch push (gather + Boris + drift with the analytic
+// static-undulator field), the single-domain z-face exchange, particle erasure and the
+// zigzag current deposit.
+#pragma once
+#include "device_common.cuh"
+
+namespace mithra {
+
+// Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
+// Solver::staticUndulator (src/beam.cc:14-76).  Adds the lab-frame undulator field, boosted
+// into the bunch frame, to bt/et.
+__device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
+                                                       const PushDev& P, double timeBunch,
+                                                       double x, double y, double z,
+                                                       double* bt, double* et) {
+  for (int u = 0; u < n_und; u++) {
+    const UndDev& U = und[u];
+    if (U.type != 0) continue;
+    const double lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift)) - U.rb;
+    const double ly = x * U.ct + y * U.st;
+    double s_ly, c_ly;
+    {
+      const double kl = U.ku * ly;
+      s_ly = sinh(kl);
+      c_ly = cosh(kl);
+    }
+    double d1, bz;
+    if (lz >= 0.0 && lz <= U.ul) {
+      double sn, cs;
+      sincos(U.ku * lz, &sn, &cs);
+      d1 = U.b0 * c_ly * sn * P.gamma;
+      bz = U.b0 * s_ly * cs;
+    } else {
+      double t0 = (lz < 0.0) ? lz : lz - U.ul;
+      const double kt = U.ku * t0;
+      double sz = exp(-(kt * kt) / 2.0);
+      const bool has = (lz < 0.0) ? U.has_prev : U.has_next;
+      if (has) {
+        const double r0 = (lz < 0.0) ? U.r0_prev : U.r0_next;
+        const bool cut = (lz < 0.0) ? (lz < r0 || r0 == 0.0) : (t0 > r0 || r0 == 0.0);
+        if (cut) sz = 0.0;
+        else
+          sz *= 0.35875 + 0.48829 * cos(kPI * t0 / r0) + 0.14128 * cos(2.0 * kPI * t0 / r0) +
+                0.01168 * cos(3.0 * kPI * t0 / r0);
+      }
+      d1 = U.b0 * c_ly * sz * U.ku * t0 * P.gamma;
+      bz = U.b0 * s_ly * sz;
+    }
+    bt[0] += d1 * U.ct;
+    bt[1] += d1 * U.st;
+    bt[2] += bz;
+    d1 *= P.c0 * P.beta;
+    et[1] += d1 * U.ct;
+    et[0] += -d1 * U.st;
+  }
+}
+
+// One Solver::bunchUpdate for every particle (src/solver.cpp:1424-1549).
+// save_rnm: also perform `rnm = rnp` first (src/solver.cpp:1311-1312).
+__global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const UndDev* __restrict__ und,
+                                                   ParticlesDev<double> pt, const float* __restrict__ E,
+                                                   const float* __restrict__ B, StateDev* st, int save_rnm) {
+  const long long n = st->n_particles;
+  const double timeBunch = st->time_bunch;
+  const long long cs = g.cstride;
+  unsigned long long local_cross = 0, local_nt = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int8_t cross = 0;
+    if (!(pt.status[p] & 1)) {
+      double x = pt.x[p], y = pt.y[p], z = pt.z[p];
+      if (save_rnm) { pt.mx[p] = x; pt.my[p] = y; pt.mz[p] = z; }
+      double zr = pmod_d(z - g.zmin, g.Lz) + g.zmin;
+      if ((zr >= g.zp0) && (zr < g.zp1)) {
+        const bool b1x = (x < g.xmax - g.dx && x > g.xmin + g.dx);
+        const bool b1y = (y < g.ymax - g.dy && y > g.ymin + g.dy);
+        const bool b1z = (z < g.zp1 && z >= g.zp0);
+        double bt[3] = {0.0, 0.0, 0.0}, et[3] = {0.0, 0.0, 0.0};
+        static_undulator_field(und, P.n_und, P, timeBunch, x, y, z, bt, et);
+        double e = pt.e[p];
+        if (e == 1.0) {
+          if (b1x && b1y && b1z) {
+            double d1;
+            const double dxr = modf((x - g.xmin) / g.dx, &d1); const int i = (int)d1;
+            const double dyr = modf((y - g.ymin) / g.dy, &d1); const int j = (int)d1;
+            const double dzr = modf((z - g.zmin) / g.dz, &d1); const int k = (int)d1;
+            const long long m = node_index(g, k, i, j);
+            const long long sI = g.P1, sK = g.plane;
+            const double wx0 = 1.0 - dxr, wy0 = 1.0 - dyr, wz0 = 1.0 - dzr;
+            const double w[8] = {wx0 * wy0 * wz0, dxr * wy0 * wz0, wx0 * dyr * wz0, dxr * dyr * wz0,
+                                 wx0 * wy0 * dzr, dxr * wy0 * dzr, wx0 * dyr * dzr, dxr * dyr * dzr};
+            const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              double se = et[c], sb = bt[c];
+#pragma unroll
+              for (int q = 0; q < 8; q++) {
+                se += w[q] * (double)__ldg(E + c * cs + nd[q]);
+                sb += w[q] * (double)__ldg(B + c * cs + nd[q]);
+              }
+              et[c] = se; bt[c] = sb;
+            }
+          } else if (!b1x && !b1y && b1z) {
+            local_nt++;
+          }
+        } else if (P.n_und > 0) {
+          const double lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift));
+          e = (lz > -P.und0_dist) ? 1.0 : 0.0;
+          pt.e[p] = e;
+        } else {
+          pt.e[p] = 1.0;
+        }
+        // Boris rotation, src/solver.cpp:1519-1535.
+        double gx = pt.gx[p], gy = pt.gy[p], gz = pt.gz[p];
+        const double mx = gx + P.r1 * et[0], my = gy + P.r1 * et[1], mz = gz + P.r1 * et[2];
+        const double d1 = sqrt(1.0 + (mx * mx + my * my + mz * mz));
+        const double f = P.r2 / d1;
+        const double px = f * (my * bt[2] - mz * bt[1]) + mx;
+        const double py = f * (mz * bt[0] - mx * bt[2]) + my;
+        const double pz = f * (mx * bt[1] - my * bt[0]) + mz;
+        const double bt2 = bt[0] * bt[0] + bt[1] * bt[1] + bt[2] * bt[2];
+        const double s = 2.0 / (d1 / P.r2 + P.r2 / d1 * bt2);
+        gx = s * (py * bt[2] - pz * bt[1]) + mx + P.r1 * et[0];
+        gy = s * (pz * bt[0] - px * bt[2]) + my + P.r1 * et[1];
+        gz = s * (px * bt[1] - py * bt[0]) + mz + P.r1 * et[2];
+        pt.gx[p] = gx; pt.gy[p] = gy; pt.gz[p] = gz;
+        // Drift, src/solver.cpp:1538-1541.
+        const double gg = P.dtb / sqrt(1.0 + (gx * gx + gy * gy + gz * gz));
+        const double drz = gg * gz;
+        pt.x[p] = x + gg * gx; pt.y[p] = y + gg * gy; pt.z[p] = z + drz;
+        zr += drz;
+        if (zr < g.zp0) cross = 1;
+        else if (zr >= g.zp1) cross = 2;
+      }
+    }
+    pt.cross[p] = cross;
+    local_cross += (cross != 0);
+  }
+  // Block-aggregated counters.
+  for (int o = 16; o > 0; o >>= 1) {
+    local_cross += __shfl_down_sync(0xffffffffu, local_cross, o);
+    local_nt += __shfl_down_sync(0xffffffffu, local_nt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (local_cross) atomicAdd(&st->n_cross, local_cross);
+    if (local_nt) atomicAdd(&st->n_transverse, local_nt);
+  }
+}
+
+// After each push: the single-rank self-exchange of src/solver.cpp:1551-1568 appends a copy of
+// every particle that crossed below zp0 (first) and then of every one that crossed at or above
+// zp1, each group in particle order; then timeBunch_ += dt_b, ++nTimeBunch_ (src/solver.cpp:1319).
+// One block; the ordered append runs only when a crossing happened.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_substep_end(ParticlesDev<T> pt, StateDev* st, double bunch_time_step) {
+  __shared__ long long s_base;
+  __shared__ int s_warp[32];
+  const unsigned long long ncross = st->n_cross;
+  if (ncross) {
+    const long long n = st->n_particles;
+    if (threadIdx.x == 0) s_base = n;
+    __syncthreads();
+    if ((long long)(n + ncross) > st->capacity) {
+      if (threadIdx.x == 0) st->overflow = 1;
+    } else {
+      for (int pass = 1; pass <= 2; pass++) {
+        for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
+          const long long p = c0 + threadIdx.x;
+          const int take = (p < n) && (pt.cross[p] == pass);
+          const unsigned bal = __ballot_sync(0xffffffffu, take);
+          const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+          if (lane == 0) s_warp[warp] = __popc(bal);
+          __syncthreads();
+          int before = 0, total = 0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            if (w < warp) before += s_warp[w];
+            total += s_warp[w];
+          }
+          before += __popc(bal & ((1u << lane) - 1u));
+          if (take) {
+            const long long d = s_base + before;
+            pt.x[d] = pt.x[p]; pt.y[d] = pt.y[p]; pt.z[d] = pt.z[p];
+            pt.gx[d] = pt.gx[p]; pt.gy[d] = pt.gy[p]; pt.gz[d] = pt.gz[p];
+            pt.mx[d] = pt.mx[p]; pt.my[d] = pt.my[p]; pt.mz[d] = pt.mz[p];
+            pt.q[d] = pt.q[p]; pt.e[d] = pt.e[p];
+            pt.status[d] = pt.status[p]; pt.cross[d] = 0;
+          }
+          __syncthreads();
+          if (threadIdx.x == 0) s_base += total;
+          __syncthreads();
+        }
+      }
+      if (threadIdx.x == 0) st->n_particles = s_base;
+    }
+  }
+  if (threadIdx.x == 0) {
+    st->n_cross = 0;
+    st->time_bunch += bunch_time_step;
+    st->n_time_bunch += 1;
+  }
+}
+
+// time_ += dt; ++nTime_ (src/solver.cpp:1396-1399).
+__global__ void k_advance_time(StateDev* st, double dt) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    st->time += dt;
+    st->n_time += 1;
+  }
+}
+
+// Solver::recycleParticles / the erasure in FdTd::currentCommunicate (src/solver.cpp:493-503,
+// src/fdtd.cpp:214-224): erase particles whose wrapped z lies outside [zp0, zp1).
+template <typename T>
+__global__ void __launch_bounds__(256) k_erase_outside(GridDev g, ParticlesDev<T> pt, StateDev* st) {
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (pt.status[p] & 1) continue;
+    const double zr = pmod_d((double)pt.z[p] - g.zmin, g.Lz) + g.zmin;
+    if (zr < g.zp0 || zr >= g.zp1) pt.status[p] |= 1;
+  }
+}
+
+// FdTd::currentUpdate, zigzag (Umeda) deposit (src/fdtd.cpp:38-185), FP64 atomics into J
+// (the anp1 buffer, zeroed before).  With rho != nullptr also the charge deposit of
+// src/fdtdSC.cpp:140-161.
+__device__ __forceinline__ void deposit_half(double* J, long long cs, long long m, long long sI, long long sK,
+                                             double qh, double dxh, double dyh, double dzh, double jx,
+                                             double jy, double jz) {
+  const double x1 = 1.0 - dxh, x2 = dxh, y1 = 1.0 - dyh, y2 = dyh, z1 = 1.0 - dzh, z2 = dzh;
+  const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+  const double wx[8] = {y1 * z1, y1 * z1, y2 * z1, y2 * z1, y1 * z2, y1 * z2, y2 * z2, y2 * z2};
+  const double wy[8] = {x1 * z1, x2 * z1, x1 * z1, x2 * z1, x1 * z2, x2 * z2, x1 * z2, x2 * z2};
+  const double wz[8] = {x1 * y1, x2 * y1, x1 * y2, x2 * y2, x1 * y1, x2 * y1, x1 * y2, x2 * y2};
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    atomicAdd(J + nd[q], qh * wx[q] * jx);
+    atomicAdd(J + cs + nd[q], qh * wy[q] * jy);
+    atomicAdd(J + 2 * cs + nd[q], qh * wz[q] * jz);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<double> pt, const StateDev* st,
+                                                      double* J, double* rho) {
+  const long long n = st->n_particles;
+  const long long cs = g.cstride, sI = g.P1, sK = g.plane;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (pt.status[p] & 1) continue;
+    const double rp0 = pt.x[p], rp1 = pt.y[p], rp2 = pt.z[p];
+    const double rm0 = pt.mx[p], rm1 = pt.my[p], rm2 = pt.mz[p];
+    const bool bp = (rp0 < g.xmax - g.dx && rp0 > g.xmin + g.dx && rp1 < g.ymax - g.dy &&
+                     rp1 > g.ymin + g.dy && rp2 < g.zp1 && rp2 >= g.zp0);
+    const bool bm = (rm0 < g.xmax - g.dx && rm0 > g.xmin + g.dx && rm1 < g.ymax - g.dy &&
+                     rm1 > g.ymin + g.dy && rm2 < g.zp1 && rm2 >= g.zp0);
+    if (!(bp || bm)) continue;
+    const double qh = pt.q[p] * 0.5;
+    const int ip = (int)floor((rp0 - g.xmin) / g.dx), jp = (int)floor((rp1 - g.ymin) / g.dy),
+              kp = (int)floor((rp2 - g.zmin) / g.dz);
+    const int im = (int)floor((rm0 - g.xmin) / g.dx), jm = (int)floor((rm1 - g.ymin) / g.dy),
+              km = (int)floor((rm2 - g.zmin) / g.dz);
+    const double r0 = fmin(min(im, ip) * g.dx + g.dx + g.xmin, fmax(max(im, ip) * g.dx + g.xmin, 0.5 * (rm0 + rp0)));
+    const double r1 = fmin(min(jm, jp) * g.dy + g.dy + g.ymin, fmax(max(jm, jp) * g.dy + g.ymin, 0.5 * (rm1 + rp1)));
+    const double r2 = fmin(min(km, kp) * g.dz + g.dz + g.zmin, fmax(max(km, kp) * g.dz + g.zmin, 0.5 * (rm2 + rp2)));
+    double c;
+    if (bp) {
+      const long long m = node_index(g, kp, ip, jp);
+      const double dxp = modf((0.5 * (rp0 + r0) - g.xmin) / g.dx, &c);
+      const double dyp = modf((0.5 * (rp1 + r1) - g.ymin) / g.dy, &c);
+      const double dzp = modf((0.5 * (rp2 + r2) - g.zmin) / g.dz, &c);
+      deposit_half(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
+      if (rho) {
+        const double fx = modf((rp0 - g.xmin) / g.dx, &c), fy = modf((rp1 - g.ymin) / g.dy, &c),
+                     fz = modf((rp2 - g.zmin) / g.dz, &c);
+        const double q = pt.q[p];
+        const double x1 = 1.0 - fx, y1 = 1.0 - fy, z1 = 1.0 - fz;
+        atomicAdd(rho + m, q * x1 * y1 * z1);
+        atomicAdd(rho + m + sI, q * fx * y1 * z1);
+        atomicAdd(rho + m + 1, q * x1 * fy * z1);
+        atomicAdd(rho + m + sI + 1, q * fx * fy * z1);
+        atomicAdd(rho + m + sK, q * x1 * y1 * fz);
+        atomicAdd(rho + m + sK + sI, q * fx * y1 * fz);
+        atomicAdd(rho + m + sK + 1, q * x1 * fy * fz);
+        atomicAdd(rho + m + sK + sI + 1, q * fx * fy * fz);
+      }
+    }
+    if (bm) {
+      const long long m = node_index(g, km, im, jm);
+      const double dxm = modf((0.5 * (rm0 + r0) - g.xmin) / g.dx, &c);
+      const double dym = modf((0.5 * (rm1 + r1) - g.ymin) / g.dy, &c);
+      const double dzm = modf((0.5 * (rm2 + r2) - g.zmin) / g.dz, &c);
+      deposit_half(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
+    }
+  }
+}
+
+// rnm = rnp (src/solver.cpp:1311-1312) as a stand-alone stage.
+template <typename T>
+__global__ void k_save_positions(ParticlesDev<T> pt, const StateDev* st) {
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    pt.mx[p] = pt.x[p]; pt.my[p] = pt.y[p]; pt.mz[p] = pt.z[p];
+  }
+}
+
+// Particle records (11 doubles) <-> device SoA.
+__global__ void k_records_to_soa(const double* __restrict__ rec, long long n, ParticlesDev<double> pt) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double* r = rec + 11 * p;
+    pt.q[p] = r[0];
+    pt.x[p] = r[1]; pt.y[p] = r[2]; pt.z[p] = r[3];
+    pt.mx[p] = r[4]; pt.my[p] = r[5]; pt.mz[p] = r[6];
+    pt.gx[p] = r[7]; pt.gy[p] = r[8]; pt.gz[p] = r[9];
+    pt.e[p] = r[10];
+    pt.status[p] = 0; pt.cross[p] = 0;
+  }
+}
+
+// Gathers the live particles in slot order (erased ones removed, as the reference's list
+// erasure does) into 11-double records.  One block: slot order is preserved by a block scan.
+__global__ void __launch_bounds__(1024) k_soa_to_records(ParticlesDev<double> pt, const StateDev* st,
+                                                         double* rec, long long cap, long long* n_out) {
+  __shared__ int s_warp[32];
+  __shared__ long long s_base;
+  const long long n = st->n_particles;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
+    const long long p = c0 + threadIdx.x;
+    const int take = (p < n) && !(pt.status[p] & 1);
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      if (w < warp) before += s_warp[w];
+      total += s_warp[w];
+    }
+    before += __popc(bal & ((1u << lane) - 1u));
+    const long long d = s_base + before;
+    if (take && d < cap) {
+      double* r = rec + 11 * d;
+      r[0] = pt.q[p];
+      r[1] = pt.x[p]; r[2] = pt.y[p]; r[3] = pt.z[p];
+      r[4] = pt.mx[p]; r[5] = pt.my[p]; r[6] = pt.mz[p];
+      r[7] = pt.gx[p]; r[8] = pt.gy[p]; r[9] = pt.gz[p];
+      r[10] = pt.e[p];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *n_out = s_base;
+}
+
+}  // namespace mithra
