@@ -133,6 +133,9 @@ int mithra_gpu_get_time(mithra_ctx* ctx, mithra_time_state* t);
 /* FdTd::fieldUpdate / FdTdSC::fieldUpdate without the MPI halo, plus the eager equivalent of
  * the lazy FdTd::fieldEvaluate (src/fdtd.cpp:231-800, :818-845). */
 int mithra_gpu_field_update(mithra_ctx* ctx);
+/* FdTd::fieldEvaluate (src/fdtd.cpp:818-845) at every interior node from the current anp1/an,
+ * plus the plane copies of src/fdtd.cpp:755-772; field_update already includes it. */
+int mithra_gpu_field_evaluate(mithra_ctx* ctx);
 /* `rnm = rnp` for all particles (src/solver.cpp:1311-1312). */
 int mithra_gpu_save_positions(mithra_ctx* ctx);
 /* One Solver::bunchUpdate (src/solver.cpp:1424-1576) followed by timeBunch_ += bunch time step

@@ -88,6 +88,7 @@ _SIGS = {
     "mithra_gpu_set_time": [_vp, _P(TimeState)],
     "mithra_gpu_get_time": [_vp, _P(TimeState)],
     "mithra_gpu_field_update": [_vp],
+    "mithra_gpu_field_evaluate": [_vp],
     "mithra_gpu_save_positions": [_vp],
     "mithra_gpu_bunch_update": [_vp],
     "mithra_gpu_recycle": [_vp],
@@ -359,6 +360,9 @@ class Context:
     # Stages, one per reference member function.
     def field_update(self):
         self.call("mithra_gpu_field_update")
+
+    def field_evaluate(self):
+        self.call("mithra_gpu_field_evaluate")
 
     def save_positions(self):
         self.call("mithra_gpu_save_positions")

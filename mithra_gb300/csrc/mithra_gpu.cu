@@ -683,6 +683,13 @@ int mithra_gpu_field_update(mithra_ctx* ctx) {
   return harvest_timers(ctx);
 }
 
+int mithra_gpu_field_evaluate(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  int r = ctx->precision == MITHRA_PRECISION_FP32 ? fp32_eval_eb(ctx) : stage_eval_eb(ctx);
+  if (r) return r;
+  return harvest_timers(ctx);
+}
+
 int mithra_gpu_save_positions(mithra_ctx* ctx) {
   if (!ctx) return MITHRA_ERR_ARG;
   return stage_save_positions(ctx);

@@ -200,6 +200,41 @@ static void pre_loop(Solver* s) {
   }
 }
 
+/* FdTd::fieldEvaluate reads the potentials through the uf_ pointers that fieldUpdate sets
+ * (src/fdtd.cpp:240-245); modes that evaluate fields without a field update set them here. */
+static void bind_field_pointers(Solver* s) {
+  s->uf_.anp1 = &(*s->anp1_)[0][0];
+  s->uf_.an = &(*s->an_)[0][0];
+  s->uf_.anm1 = &(*s->anm1_)[0][0];
+  s->uf_.jn = &(*s->anp1_)[0][0];
+  s->uf_.en = &s->en_[0][0];
+  s->uf_.bn = &s->bn_[0][0];
+  if (s->mesh_.spaceCharge_) {
+    s->uf_.fnp1 = &(*s->fnp1_)[0];
+    s->uf_.fn = &(*s->fn_)[0];
+    s->uf_.fnm1 = &(*s->fnm1_)[0];
+    s->uf_.rn = &(*s->fnp1_)[0];
+  }
+}
+
+/* The E/B state FdTd::fieldUpdate leaves behind (src/fdtd.cpp:742-774): planes k = 1 and
+ * np-2 evaluated, copied into k = 0 and np-1, and flagged as evaluated. */
+static void eval_boundary_planes(Solver* s) {
+  for (int i = 1; i < s->N0_ - 1; i++)
+    for (int j = 1; j < s->N1_ - 1; j++) {
+      long m = s->N1N0_ + s->N1_ * i + j;
+      s->fieldEvaluate(m);
+      s->pic_[m - s->N1N0_] = true;
+      s->en_[m - s->N1N0_] = s->en_[m];
+      s->bn_[m - s->N1N0_] = s->bn_[m];
+      m = (long)s->N1N0_ * (s->np_ - 2) + s->N1_ * i + j;
+      s->fieldEvaluate(m);
+      s->pic_[m + s->N1N0_] = true;
+      s->en_[m + s->N1N0_] = s->en_[m];
+      s->bn_[m + s->N1N0_] = s->bn_[m];
+    }
+}
+
 static void dump_state(Solver* s, const std::string& dir) {
   mkdir(dir.c_str(), 0755);
   dump_meta(s, jp(dir, "meta.txt"));
@@ -279,6 +314,8 @@ int main(int argc, char** argv) {
     std::vector<char> tb = read_raw(jp(in, "timebunch.bin"));
     memcpy(&s->timeBunch_, tb.data(), 8);
     std::fill(s->pic_.begin(), s->pic_.end(), false);
+    bind_field_pointers(s);
+    eval_boundary_planes(s);
     s->bunchUpdate();
     dump_particles(jp(out, "particles.bin"), s->chargeVectorn_);
   } else if (mode == "deposit") {
@@ -300,6 +337,8 @@ int main(int argc, char** argv) {
       load_vec3(jp(in, "an_" + std::to_string(t) + ".bin"), s->an_);
       load_vec3(jp(in, "anp1_" + std::to_string(t) + ".bin"), s->anp1_);
       std::fill(s->pic_.begin(), s->pic_.end(), false);
+      bind_field_pointers(s);
+      eval_boundary_planes(s);
       s->powerSample();
       for (size_t jf = 0; jf < s->FEL_.size(); jf++) {
         if (!s->FEL_[jf].radiationPower_.sampling_) continue;

@@ -1,0 +1,18 @@
+"""Loading helpers for the golden vectors produced by tests/golden/make_golden.py."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def load(tag: str, name: str):
+    return np.load(os.path.join(GOLDEN, tag, name + ".npz"))
+
+
+def meta(tag: str) -> dict:
+    z = load(tag, "init")
+    return {str(k): float(v) for k, v in zip(z["meta_keys"], z["meta_vals"])}
+
+
+TAGS = {"kat-small-fd": ("kat-small.job", 0), "kat-small-nsfd": ("kat-small-nsfd.job", 1)}

@@ -1,0 +1,124 @@
+"""Generates the golden vectors under tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_harness (the unmodified reference sources built by oracle/Makefile.ref
+against the single-rank MPI stand-in) on the small known-answer jobs and stores inputs and
+outputs as compressed .npz files.  Run from the repository root in a checkout that has the
+reference tree:
+
+    python tests/golden/make_golden.py [REF_SRC]
+
+Seeded random inputs (numpy default_rng) make every fixture reproducible.
+"""
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, REPO)
+from oracle import pyoracle  # noqa: E402
+
+OUT = os.path.join(REPO, "tests", "golden")
+JOBS = os.path.join(REPO, "mithra_gb300", "jobs")
+
+
+def meta_arrays(path):
+    m = pyoracle.read_meta(path)
+    keys = sorted(m)
+    return np.array(keys), np.array([m[k] for k in keys])
+
+
+def run(harness, *args, cwd):
+    subprocess.run([harness] + [str(a) for a in args], check=True, cwd=cwd,
+                   stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+
+
+def fixtures_for(harness, jobname, tag, with_kats=True):
+    job = os.path.join(JOBS, jobname)
+    dst = os.path.join(OUT, tag)
+    os.makedirs(dst, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        # Initial state and a 12-step march, dumped at steps 6 and 12.
+        run(harness, "run", job, 12, os.path.join(tmp, "run"), 6, cwd=tmp)
+        r = os.path.join(tmp, "run")
+        ld = lambda s, n: np.fromfile(os.path.join(r, "step%d" % s, n + ".bin"))
+        keys, vals = meta_arrays(os.path.join(r, "step0", "meta.txt"))
+        np.savez_compressed(os.path.join(dst, "init.npz"), meta_keys=keys, meta_vals=vals,
+                            particles=ld(0, "particles").reshape(-1, 11), an=ld(0, "an"), anm1=ld(0, "anm1"),
+                            anp1=ld(0, "anp1"))
+        np.savez_compressed(os.path.join(dst, "run.npz"),
+                            an6=ld(6, "an"), anp1_6=ld(6, "anp1"), particles6=ld(6, "particles").reshape(-1, 11),
+                            an12=ld(12, "an"), anm1_12=ld(12, "anm1"), anp1_12=ld(12, "anp1"),
+                            particles12=ld(12, "particles").reshape(-1, 11),
+                            power=np.fromfile(os.path.join(r, "power.bin")).reshape(12, -1))
+        if not with_kats:
+            return
+        meta = pyoracle.read_meta(os.path.join(r, "step0", "meta.txt"))
+        nodes = int(meta["N0"]) * int(meta["N1"]) * int(meta["np"])
+        rng = np.random.default_rng(20261203)
+
+        # Field update with random potentials and current.
+        fin = os.path.join(tmp, "field_in")
+        os.makedirs(fin)
+        an, anm1, anp1 = (rng.standard_normal(nodes * 3) for _ in range(3))
+        an.tofile(os.path.join(fin, "an.bin"))
+        anm1.tofile(os.path.join(fin, "anm1.bin"))
+        anp1.tofile(os.path.join(fin, "anp1.bin"))
+        run(harness, "field", job, fin, os.path.join(tmp, "field_out"), cwd=tmp)
+        fo = os.path.join(tmp, "field_out")
+        np.savez_compressed(os.path.join(dst, "field.npz"), an=an, anm1=anm1, anp1=anp1,
+                            out_anp1=np.fromfile(os.path.join(fo, "anp1.bin")),
+                            en=np.fromfile(os.path.join(fo, "en.bin"), dtype=np.float32),
+                            bn=np.fromfile(os.path.join(fo, "bn.bin"), dtype=np.float32))
+
+        # One push of the initial bunch with all particles past the entrance, inside the
+        # undulator (lz about 10.3 periods), in random radiation fields.
+        parts = ld(0, "particles").reshape(-1, 11).copy()
+        parts[:, 10] = 1.0
+        lu = meta["und0_lu"]
+        tb = -meta["dt_shift"] + 10.3 * lu / (meta["gamma"] * meta["beta"] * meta["c0"])
+        pin = os.path.join(tmp, "push_in")
+        os.makedirs(pin)
+        a_n = 1e-3 * rng.standard_normal(nodes * 3)
+        a_np1 = a_n + 1e-5 * rng.standard_normal(nodes * 3)
+        a_n.tofile(os.path.join(pin, "an.bin"))
+        a_np1.tofile(os.path.join(pin, "anp1.bin"))
+        parts.tofile(os.path.join(pin, "particles.bin"))
+        np.array([tb]).tofile(os.path.join(pin, "timebunch.bin"))
+        run(harness, "push", job, pin, os.path.join(tmp, "push_out"), cwd=tmp)
+        np.savez_compressed(os.path.join(dst, "push.npz"), an=a_n, anp1=a_np1, particles=parts,
+                            time_bunch=np.array([tb]),
+                            out=np.fromfile(os.path.join(tmp, "push_out", "particles.bin")).reshape(-1, 11))
+
+        # Deposit of particles that moved by a random sub-cell step.
+        dep = ld(0, "particles").reshape(-1, 11).copy()
+        dep[:, 4:7] = dep[:, 1:4]
+        step = np.array([meta["dx"], meta["dy"], meta["dz"]]) * 0.7
+        dep[:, 1:4] += step * rng.uniform(-1, 1, size=(dep.shape[0], 3))
+        din = os.path.join(tmp, "dep_in")
+        os.makedirs(din)
+        dep.tofile(os.path.join(din, "particles.bin"))
+        run(harness, "deposit", job, din, os.path.join(tmp, "dep_out"), cwd=tmp)
+        np.savez_compressed(os.path.join(dst, "deposit.npz"), particles=dep,
+                            J=np.fromfile(os.path.join(tmp, "dep_out", "anp1.bin")))
+    finally:
+        shutil.rmtree(tmp)
+
+
+def main():
+    ref_src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    harness = pyoracle.build_reference(ref_src)
+    if harness is None:
+        sys.exit("reference sources not found at %s" % ref_src)
+    harness = os.path.abspath(harness)
+    fixtures_for(harness, "kat-small.job", "kat-small-fd")
+    fixtures_for(harness, "kat-small-nsfd.job", "kat-small-nsfd")
+    print("golden vectors written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

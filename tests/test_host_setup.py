@@ -1,0 +1,49 @@
+"""Host parser + FP64 initialisation against the reference's initial state (golden vectors)."""
+import numpy as np
+import pytest
+
+import mithra_gb300 as mg
+from tests._golden import TAGS, load, meta
+from tests.conftest import job
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_setup_matches_reference(tag):
+    ref = meta(tag)
+    s = mg.Setup.from_job(job(TAGS[tag][0]))
+    m = s.meta()
+    for k, v in ref.items():
+        assert k in m, k
+        assert m[k] == v, (k, m[k], v)
+    assert np.array_equal(s.particles(), load(tag, "init")["particles"])
+
+
+def test_config1_setup_particle_count():
+    s = mg.Setup.from_job(job("fel-ir-48x48x384.job"))
+    g = s.grid()
+    assert (g.N0, g.N1, g.N2) == (50, 50, 386)
+    assert s.particles().shape == (237572, 11)   # 2e5 requested, beamlets of 4 + taper
+    assert s.meta()["nUpdateBunch"] > 4.9
+
+
+def test_parse_errors_are_reported(tmp_path):
+    bad = tmp_path / "bad.job"
+    bad.write_text("MESH\n{\n  no-such-key = 1\n}\n")
+    with pytest.raises(mg.MithraError, match="not defined in solver group"):
+        mg.Setup.from_job(str(bad))
+    bad.write_text("WRONGGROUP\n{\n}\n")
+    with pytest.raises(mg.MithraError, match="is not a defined group"):
+        mg.Setup.from_job(str(bad))
+    with pytest.raises(mg.MithraError, match="Unable to open file"):
+        mg.Setup.from_job(str(tmp_path / "missing.job"))
+
+
+def test_comment_and_whitespace_rules(tmp_path):
+    text = open(job("kat-small.job")).read()
+    mangled = "\n".join(("\t" + l.replace(" ", "  ") + "   # trailing comment") if l.strip() and not l.startswith("#")
+                        else l for l in text.splitlines())
+    p = tmp_path / "m.job"
+    p.write_text(mangled)
+    a = mg.Setup.from_job(job("kat-small.job")).particles()
+    b = mg.Setup.from_job(str(p)).particles()
+    assert np.array_equal(a, b)

@@ -1,0 +1,82 @@
+"""The C oracle against the reference's own outputs (golden vectors from oracle/_ref).
+
+Bit-exact: the oracle restates the reference's arithmetic in the same order and is built with
+-ffp-contract=off, so every comparison here is array_equal."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from tests._golden import TAGS, load, meta
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_oracle_march_matches_reference(tag):
+    m = meta(tag)
+    init, run = load(tag, "init"), load(tag, "run")
+    solver = TAGS[tag][1]
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=solver, order=2)
+    for step in range(1, 13):
+        r.step()
+        zl, pg = r.power_rows[-1]
+        row = np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)]))
+        assert np.array_equal(row, run["power"][step - 1]), "power row %d" % step
+        if step == 6:
+            assert np.array_equal(r.an, run["an6"])
+            assert np.array_equal(r.anp1, run["anp1_6"])
+            assert np.array_equal(r.particles, run["particles6"])
+    assert np.array_equal(r.an, run["an12"])
+    assert np.array_equal(r.anm1, run["anm1_12"])
+    assert np.array_equal(r.anp1, run["anp1_12"])
+    assert np.array_equal(r.particles, run["particles12"])
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_oracle_field_update_matches_reference(tag):
+    m = meta(tag)
+    f = load(tag, "field")
+    fp = po.field_params(m, TAGS[tag][1], 2)
+    anp1 = f["anp1"].copy()
+    po.lib().mo_field_update(po.C.byref(fp), po.dptr(anp1), po.dptr(f["an"].copy()), po.dptr(f["anm1"].copy()))
+    assert np.array_equal(anp1, f["out_anp1"])
+    nodes = anp1.size // 3
+    en = np.zeros(nodes * 3, dtype=np.float32)
+    bn = np.zeros(nodes * 3, dtype=np.float32)
+    po.lib().mo_eval_eb(po.C.byref(fp), po.dptr(anp1), po.dptr(f["an"].copy()), None, po.fptr(en), po.fptr(bn))
+    N0, N1, N2 = int(m["N0"]), int(m["N1"]), int(m["np"])
+    sel = np.zeros((N2, N0, N1), dtype=bool)
+    sel[:, 1:-1, 1:-1] = True
+    sel = np.repeat(sel.ravel(), 3)
+    assert np.array_equal(en[sel], f["en"][sel])
+    assert np.array_equal(bn[sel], f["bn"][sel])
+
+
+def test_oracle_push_matches_reference():
+    tag = "kat-small-fd"
+    m = meta(tag)
+    p = load(tag, "push")
+    fp = po.field_params(m, 0, 2)
+    nodes = p["an"].size // 3
+    en = np.zeros(nodes * 3, dtype=np.float32)
+    bn = np.zeros(nodes * 3, dtype=np.float32)
+    po.lib().mo_eval_eb(po.C.byref(fp), po.dptr(p["anp1"].copy()), po.dptr(p["an"].copy()), None, po.fptr(en), po.fptr(bn))
+    rec = np.zeros((p["out"].shape[0] + 16, 11))
+    n = p["particles"].shape[0]
+    rec[:n] = p["particles"]
+    pp = po.push_params(m)
+    nt = po.C.c_long(0)
+    n2 = po.lib().mo_push_substep(po.C.byref(pp), float(p["time_bunch"][0]), po.dptr(rec), n, rec.shape[0],
+                                  po.fptr(en), po.fptr(bn), po.C.byref(nt))
+    assert n2 == p["out"].shape[0]
+    assert np.array_equal(rec[:n2], p["out"])
+
+
+def test_oracle_deposit_matches_reference():
+    tag = "kat-small-fd"
+    m = meta(tag)
+    d = load(tag, "deposit")
+    dp = po.deposit_params(m)
+    J = np.zeros_like(d["J"])
+    po.lib().mo_deposit_current(po.C.byref(dp), po.dptr(np.ascontiguousarray(d["particles"])), d["particles"].shape[0],
+                                po.dptr(J), None)
+    assert np.array_equal(J, d["J"])
+    assert np.count_nonzero(J) > 0
