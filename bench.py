@@ -1,0 +1,374 @@
+#!/usr/bin/env python3
+"""Throughput of the MITHRA FdTd time-marching loop on GB300.
+
+Metric: cell+particle updates per second, i.e. (mesh nodes + particle pushes) per field step
+divided by the step time, where particle pushes = particles x bunch substeps.  The default
+workload is the 128 x 128 x 2048-cell job (130 x 130 x 2050 nodes, ~8.1e6 macro-particles,
+two bunch substeps per field step) in the plain FP64 form; --precision fp32 selects the mixed
+form.  Inputs are seeded synthetic bunches (Halton sequence) built by the reference's own
+initialisation restated on the host; the field state (3.4 GB) exceeds the 129 MB L2, so no L2
+flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path is a
+single domain per GPU); the value is the sum over ranks and the time the maximum over ranks.
+`--impl reference` times the reference algorithm on the host cores instead: the C restatement
+in oracle/ (the reference tree itself is not present on the GPU host), with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    "fel-130x130x2050": "fel-130x130x2050.job",
+    "fel-ir-48x48x384": "fel-ir-48x48x384.job",
+    "fel-98x98x1026": "fel-98x98x1026.job",  # profiling case (about 1 GB on the device)
+}
+METRIC = "cell+particle updates/s"
+
+# Algorithmic bytes per unit (each array element counted once, halo re-reads free).
+# Units: interior node for the field kernels, particle for the particle kernels.
+ALGO_BYTES = {
+    "fp64": {"potential_interior_fd": 96, "potential_interior_nsfd": 96, "eval_eb": 72, "push": 96 + 1,
+             "deposit": 48 + 8, "erase": 8 + 1},
+    "fp32": {"potential_interior_fd": 48, "potential_interior_nsfd": 48, "eval_eb": 48, "push": 56 + 1,
+             "deposit": 24 + 4 + 20, "erase": 12 + 1},
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+class Dist:
+    def __init__(self, want_gpus: int):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+            self.torch = torch
+            self.backend = backend
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi samples of the SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_table():
+    try:
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def cpu_threads() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_run_for(jobpath):
+    """The CPU restatement (oracle/) started from the same host initialisation."""
+    import mithra_gb300 as mg
+    from oracle import pyoracle as po
+    s = mg.Setup.from_job(jobpath)
+    m = s.meta()
+    g = s.grid()
+    anp1, an, anm1 = s.fields()
+    return po, po.OracleRun(m, an, anm1, anp1, s.particles(), solver=g.solver, order=g.truncation_order), m
+
+
+def units_per_step(meta, n_particles):
+    nsub = 0
+    t = 0.0
+    while t < meta["nUpdateBunch"]:
+        nsub += 1
+        t += 1.0
+    nodes = int(meta["N0"]) * int(meta["N1"]) * int(meta["N2"])
+    return nodes, n_particles * nsub, nsub
+
+
+def cpu_baseline(jobpath, sample_seconds):
+    po, run, m = oracle_run_for(jobpath)
+    threads = cpu_threads()
+    po.set_threads(threads)
+    nodes, pushes, _ = units_per_step(m, run.n)
+    run.step()  # first-touch of the arrays
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        run.step()
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= sample_seconds or steps >= 200:
+            break
+    po.set_threads(1)
+    return {"value": (nodes + pushes) * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "%d field steps of the same job (after one untimed step), C restatement of the "
+                      "reference with OpenMP over %d host threads, %.1f s" % (steps, threads, el)}
+
+
+def run_reference(args, dist):
+    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
+    if dist.rank != 0:
+        return
+    po, run, m = oracle_run_for(jobpath)
+    threads = cpu_threads()
+    po.set_threads(threads)
+    nodes, pushes, nsub = units_per_step(m, run.n)
+    for _ in range(args.warmup):
+        run.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        run.step()
+    el = time.perf_counter() - t0
+    value = (nodes + pushes) * args.steps / el
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Halton bunch of the job file)",
+        "config": {"workload": args.workload, "nodes": nodes, "particles": run.n, "substeps": nsub,
+                   "precision": "fp64", "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": "%d timed field steps after %d warm-up steps, C restatement of the reference "
+                                   "(oracle/) with OpenMP over %d host threads" % (args.steps, args.warmup, threads)},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args, dist):
+    import numpy as np
+
+    import mithra_gb300 as mg
+    prec = mg.FP64 if args.precision == "fp64" else mg.FP32
+    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
+    setup = mg.Setup.from_job(jobpath)
+    meta = setup.meta()
+    ctx = mg.Context.from_setup(setup, prec, device=dist.local)
+    n_part = ctx.particle_count()
+    nodes, pushes, nsub = units_per_step(meta, n_part)
+    units = nodes + pushes
+    ctx.run_prelude()
+    ctx.run(args.warmup)
+    ctx.synchronize()
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ms = ctx.run_timed(args.steps)
+    dist.barrier()
+    ms_max = dist.max(ms)
+    value = dist.world * units * args.steps / (ms_max / 1e3)
+
+    # Per-kernel device times: the same K steps again, each kernel bracketed by CUDA events on
+    # the context stream (direct launches instead of the step graph).
+    ctx.enable_timing(True)
+    ctx.run(args.steps)
+    kt = ctx.kernel_times()
+    ctx.enable_timing(False)
+    total_k = sum(v[0] for v in kt.values())
+    dominant = max(kt.items(), key=lambda kv: kv[1][0])[0]
+    dom_ms, dom_launches = kt[dominant]
+    g = setup.grid()
+    interior = (g.N0 - 2) * (g.N1 - 2) * (g.N2 - 2)
+    unit_count = n_part if dominant in ("push", "deposit", "erase") else interior
+    per_unit = ALGO_BYTES[args.precision].get(dominant)
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if per_unit:
+        avg_s = dom_ms / dom_launches / 1e3
+        achieved = per_unit * unit_count / avg_s / 1e9
+        tr = traffic_table().get(args.precision, {}).get(dominant)
+        roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": per_unit * unit_count,
+                "traffic": (tr * unit_count if tr else None),
+                "avg_launch_ms": dom_ms / dom_launches, "share": dom_ms / total_k}
+    kernels = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k} for k, v in kt.items()}
+
+    # End to end through the public API with host buffers: upload the initial state from pinned
+    # host memory, march K steps, read the power rows back.
+    e2e = None
+    if not args.no_e2e:
+        anp1, an, anm1 = setup.fields()
+        parts = setup.particles()
+        bufs = [mg.PinnedArray(anp1.shape), mg.PinnedArray(an.shape), mg.PinnedArray(anm1.shape),
+                mg.PinnedArray(parts.shape)]
+        for b, src in zip(bufs, (anp1, an, anm1, parts)):
+            b.array[...] = src
+        t0_state = setup.time()
+        h2d = sum(b.array.nbytes for b in bufs)
+        dist.barrier()
+        t0 = time.perf_counter()
+        ctx.upload_fields(bufs[0].array, bufs[1].array, bufs[2].array)
+        ctx.upload_particles(bufs[3].array)
+        ctx.set_time(t0_state)
+        ctx.run(args.steps)
+        rows = ctx.power_rows()
+        el = time.perf_counter() - t0
+        el = dist.max(el)
+        e2e = {"value": dist.world * units * args.steps / el, "unit": METRIC,
+               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": rows.nbytes / args.steps,
+               "ms_per_step": 1e3 * el / args.steps}
+        for b in bufs:
+            b.free()
+    launches = ctx.launches_per_step() * args.steps
+    ctx.close()
+
+    if dist.rank != 0:
+        return
+    cpu = None
+    if dist.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(jobpath, args.cpu_sample_seconds)
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+        "data": "synthetic (seeded Halton bunch of the job file)",
+        "config": {"workload": args.workload, "nodes": nodes, "particles": n_part, "substeps": nsub,
+                   "precision": args.precision, "parallelism": "replicas" if dist.world > 1 else "single-gpu",
+                   "l2": "inputs larger than L2 (%.1f GB of field state)" % (nodes * 3 * 3 * 8 / 1e9)},
+        "cell_updates_per_s": dist.world * nodes * args.steps / (ms_max / 1e3),
+        "particle_pushes_per_s": dist.world * pushes * args.steps / (ms_max / 1e3),
+        "roofline": roof,
+        "kernels": kernels,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    dist = Dist(args.gpus)
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_gpu(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

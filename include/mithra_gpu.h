@@ -157,6 +157,11 @@ int mithra_gpu_advance_time(mithra_ctx* ctx);
 /* `nsteps` iterations of the body of Solver::solve's main loop (src/solver.cpp:1300-1414),
  * replayed from CUDA graphs with no host synchronisation between steps. */
 int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps);
+/* mithra_gpu_run bracketed by CUDA events recorded on the context's stream; returns the device
+ * time of the `nsteps` steps in milliseconds (the stream is synchronised). */
+int mithra_gpu_run_timed(mithra_ctx* ctx, int64_t nsteps, double* device_ms);
+/* Number of kernels the library launches for one field step of this context. */
+int mithra_gpu_launches_per_step(mithra_ctx* ctx, int* n);
 /* The negative-time particle loop of Solver::solve (src/solver.cpp:1232-1291): field-free
  * substeps while time_ < 0. */
 int mithra_gpu_run_prelude(mithra_ctx* ctx);
@@ -170,6 +175,10 @@ int mithra_gpu_power_rows(mithra_ctx* ctx, double* out, size_t cap_values, size_
  * names/ms are filled for up to `cap` kernels; returns the count through *n. */
 int mithra_gpu_kernel_times(mithra_ctx* ctx, char* names, size_t name_len, double* ms, int cap, int* n);
 int mithra_gpu_enable_timing(mithra_ctx* ctx, int on);
+
+/* Page-locked host buffers for transfers that overlap with device work (cudaMallocHost). */
+int mithra_host_alloc(size_t bytes, void** p);
+int mithra_host_free(void* p);
 
 /* ---- job-file level entry points (host initialisation of the reference, then a context) --- */
 

@@ -20,7 +20,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Setup", "Context", "FdTd", "FdTdSC", "MithraError", "lib", "FP64", "FP32"]
+__all__ = ["Setup", "Context", "FdTd", "FdTdSC", "MithraError", "PinnedArray", "lib", "FP64", "FP32"]
 
 FP64 = 0
 FP32 = 1
@@ -98,6 +98,10 @@ _SIGS = {
     "mithra_gpu_advance_time": [_vp],
     "mithra_gpu_run": [_vp, C.c_int64],
     "mithra_gpu_run_prelude": [_vp],
+    "mithra_gpu_run_timed": [_vp, C.c_int64, _dp],
+    "mithra_gpu_launches_per_step": [_vp, _P(C.c_int)],
+    "mithra_host_alloc": [C.c_size_t, _P(_vp)],
+    "mithra_host_free": [_vp],
     "mithra_gpu_power_rows": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
     "mithra_gpu_kernel_times": [_vp, C.c_char_p, C.c_size_t, _dp, C.c_int, _P(C.c_int)],
     "mithra_gpu_enable_timing": [_vp, C.c_int],
@@ -144,6 +148,29 @@ def fptr(a):
         return None
     assert a.dtype == np.float32 and a.flags.c_contiguous, "float32 C-contiguous array expected"
     return a.ctypes.data_as(_fp)
+
+
+class PinnedArray:
+    """A page-locked host buffer (cudaMallocHost) exposed as a numpy array."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.dtype = np.dtype(dtype)
+        n = int(np.prod(shape))
+        self._p = _vp()
+        r = lib().mithra_host_alloc(max(n, 1) * self.dtype.itemsize, C.byref(self._p))
+        if r != 0:
+            raise MithraError("mithra_host_alloc failed with status %d" % r)
+        buf = (C.c_char * (max(n, 1) * self.dtype.itemsize)).from_address(self._p.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=n).reshape(shape)
+
+    def free(self):
+        if getattr(self, "_p", None) and self._p.value and _lib is not None:
+            self.array = None
+            _lib.mithra_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        self.free()
 
 
 class Setup:
@@ -387,6 +414,17 @@ class Context:
 
     def run(self, nsteps: int):
         self.call("mithra_gpu_run", int(nsteps))
+
+    def run_timed(self, nsteps: int) -> float:
+        """Runs `nsteps` steps; returns their device time in ms (CUDA events on the context stream)."""
+        ms = C.c_double()
+        self.call("mithra_gpu_run_timed", int(nsteps), C.byref(ms))
+        return ms.value
+
+    def launches_per_step(self) -> int:
+        n = C.c_int()
+        self.call("mithra_gpu_launches_per_step", C.byref(n))
+        return n.value
 
     def run_prelude(self):
         self.call("mithra_gpu_run_prelude")

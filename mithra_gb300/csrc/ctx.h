@@ -55,6 +55,7 @@ struct mithra_ctx {
   mithra::StateDev* st_host = nullptr;  // pinned mirror
   std::vector<mithra::PowerOut> power;
   long long row_cap = 0;
+  long long rows_pending = 0;  // power rows appended since the last drain (host-side count)
   cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
   bool timing = false;
   std::vector<mithra::KernelTimer> timers;
@@ -63,7 +64,10 @@ struct mithra_ctx {
   bool particles_loaded = false;
   std::string err;
   int sm_count = 152;
-  long long st_host_rows();
+  int launches_per_step = 0;
+  int launch_counter = 0;
+  void* staging = nullptr;  // device staging buffer for host-layout transfers
+  size_t staging_bytes = 0;
 };
 
 namespace mithra {
@@ -88,6 +92,9 @@ cudaError_t dalloc(T** p, size_t n) {
 
 inline long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
 
+// Returns a device staging buffer of at least `bytes` (kept for later transfers).
+int staging(mithra_ctx* ctx, size_t bytes, void** p);
+
 // Launches one kernel through `fn` on ctx->stream; in timing mode it is bracketed by CUDA
 // events recorded on the same stream and accumulated under `name`.
 template <typename Fn>
@@ -99,6 +106,7 @@ int timed(mithra_ctx* ctx, const char* name, Fn fn) {
     if (r) return r;
   }
   fn();
+  ctx->launch_counter++;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "launch %s: %s", name, cudaGetErrorString(e));
   if (ctx->timing) return timer_end(ctx, slot, a, b);

@@ -80,6 +80,20 @@ int harvest_timers(mithra_ctx* ctx) {
   return MITHRA_OK;
 }
 
+int staging(mithra_ctx* ctx, size_t bytes, void** p) {
+  if (bytes > ctx->staging_bytes) {
+    if (ctx->staging) {
+      CK(cudaStreamSynchronize(ctx->stream));
+      CK(cudaFree(ctx->staging));
+      ctx->staging = nullptr;
+    }
+    CK(cudaMalloc(&ctx->staging, bytes));
+    ctx->staging_bytes = bytes;
+  }
+  *p = ctx->staging;
+  return MITHRA_OK;
+}
+
 void invalidate_graphs(mithra_ctx* ctx) {
   for (auto& gr : ctx->graph)
     if (gr) { cudaGraphExecDestroy(gr); gr = nullptr; }
@@ -235,11 +249,13 @@ int enqueue_step(mithra_ctx* ctx) {
   return stage_advance_time(ctx);
 }
 
+// Makes room for `extra` more rows in the device row log; the count of rows already logged is
+// tracked on the host, so no device round trip is needed when there is room.
 int ensure_rows(mithra_ctx* ctx, long long extra) {
   if (ctx->power.empty()) return MITHRA_OK;
-  CK(cudaStreamSynchronize(ctx->stream));
-  const long long need = ctx->st_host_rows() + extra;
+  const long long need = ctx->rows_pending + extra;
   if (need <= ctx->row_cap) return MITHRA_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
   long long cap = std::max(need, 2 * ctx->row_cap + 64);
   for (auto& po : ctx->power) {
     const long long rowlen = (long long)po.dev.N * (1 + po.dev.Nl);
@@ -269,11 +285,6 @@ int check_state(mithra_ctx* ctx) {
 
 }  // namespace
 
-long long mithra_ctx::st_host_rows() {
-  if (cudaMemcpyAsync(st_host, st, sizeof(StateDev), cudaMemcpyDeviceToHost, stream) != cudaSuccess) return 0;
-  cudaStreamSynchronize(stream);
-  return st_host->n_power_rows;
-}
 
 // ---- C ABI ----------------------------------------------------------------------------------
 
@@ -376,6 +387,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   void* ps[] = {pt.x, pt.y, pt.z, pt.gx, pt.gy, pt.gz, pt.mx, pt.my, pt.mz, pt.q, pt.e, pt.status, pt.cross};
   for (void* p : ps) cudaFree(p);
   fp32_free(ctx);
+  cudaFree(ctx->staging);
   cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
@@ -481,6 +493,7 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->st_host->n_power_rows = 0;
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+  ctx->rows_pending = 0;
   invalidate_graphs(ctx);
   return ensure_rows(ctx, 256);
 }
@@ -490,7 +503,7 @@ int mithra_gpu_upload_fields(mithra_ctx* ctx, const double* anp1, const double* 
   const GridDev& g = ctx->g;
   const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
   double* staging = nullptr;
-  CK(dalloc(&staging, n));
+  { int r = mithra::staging(ctx, n * sizeof(double), (void**)&staging); if (r) return r; }
   const double* src[3] = {anp1, an, anm1};
   for (int l = 0; l < 3; l++) {
     if (!src[l]) continue;
@@ -502,7 +515,6 @@ int mithra_gpu_upload_fields(mithra_ctx* ctx, const double* anp1, const double* 
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaFree(staging));
   return MITHRA_OK;
 }
 
@@ -511,7 +523,7 @@ int mithra_gpu_download_fields(mithra_ctx* ctx, double* anp1, double* an, double
   const GridDev& g = ctx->g;
   const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
   double* staging = nullptr;
-  CK(dalloc(&staging, n));
+  { int r = mithra::staging(ctx, n * sizeof(double), (void**)&staging); if (r) return r; }
   double* dst[3] = {anp1, an, anm1};
   for (int l = 0; l < 3; l++) {
     if (!dst[l]) continue;
@@ -523,7 +535,6 @@ int mithra_gpu_download_fields(mithra_ctx* ctx, double* anp1, double* an, double
     CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
-  CK(cudaFree(staging));
   return MITHRA_OK;
 }
 
@@ -533,7 +544,7 @@ int mithra_gpu_upload_scalar(mithra_ctx* ctx, const double* fnp1, const double* 
   const GridDev& g = ctx->g;
   const size_t n = (size_t)g.N0 * g.N1 * g.N2;
   double* staging = nullptr;
-  CK(dalloc(&staging, n));
+  { int r = mithra::staging(ctx, n * sizeof(double), (void**)&staging); if (r) return r; }
   const double* src[3] = {fnp1, fn, fnm1};
   for (int l = 0; l < 3; l++) {
     if (!src[l]) continue;
@@ -545,7 +556,6 @@ int mithra_gpu_upload_scalar(mithra_ctx* ctx, const double* fnp1, const double* 
     CK(cudaGetLastError());
   }
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaFree(staging));
   return MITHRA_OK;
 }
 
@@ -555,7 +565,7 @@ int mithra_gpu_download_scalar(mithra_ctx* ctx, double* fnp1, double* fn, double
   const GridDev& g = ctx->g;
   const size_t n = (size_t)g.N0 * g.N1 * g.N2;
   double* staging = nullptr;
-  CK(dalloc(&staging, n));
+  { int r = mithra::staging(ctx, n * sizeof(double), (void**)&staging); if (r) return r; }
   double* dst[3] = {fnp1, fn, fnm1};
   for (int l = 0; l < 3; l++) {
     if (!dst[l]) continue;
@@ -567,7 +577,6 @@ int mithra_gpu_download_scalar(mithra_ctx* ctx, double* fnp1, double* fn, double
     CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
-  CK(cudaFree(staging));
   return MITHRA_OK;
 }
 
@@ -576,7 +585,7 @@ int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
   const GridDev& g = ctx->g;
   const size_t n = (size_t)g.N0 * g.N1 * g.N2 * 3;
   float* staging = nullptr;
-  CK(dalloc(&staging, n));
+  { int r = mithra::staging(ctx, n * sizeof(float), (void**)&staging); if (r) return r; }
   float* dst[2] = {en, bn};
   const float* srcs[2] = {ctx->E, ctx->B};
   for (int l = 0; l < 2; l++) {
@@ -586,7 +595,6 @@ int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
     CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
   }
-  CK(cudaFree(staging));
   return MITHRA_OK;
 }
 
@@ -594,7 +602,7 @@ int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
   if (!ctx || (n && !rec)) return MITHRA_ERR_ARG;
   if (n > ctx->capacity) return fail(ctx, MITHRA_ERR_CAPACITY, "%zu particles exceed capacity %zu", n, ctx->capacity);
   double* staging = nullptr;
-  CK(dalloc(&staging, n * 11));
+  { int r = mithra::staging(ctx, std::max<size_t>(n, 1) * 11 * sizeof(double), (void**)&staging); if (r) return r; }
   if (n) CK(cudaMemcpyAsync(staging, rec, n * 11 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->precision == MITHRA_PRECISION_FP64) {
     k_records_to_soa<<<grid_stride_blocks(ctx, (long long)n, 256), 256, 0, ctx->stream>>>(staging, (long long)n, ctx->pt);
@@ -610,7 +618,6 @@ int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
   ctx->st_host->overflow = 0;
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaFree(staging));
   ctx->particles_loaded = true;
   return MITHRA_OK;
 }
@@ -630,8 +637,8 @@ int mithra_gpu_download_particles(mithra_ctx* ctx, double* rec, size_t cap, size
   if (r) return r;
   double* staging = nullptr;
   long long* dn = nullptr;
-  CK(dalloc(&staging, std::max<size_t>(slots, 1) * 11));
-  CK(dalloc(&dn, 1));
+  if ((r = mithra::staging(ctx, (std::max<size_t>(slots, 1) * 11 + 1) * sizeof(double), (void**)&staging))) return r;
+  dn = (long long*)(staging + std::max<size_t>(slots, 1) * 11);
   if (ctx->precision == MITHRA_PRECISION_FP64) {
     k_soa_to_records<<<1, 1024, 0, ctx->stream>>>(ctx->pt, ctx->st, staging, (long long)slots, dn);
     CK(cudaGetLastError());
@@ -645,8 +652,6 @@ int mithra_gpu_download_particles(mithra_ctx* ctx, double* rec, size_t cap, size
   const size_t take = std::min<size_t>((size_t)live, cap);
   if (take) CK(cudaMemcpyAsync(rec, staging, take * 11 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
-  CK(cudaFree(staging));
-  CK(cudaFree(dn));
   *n = (size_t)live;
   if ((size_t)live > cap) return fail(ctx, MITHRA_ERR_CAPACITY, "buffer holds %zu of %lld particles", cap, live);
   return MITHRA_OK;
@@ -713,6 +718,7 @@ int mithra_gpu_power_sample(mithra_ctx* ctx) {
   if (!ctx) return MITHRA_ERR_ARG;
   int r = ensure_rows(ctx, 1);
   if (r) return r;
+  if (!ctx->power.empty()) ctx->rows_pending += 1;
   return stage_power(ctx);
 }
 
@@ -739,11 +745,11 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
   if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
   int r = ensure_rows(ctx, nsteps);
   if (r) return r;
+  if (!ctx->power.empty()) ctx->rows_pending += nsteps;
   if (ctx->timing) {
-    for (int64_t s = 0; s < nsteps; s++) {
+    for (int64_t s = 0; s < nsteps; s++)
       if ((r = enqueue_step(ctx))) return r;
-      if ((r = harvest_timers(ctx))) return r;
-    }
+    if ((r = harvest_timers(ctx))) return r;
     return check_state(ctx);
   }
   for (int64_t s = 0; s < nsteps; s++) {
@@ -752,7 +758,9 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
       cudaGraph_t graph;
       const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      ctx->launch_counter = 0;
       r = enqueue_step(ctx);
+      ctx->launches_per_step = ctx->launch_counter;
       cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
       if (r) return r;
       if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
@@ -765,6 +773,57 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
     rotate(ctx);
   }
   return check_state(ctx);
+}
+
+int mithra_gpu_run_timed(mithra_ctx* ctx, int64_t nsteps, double* device_ms) {
+  if (!ctx || !device_ms) return MITHRA_ERR_ARG;
+  int r = ensure_rows(ctx, nsteps);
+  if (r) return r;
+  if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->stream));
+  r = mithra_gpu_run(ctx, nsteps);
+  if (r) { cudaEventDestroy(a); cudaEventDestroy(b); return r; }
+  CK(cudaEventRecord(b, ctx->stream));
+  CK(cudaEventSynchronize(b));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *device_ms = ms;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_launches_per_step(mithra_ctx* ctx, int* n) {
+  if (!ctx || !n) return MITHRA_ERR_ARG;
+  if (!ctx->launches_per_step) {
+    // Count by recording one step into a throw-away capture.
+    cudaGraph_t graph;
+    const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->launch_counter = 0;
+    int r = enqueue_step(ctx);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
+    if (r) return r;
+    if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "capture: %s", cudaGetErrorString(ce));
+    cudaGraphDestroy(graph);
+    ctx->launches_per_step = ctx->launch_counter;
+  }
+  *n = ctx->launches_per_step;
+  return MITHRA_OK;
+}
+
+int mithra_host_alloc(size_t bytes, void** p) {
+  if (!p) return MITHRA_ERR_ARG;
+  return cudaMallocHost(p, std::max<size_t>(bytes, 1)) == cudaSuccess ? MITHRA_OK : MITHRA_ERR_CUDA;
+}
+
+int mithra_host_free(void* p) {
+  if (!p) return MITHRA_ERR_ARG;
+  return cudaFreeHost(p) == cudaSuccess ? MITHRA_OK : MITHRA_ERR_CUDA;
 }
 
 int mithra_gpu_run_prelude(mithra_ctx* ctx) {
@@ -813,6 +872,7 @@ int mithra_gpu_power_rows(mithra_ctx* ctx, double* out, size_t cap_values, size_
   ctx->st_host->n_power_rows = 0;
   CK(cudaMemcpyAsync(&ctx->st->n_power_rows, &ctx->st_host->n_power_rows, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->rows_pending = 0;
   return MITHRA_OK;
 }
 
