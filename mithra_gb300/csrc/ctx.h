@@ -25,10 +25,28 @@ struct KernelTimer {
 };
 
 // Device buffers of the mixed-precision form (allocated only when it is selected).
+struct TileGridHost {
+  int ntx = 0, nty = 0, ntz = 0, n_tiles = 0, bin_outside = 0, bin_erased = 0, n_bins = 0;
+};
+
 struct Fp32State {
   float* A[3] = {nullptr, nullptr, nullptr};
   float* F[3] = {nullptr, nullptr, nullptr};
   ParticlesF32 pt{};
+  ParticlesF32 alt{};  // second buffer set: the tile sort scatters into it, then the two swap
+  int parity = 0;      // which of the two sets is current (flips at every sort)
+  int* counts = nullptr;
+  int* offsets = nullptr;
+  int* key = nullptr;
+  int* rank = nullptr;
+  int* block_sums = nullptr;  // 1024 block totals of the bin scan + grand total
+  TileGridHost tiles;
+  // TMA descriptors of the three A buffers (4D: j, i, k, component): box with halo rows for
+  // A^n, box of the tile rows for A^{n-1} and J.
+  alignas(64) unsigned char map_an[3][128];
+  alignas(64) unsigned char map_c[3][128];
+  bool tma_ready = false;
+  int* tma_error = nullptr;
 };
 
 }  // namespace mithra
@@ -47,8 +65,12 @@ struct mithra_ctx {
   double* F[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of phi
   mithra::ParticlesDev<double> pt{};
   mithra::Fp32State f32{};
-  float* E = nullptr;  // 3 components, cstride apart
+  float* E = nullptr;  // mixed form: E and B, 3 components, cstride apart
   float* B = nullptr;
+  double* E64 = nullptr;  // FP64 form: E and B as doubles holding float-rounded values
+  double* B64 = nullptr;
+  uint8_t* plane_needed = nullptr;  // N2 flags: planes read by a power sample
+  void* und_table = nullptr;        // mixed form: per-plane undulator lz and phase
   int idx[3] = {0, 1, 2};  // buffer index of np1, n, nm1
   size_t capacity = 0;
   mithra::StateDev* st = nullptr;
@@ -56,7 +78,7 @@ struct mithra_ctx {
   std::vector<mithra::PowerOut> power;
   long long row_cap = 0;
   long long rows_pending = 0;  // power rows appended since the last drain (host-side count)
-  cudaGraphExec_t graph[3] = {nullptr, nullptr, nullptr};
+  cudaGraphExec_t graph[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};  // buffer rotation x sort parity
   bool timing = false;
   std::vector<mithra::KernelTimer> timers;
   std::vector<cudaEvent_t> ev_pool;
@@ -121,10 +143,11 @@ float* fp32_scalar(mithra_ctx* ctx, int level);
 int fp32_records_to_soa(mithra_ctx* ctx, const double* staging, long long n);
 int fp32_soa_to_records(mithra_ctx* ctx, double* staging, long long slots, long long* n_out);
 int fp32_field_update(mithra_ctx* ctx);
-int fp32_eval_eb(mithra_ctx* ctx);
+int fp32_eval_eb(mithra_ctx* ctx, bool full = false);
 int fp32_push(mithra_ctx* ctx, int save_rnm);
 int fp32_save_positions(mithra_ctx* ctx);
 int fp32_erase(mithra_ctx* ctx);
 int fp32_current(mithra_ctx* ctx);
+void fp32_after_step(mithra_ctx* ctx);  // swap the particle buffer sets as one step's sort did
 
 }  // namespace mithra

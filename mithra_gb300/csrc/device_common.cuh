@@ -28,6 +28,7 @@ struct GridDev {
   double nsfd_alpha, nsfd_beta;
   double bB[5], cB[5], dB[5], eE[5], fE[5], gE[5], hC[17];
   double dt, dx, dy, dz;
+  double rdx, rdy, rdz;  // reciprocals of dx, dy, dz
   double xmin, xmax, ymin, ymax, zmin, zmax, zp0, zp1, Lz;
 };
 
@@ -43,10 +44,13 @@ struct UndDev {
   double b0, ku, ct, st, ul;  // ul = length * lu
   double r0_prev, r0_next;    // gap to the previous / next module (src/beam.cc:35, :60)
   int has_prev, has_next;
+  // FP32 copies for the mixed form.
+  float ct_f, st_f, ku_f, b0_f, ul_f, r0_prev_f, r0_next_f;
 };
 
 struct PushDev {
   double dtb, r1, r2, gamma, beta, c0, dt_shift, bunch_time_step;
+  double inv_r2;  // 1 / r2
   int n_und;
   double und0_dist;
 };
@@ -64,6 +68,10 @@ struct StateDev {
   int nonfinite;
   long long n_power_rows;
   long long power_row_cap;
+  // z-slab (cells) occupied by particles: E/B are evaluated only where a gather can read them.
+  int k_lo, k_hi;            // range used by this step's E/B evaluation
+  int k_lo_next, k_hi_next;  // accumulated by the deposit for the next step
+  long long next_id;         // mixed form: id given to the next z-face copy
 };
 
 template <typename T>
@@ -90,6 +98,7 @@ struct ParticlesF32 {
   uint8_t* e;
   uint8_t* status;
   int8_t* cross;
+  int* id;  // creation index: initial list position, or the slot of a z-face copy
 };
 
 constexpr long long kCellBias = 1LL << 20;
@@ -121,6 +130,16 @@ struct PowerDev {
   int blocks_per_plane;
   long long row_cap;
 };
+
+// True when node plane k has to be evaluated: inside the particle slab (with two cells of margin
+// for the motion during the step) or read by a power sample.
+__device__ __forceinline__ bool eb_plane_wanted(int k, const StateDev* st, const uint8_t* planes, int N2) {
+  if (!st) return true;
+  const int lo = st->k_lo - 2, hi = st->k_hi + 3;
+  if (k >= lo && k <= hi) return true;
+  if (planes && (planes[k] || (k == 1 && planes[0]) || (k == N2 - 2 && planes[N2 - 1]))) return true;
+  return false;
+}
 
 // pmod, src/stdinclude.cpp:88-93.
 __device__ __forceinline__ double pmod_d(double a, double b) {

@@ -10,13 +10,34 @@
 
 namespace mithra {
 
+// Coefficients in the arithmetic type of the kernel, converted once on the host.
+template <typename T>
+struct Coeffs {
+  T a0, a1, a2, a3, al, be;
+  T bB[5], cB[5], dB[5], eE[5], fE[5], gE[5], hC[17];
+};
+
+template <typename T>
+Coeffs<T> make_coeffs(const GridDev& g) {
+  Coeffs<T> c;
+  c.a0 = (T)g.a[0]; c.a1 = (T)g.a[1]; c.a2 = (T)g.a[2]; c.a3 = (T)g.a[3];
+  c.al = (T)g.nsfd_alpha; c.be = (T)g.nsfd_beta;
+  for (int i = 0; i < 5; i++) {
+    c.bB[i] = (T)g.bB[i]; c.cB[i] = (T)g.cB[i]; c.dB[i] = (T)g.dB[i];
+    c.eE[i] = (T)g.eE[i]; c.fE[i] = (T)g.fE[i]; c.gE[i] = (T)g.gE[i];
+  }
+  for (int i = 0; i < 17; i++) c.hC[i] = (T)g.hC[i];
+  return c;
+}
+
 template <typename T>
 struct PotentialArgs {
   T* np1;        // anp1 (holds J on entry) or fnp1 (holds rho)
   const T* n;    // an / fn
   const T* nm1;  // anm1 / fnm1
   int ncomp;     // 3 for A, 1 for phi
-  double asrc;   // a[4] for J, a[5] for rho
+  T asrc;        // a[4] for J, a[5] for rho
+  Coeffs<T> k;
 };
 
 // Interior update, AdvanceField::advanceMagneticPotentialFD/NSFD and the scalar variants
@@ -31,14 +52,14 @@ __global__ void __launch_bounds__(256) k_potential_interior(GridDev g, Potential
   if (j > g.N1 - 2 || i > g.N0 - 2) return;
   const long long m = node_index(g, k, i, j);
   const long long sI = g.P1, sK = g.plane;
-  const T a0 = (T)g.a[0], a1 = (T)g.a[1], a2 = (T)g.a[2], a3 = (T)g.a[3], as = (T)p.asrc;
+  const T a0 = p.k.a0, a1 = p.k.a1, a2 = p.k.a2, a3 = p.k.a3, as = p.asrc;
   for (int c = 0; c < p.ncomp; c++) {
     const T* an = p.n + c * g.cstride;
     const T* am = p.nm1 + c * g.cstride;
     T* ap = p.np1 + c * g.cstride;
     T v;
     if (NSFD) {
-      const T al = (T)g.nsfd_alpha, be = (T)g.nsfd_beta;
+      const T al = p.k.al, be = p.k.be;
       T sx = an[m + sI] + an[m - sI] + be * (an[m + sI + sK] + an[m + sI - sK] + an[m - sI + sK] + an[m - sI - sK]);
       T sy = an[m + 1] + an[m - 1] + be * (an[m + 1 + sK] + an[m + 1 - sK] + an[m - 1 + sK] + an[m - 1 - sK]);
       v = a0 * an[m] - am[m] + al * (a1 * sx + a2 * sy) + a3 * (an[m + sK] + an[m - sK]) + as * ap[m];
@@ -53,11 +74,11 @@ __global__ void __launch_bounds__(256) k_potential_interior(GridDev g, Potential
 // Mur faces, AdvanceField::advanceBoundaryF/S (src/database.cpp:137-176) with the argument
 // pattern of src/fdtd.cpp:377-472: `in` points into the domain, o1/o2 along the face.
 template <typename T>
-__device__ __forceinline__ T face_value(const double* B, const T* np1, const T* n, const T* nm1,
+__device__ __forceinline__ T face_value(const T* B, const T* np1, const T* n, const T* nm1,
                                         long long m, long long in, long long o1, long long o2) {
-  return (T)B[0] * (nm1[m] + np1[m + in]) + (T)B[1] * nm1[m + in] + (T)B[2] * (n[m] + n[m + in]) +
-         (T)B[3] * (n[m + in + o1] + n[m + in - o1] + n[m + o1] + n[m - o1]) +
-         (T)B[4] * (n[m + in + o2] + n[m + in - o2] + n[m + o2] + n[m - o2]);
+  return B[0] * (nm1[m] + np1[m + in]) + B[1] * nm1[m + in] + B[2] * (n[m] + n[m + in]) +
+         B[3] * (n[m + in + o1] + n[m + in - o1] + n[m + o1] + n[m - o1]) +
+         B[4] * (n[m + in + o2] + n[m + in - o2] + n[m + o2] + n[m - o2]);
 }
 
 template <typename T>
@@ -70,24 +91,24 @@ __global__ void __launch_bounds__(256) k_potential_faces(GridDev g, PotentialArg
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     long long m, in, o1, o2;
-    const double* B;
+    const T* B;
     long long u = t;
     if (u < 2 * nx) {  // x faces: j in [1,N1-2], k in [1,N2-2]
       int side = u >= nx; u -= side * nx;
       int j = 1 + (int)(u % (g.N1 - 2)), k = 1 + (int)(u / (g.N1 - 2));
       m = node_index(g, k, side ? g.N0 - 1 : 0, j);
-      in = side ? -sI : sI; o1 = 1; o2 = sK; B = g.bB;
+      in = side ? -sI : sI; o1 = 1; o2 = sK; B = p.k.bB;
     } else if ((u -= 2 * nx) < 2 * ny) {  // y faces: i in [1,N0-2], k in [1,N2-2]
       int side = u >= ny; u -= side * ny;
       int i = 1 + (int)(u % (g.N0 - 2)), k = 1 + (int)(u / (g.N0 - 2));
       m = node_index(g, k, i, side ? g.N1 - 1 : 0);
-      in = side ? -1 : 1; o1 = sI; o2 = sK; B = g.cB;
+      in = side ? -1 : 1; o1 = sI; o2 = sK; B = p.k.cB;
     } else {  // z faces: i in [1,N0-2], j in [1,N1-2]
       u -= 2 * ny;
       int side = u >= nz; u -= side * nz;
       int j = 1 + (int)(u % (g.N1 - 2)), i = 1 + (int)(u / (g.N1 - 2));
       m = node_index(g, side ? g.N2 - 1 : 0, i, j);
-      in = side ? -sK : sK; o1 = sI; o2 = 1; B = g.dB;
+      in = side ? -sK : sK; o1 = sI; o2 = 1; B = p.k.dB;
     }
     for (int c = 0; c < p.ncomp; c++) {
       const long long off = c * g.cstride;
@@ -99,12 +120,12 @@ __global__ void __launch_bounds__(256) k_potential_faces(GridDev g, PotentialArg
 // Mur edges, AdvanceField::advanceEdgeF/S (src/database.cpp:179-229) with the argument
 // pattern of src/fdtd.cpp:480-645: a, b point into the domain, t runs along the edge.
 template <typename T>
-__device__ __forceinline__ T edge_value(const double* E, const T* np1, const T* n, const T* nm1,
+__device__ __forceinline__ T edge_value(const T* E, const T* np1, const T* n, const T* nm1,
                                         long long m, long long a, long long b, long long t) {
-  return (T)E[0] * (np1[m + a] + nm1[m + b]) + (T)E[1] * (nm1[m + a] + np1[m + b]) +
-         (T)E[2] * (nm1[m] + np1[m + a + b]) + (T)E[3] * (n[m] + n[m + a] + n[m + b] + n[m + a + b]) +
-         (T)E[4] * (n[m - t] + n[m + a - t] + n[m + b - t] + n[m + a + b - t] + n[m + t] + n[m + a + t] +
-                    n[m + b + t] + n[m + a + b + t]) -
+  return E[0] * (np1[m + a] + nm1[m + b]) + E[1] * (nm1[m + a] + np1[m + b]) +
+         E[2] * (nm1[m] + np1[m + a + b]) + E[3] * (n[m] + n[m + a] + n[m + b] + n[m + a + b]) +
+         E[4] * (n[m - t] + n[m + a - t] + n[m + b - t] + n[m + a + b - t] + n[m + t] + n[m + a + t] +
+                 n[m + b + t] + n[m + a + b + t]) -
          nm1[m + a + b];
 }
 
@@ -116,23 +137,23 @@ __global__ void __launch_bounds__(256) k_potential_edges(GridDev g, PotentialArg
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     long long u = t, m, a, b, tt;
-    const double* E;
+    const T* E;
     if (u < 4 * ez) {  // edges along z (eE), src/fdtd.cpp:480-522
       int which = (int)(u / ez); int k = 1 + (int)(u % ez);
       int hi_i = which & 1, hi_j = which >> 1;
       m = node_index(g, k, hi_i ? g.N0 - 1 : 0, hi_j ? g.N1 - 1 : 0);
-      a = hi_i ? -sI : sI; b = hi_j ? -1 : 1; tt = sK; E = g.eE;
+      a = hi_i ? -sI : sI; b = hi_j ? -1 : 1; tt = sK; E = p.k.eE;
     } else if ((u -= 4 * ez) < 4 * ex) {  // edges along x (fE), src/fdtd.cpp:527-579
       int which = (int)(u / ex); int i = 1 + (int)(u % ex);
       int hi_j = which & 1, hi_k = which >> 1;
       m = node_index(g, hi_k ? g.N2 - 1 : 0, i, hi_j ? g.N1 - 1 : 0);
-      a = hi_j ? -1 : 1; b = hi_k ? -sK : sK; tt = sI; E = g.fE;
+      a = hi_j ? -1 : 1; b = hi_k ? -sK : sK; tt = sI; E = p.k.fE;
     } else {  // edges along y (gE), src/fdtd.cpp:584-645
       u -= 4 * ex;
       int which = (int)(u / ey); int j = 1 + (int)(u % ey);
       int hi_i = which & 1, hi_k = which >> 1;
       m = node_index(g, hi_k ? g.N2 - 1 : 0, hi_i ? g.N0 - 1 : 0, j);
-      a = hi_k ? -sK : sK; b = hi_i ? -sI : sI; tt = 1; E = g.gE;
+      a = hi_k ? -sK : sK; b = hi_i ? -sI : sI; tt = 1; E = p.k.gE;
     }
     for (int c = 0; c < p.ncomp; c++) {
       const long long off = c * g.cstride;
@@ -154,15 +175,15 @@ __global__ void k_potential_corners(GridDev g, PotentialArgs<T> p) {
   const T* nm1 = p.nm1 + off;
   const long long m = node_index(g, hi_k ? g.N2 - 1 : 0, hi_i ? g.N0 - 1 : 0, hi_j ? g.N1 - 1 : 0);
   const long long a = hi_i ? -(long long)g.P1 : g.P1, b = hi_j ? -1 : 1, cc = hi_k ? -g.plane : g.plane;
-  const double* h = g.hC;
+  const T* h = p.k.hC;
   const long long P1 = m + a, P2 = m + b, P3 = m + cc, P4 = m + a + b, P5 = m + cc + a, P6 = m + cc + b,
                   P7 = m + a + b + cc;
-  T s = n[m] * (T)h[16] + nm1[m] * (T)h[8] + np1[P1] * (T)h[1] + n[P1] * (T)h[16] + nm1[P1] * (T)h[9] +
-        np1[P2] * (T)h[2] + n[P2] * (T)h[16] + nm1[P2] * (T)h[10] + np1[P3] * (T)h[3] + n[P3] * (T)h[16] +
-        nm1[P3] * (T)h[11] + np1[P4] * (T)h[4] + n[P4] * (T)h[16] + nm1[P4] * (T)h[12] + np1[P5] * (T)h[5] +
-        n[P5] * (T)h[16] + nm1[P5] * (T)h[13] + np1[P6] * (T)h[6] + n[P6] * (T)h[16] + nm1[P6] * (T)h[14] +
-        np1[P7] * (T)h[7] + n[P7] * (T)h[16] + nm1[P7] * (T)h[15];
-  p.np1[off + m] = -s / (T)h[0];
+  T s = n[m] * h[16] + nm1[m] * h[8] + np1[P1] * h[1] + n[P1] * h[16] + nm1[P1] * h[9] +
+        np1[P2] * h[2] + n[P2] * h[16] + nm1[P2] * h[10] + np1[P3] * h[3] + n[P3] * h[16] +
+        nm1[P3] * h[11] + np1[P4] * h[4] + n[P4] * h[16] + nm1[P4] * h[12] + np1[P5] * h[5] +
+        n[P5] * h[16] + nm1[P5] * h[13] + np1[P6] * h[6] + n[P6] * h[16] + nm1[P6] * h[14] +
+        np1[P7] * h[7] + n[P7] * h[16] + nm1[P7] * h[15];
+  p.np1[off + m] = -s / h[0];
 }
 
 // E and B at every interior node, the eager form of FdTd::fieldEvaluate (src/fdtd.cpp:818-845;
@@ -173,10 +194,14 @@ template <typename T>
 struct EBArgs {
   const T* anp1;
   const T* an;
-  const T* fn;  // scalar potential phi^n, or nullptr without space charge
-  float* E;     // 3 components, cstride apart
-  float* B;
+  const T* fn;   // scalar potential phi^n, or nullptr without space charge
+  T* E;          // 3 components, cstride apart; values are float-rounded
+  T* B;
+  const StateDev* st;          // slab of particle cells, or nullptr for every plane
+  const uint8_t* plane_needed; // N2 flags: planes a power sample reads, or nullptr
+  double rmdt, rdx2, rdy2, rdz2;  // -1/dt and 1/(2 d) per axis
 };
+
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_lo, int k_hi) {
@@ -184,10 +209,11 @@ __global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_l
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + k_lo;
   if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
+  if (!eb_plane_wanted(k, p.st, p.plane_needed, g.N2)) return;
   const long long m = node_index(g, k, i, j);
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
-  const double rmdt = -1.0 / g.dt;
-  const double rdx2 = 1.0 / (2.0 * g.dx), rdy2 = 1.0 / (2.0 * g.dy), rdz2 = 1.0 / (2.0 * g.dz);
+  const double rmdt = p.rmdt;
+  const double rdx2 = p.rdx2, rdy2 = p.rdy2, rdz2 = p.rdz2;
   const T *A1 = p.anp1, *A0 = p.an;
   float e[3], b[3];
 #pragma unroll
@@ -202,25 +228,27 @@ __global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_l
     e[2] = (float)((double)e[2] - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
   }
   const T *X0 = A0, *Y0 = A0 + cs, *Z0 = A0 + 2 * cs, *X1 = A1, *Y1 = A1 + cs, *Z1 = A1 + 2 * cs;
-  double bx = 0.5 * (((double)Z0[m + 1] - Z0[m - 1]) * rdy2 - ((double)Y0[m + sK] - Y0[m - sK]) * rdz2 +
-                     ((double)Z1[m + 1] - Z1[m - 1]) * rdy2 - ((double)Y1[m + sK] - Y1[m - sK]) * rdz2);
-  double by = 0.5 * (((double)X0[m + sK] - X0[m - sK]) * rdz2 - ((double)Z0[m + sI] - Z0[m - sI]) * rdx2 +
-                     ((double)X1[m + sK] - X1[m - sK]) * rdz2 - ((double)Z1[m + sI] - Z1[m - sI]) * rdx2);
-  double bz = 0.5 * (((double)Y0[m + sI] - Y0[m - sI]) * rdx2 - ((double)X0[m + 1] - X0[m - 1]) * rdy2 +
-                     ((double)Y1[m + sI] - Y1[m - sI]) * rdx2 - ((double)X1[m + 1] - X1[m - 1]) * rdy2);
+  // 0.5 * (curl A^n + curl A^{n+1}) with the two levels summed first.
+  const double hx = 0.5 * rdx2, hy = 0.5 * rdy2, hz = 0.5 * rdz2;
+  double bx = (((double)Z0[m + 1] + Z1[m + 1]) - ((double)Z0[m - 1] + Z1[m - 1])) * hy -
+              (((double)Y0[m + sK] + Y1[m + sK]) - ((double)Y0[m - sK] + Y1[m - sK])) * hz;
+  double by = (((double)X0[m + sK] + X1[m + sK]) - ((double)X0[m - sK] + X1[m - sK])) * hz -
+              (((double)Z0[m + sI] + Z1[m + sI]) - ((double)Z0[m - sI] + Z1[m - sI])) * hx;
+  double bz = (((double)Y0[m + sI] + Y1[m + sI]) - ((double)Y0[m - sI] + Y1[m - sI])) * hx -
+              (((double)X0[m + 1] + X1[m + 1]) - ((double)X0[m - 1] + X1[m - 1])) * hy;
   b[0] = (float)bx; b[1] = (float)by; b[2] = (float)bz;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    p.E[c * cs + m] = e[c];
-    p.B[c * cs + m] = b[c];
+    p.E[c * cs + m] = (T)e[c];
+    p.B[c * cs + m] = (T)b[c];
   }
   if (k == 1) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = e[c]; p.B[c * cs + m - sK] = b[c]; }
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = (T)e[c]; p.B[c * cs + m - sK] = (T)b[c]; }
   }
   if (k == g.N2 - 2) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = e[c]; p.B[c * cs + m + sK] = b[c]; }
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = (T)e[c]; p.B[c * cs + m + sK] = (T)b[c]; }
   }
 }
 

@@ -1,0 +1,522 @@
+// Kernels of the mixed-precision form.
+//
+// Storage: potentials, J, rho, E and B in FP32; particles as an integer cell (packed 64-bit) plus
+// an FP32 offset inside the cell (in cell units) and FP32 gamma*beta.  FP64 is kept where the
+// magnitudes need it: the lab-frame undulator coordinate lz (up to ~1e6 length units, whose
+// phase ku*lz must be exact to ~1e-7 rad) is formed and range-reduced in FP64, and the time
+// state stays FP64.  Everything else runs on the FP32 pipes.
+#pragma once
+#include "device_common.cuh"
+
+namespace mithra {
+
+// E and B from FP32 potentials (the FdTd::fieldEvaluate formulas, src/fdtd.cpp:818-845, in
+// float; with space charge src/fdtdSC.cpp:1116-1118).
+struct EBConstF32 {
+  float rdt, hx, hy, hz;  // 1/dt and 0.5/(2 d) per axis
+};
+
+__global__ void __launch_bounds__(256) k_eval_eb_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
+                                                     const float* __restrict__ A0,
+                                                     const float* __restrict__ fn, float* __restrict__ E,
+                                                     float* __restrict__ B, int k_lo, int k_hi, const StateDev* st,
+                                                     const uint8_t* plane_needed) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + k_lo;
+  if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
+  if (!eb_plane_wanted(k, st, plane_needed, g.N2)) return;
+  const long long m = node_index(g, k, i, j);
+  const long long cs = g.cstride, sI = g.P1, sK = g.plane;
+  const float rdt = c.rdt, hx = c.hx, hy = c.hy, hz = c.hz;
+  float e0 = (A0[m] - A1[m]) * rdt;
+  float e1 = (A0[cs + m] - A1[cs + m]) * rdt;
+  float e2 = (A0[2 * cs + m] - A1[2 * cs + m]) * rdt;
+  if (fn) {
+    e0 -= (fn[m + sI] - fn[m - sI]) * (2.0f * hx);
+    e1 -= (fn[m + 1] - fn[m - 1]) * (2.0f * hy);
+    e2 -= (fn[m + sK] - fn[m - sK]) * (2.0f * hz);
+  }
+  const float *X0 = A0, *Y0 = A0 + cs, *Z0 = A0 + 2 * cs, *X1 = A1, *Y1 = A1 + cs, *Z1 = A1 + 2 * cs;
+  const float b0 = ((Z0[m + 1] + Z1[m + 1]) - (Z0[m - 1] + Z1[m - 1])) * hy -
+                   ((Y0[m + sK] + Y1[m + sK]) - (Y0[m - sK] + Y1[m - sK])) * hz;
+  const float b1 = ((X0[m + sK] + X1[m + sK]) - (X0[m - sK] + X1[m - sK])) * hz -
+                   ((Z0[m + sI] + Z1[m + sI]) - (Z0[m - sI] + Z1[m - sI])) * hx;
+  const float b2 = ((Y0[m + sI] + Y1[m + sI]) - (Y0[m - sI] + Y1[m - sI])) * hx -
+                   ((X0[m + 1] + X1[m + 1]) - (X0[m - 1] + X1[m - 1])) * hy;
+  E[m] = e0; E[cs + m] = e1; E[2 * cs + m] = e2;
+  B[m] = b0; B[cs + m] = b1; B[2 * cs + m] = b2;
+  if (k == 1) {
+    E[m - sK] = e0; E[cs + m - sK] = e1; E[2 * cs + m - sK] = e2;
+    B[m - sK] = b0; B[cs + m - sK] = b1; B[2 * cs + m - sK] = b2;
+  }
+  if (k == g.N2 - 2) {
+    E[m + sK] = e0; E[cs + m + sK] = e1; E[2 * cs + m + sK] = e2;
+    B[m + sK] = b0; B[cs + m + sK] = b1; B[2 * cs + m + sK] = b2;
+  }
+}
+
+// Per-launch constants of the mixed-precision push, prepared on the host from GridDev/PushDev.
+struct PushF32 {
+  float rdx, rdy, rdz;           // 1/d in cell units per length unit
+  float dx, dy, dz;
+  float xmin, ymin;              // for the transverse undulator coordinate
+  float r1, r2, dtb;
+  int N0, N1, N2;
+  double zmin, dzd, gamma, bc;   // FP64: z reconstruction and the lab frame (bc = beta*c0)
+  double dt_shift;
+  int n_und;
+  double und0_dist;
+  float gamma_f, bc_f, gdz;      // gamma, beta*c0 and gamma*dz in FP32
+  float zmin_f, dz_f, und0_dist_f;
+};
+
+// Static undulator field (src/solver.cpp:1798-1824, src/beam.cc:14-76).
+//
+// The lab coordinate lz = gamma (z + beta c0 (timeBunch + dt_)) - rb reaches ~1e6 length units,
+// so the phase ku*lz cannot be formed in FP32.  With z = zmin + (k + fz) dz it splits into a
+// per-plane part, computed in FP64 and reduced modulo 2 pi once per substep for every plane k
+// (k_undulator_table), and an in-cell part (ku gamma dz) fz that is small and formed in FP32.
+struct UndTableEntry {
+  float lz;     // lab coordinate of plane k (relative to the module start)
+  float phase;  // ku * lz reduced to [-pi, pi]
+};
+
+__global__ void k_undulator_table(const UndDev* __restrict__ und, int n_und, int N2, double zmin, double dz,
+                                  double gamma, double bc, double dt_shift, const StateDev* st,
+                                  UndTableEntry* table) {
+  const double tshift = bc * (st->time_bunch + dt_shift);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_und * (N2 + 1); t += gridDim.x * blockDim.x) {
+    const int u = t / (N2 + 1), k = t % (N2 + 1);
+    const double lz = gamma * (zmin + (double)k * dz + tshift) - und[u].rb;
+    const double ph = und[u].ku * lz;
+    const double n = rint(ph * (1.0 / (2.0 * kPI)));
+    table[t].lz = (float)lz;
+    table[t].phase = (float)fma(-n, 2.0 * kPI, ph);
+  }
+}
+
+__device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, const UndTableEntry* __restrict__ table,
+                                              int n_und, int N2, float gdz, int k, float fz, double zd_slow,
+                                              double tshift, double gamma, float x, float y, float* bt, float* et,
+                                              float gamma_f, float bc_f) {
+  for (int u = 0; u < n_und; u++) {
+    const UndDev& U = und[u];
+    if (U.type != 0) continue;
+    float lz, phase;
+    if (k >= 0 && k <= N2) {
+      const UndTableEntry te = table[u * (N2 + 1) + k];
+      lz = fmaf(gdz, fz, te.lz);
+      phase = fmaf(U.ku_f * gdz, fz, te.phase);
+    } else {  // outside the mesh along z (rare): form the phase in FP64
+      const double lzd = gamma * (zd_slow + tshift) - U.rb;
+      const double ph = U.ku * lzd;
+      lz = (float)lzd;
+      phase = (float)fma(-rint(ph * (1.0 / (2.0 * kPI))), 2.0 * kPI, ph);
+    }
+    const float ct = U.ct_f, st = U.st_f, ku = U.ku_f, b0 = U.b0_f;
+    const float ly = x * ct + y * st;
+    float s_ly, c_ly;
+    {
+      const float a = ku * ly;
+      const float e = __expf(a);
+      const float ie = 1.0f / e;
+      c_ly = 0.5f * (e + ie);
+      if (fabsf(a) < 0.05f) {  // short series where e - 1/e cancels
+        const float a2 = a * a;
+        s_ly = a * (1.0f + a2 * (1.0f / 6.0f) * (1.0f + a2 * (1.0f / 20.0f)));
+      } else {
+        s_ly = 0.5f * (e - ie);
+      }
+    }
+    float d1, bz;
+    if (lz >= 0.0f && lz <= U.ul_f) {
+      float sn, cs;
+      __sincosf(phase, &sn, &cs);
+      d1 = b0 * c_ly * sn * gamma_f;
+      bz = b0 * s_ly * cs;
+    } else {
+      const float t0 = (lz < 0.0f) ? lz : lz - U.ul_f;
+      const float kt = ku * t0;
+      float sz = __expf(-0.5f * kt * kt);
+      const bool has = (lz < 0.0f) ? U.has_prev : U.has_next;
+      if (has) {
+        const float r0 = (lz < 0.0f) ? U.r0_prev_f : U.r0_next_f;
+        const bool cut = (lz < 0.0f) ? (t0 < r0 || r0 == 0.0f) : (t0 > r0 || r0 == 0.0f);
+        if (cut) sz = 0.0f;
+        else {
+          const float a = 3.1415926535f * t0 / r0;
+          sz *= 0.35875f + 0.48829f * __cosf(a) + 0.14128f * __cosf(2.0f * a) + 0.01168f * __cosf(3.0f * a);
+        }
+      }
+      d1 = b0 * c_ly * sz * ku * t0 * gamma_f;
+      bz = b0 * s_ly * sz;
+    }
+    bt[0] += d1 * ct;
+    bt[1] += d1 * st;
+    bt[2] += bz;
+    d1 *= bc_f;
+    et[1] += d1 * ct;
+    et[0] -= d1 * st;
+  }
+}
+
+// One bunch substep (src/solver.cpp:1424-1549) in the mixed form.  Positions are (cell, offset)
+// in cell units; the owned-domain test of the reference (wrapped z in [zp0, zp1)) is always true
+// for one domain and is folded into the crossing test.
+__global__ void __launch_bounds__(256) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
+                                                  const UndTableEntry* __restrict__ table, ParticlesF32 pt,
+                                                  const float* __restrict__ E, const float* __restrict__ B,
+                                                  long long cstride, long long plane, int P1, StateDev* st,
+                                                  int save_rnm) {
+  const long long n = st->n_particles;
+  const double tb = st->time_bunch;
+  const double tshift = C.bc * (tb + C.dt_shift);  // beta c0 (timeBunch + dt_)
+  unsigned long long local_cross = 0, local_nt = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    int8_t cross = 0;
+    if (!(pt.status[p] & 1)) {
+      const long long cell = pt.cell[p];
+      int i, j, k;
+      unpack_cell(cell, i, j, k);
+      const int Lk = C.N2 - 1;
+      const int kw = ((k % Lk) + Lk) % Lk;  // wrapped cell of pmod(z - zmin, Lz)
+      float fx = pt.fx[p], fy = pt.fy[p], fz = pt.fz[p];
+      if (save_rnm) { pt.mcell[p] = cell; pt.mfx[p] = fx; pt.mfy[p] = fy; pt.mfz[p] = fz; }
+      const float x = C.xmin + ((float)i + fx) * C.dx, y = C.ymin + ((float)j + fy) * C.dy;
+      const bool b1x = (i >= 1 && i <= C.N0 - 3 && (i > 1 || fx > 0.0f));
+      const bool b1y = (j >= 1 && j <= C.N1 - 3 && (j > 1 || fy > 0.0f));
+      const bool b1z = (k >= 0 && k <= C.N2 - 2);
+      float bt[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
+      const bool k_in = (k >= 0 && k <= C.N2);
+      const double zd_slow = k_in ? 0.0 : C.zmin + ((double)k + (double)fz) * C.dzd;
+      undulator_f32(und, table, C.n_und, C.N2, C.gdz, k, fz, zd_slow, tshift, C.gamma, x, y, bt, et, C.gamma_f, C.bc_f);
+      uint8_t e = pt.e[p];
+      if (e) {
+        if (b1x && b1y && b1z) {
+          const long long m = (long long)k * plane + (long long)i * P1 + j;
+          const long long sI = P1, sK = plane;
+          const float wx0 = 1.0f - fx, wy0 = 1.0f - fy, wz0 = 1.0f - fz;
+          const float w[8] = {wx0 * wy0 * wz0, fx * wy0 * wz0, wx0 * fy * wz0, fx * fy * wz0,
+                              wx0 * wy0 * fz, fx * wy0 * fz, wx0 * fy * fz, fx * fy * fz};
+          const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+#pragma unroll
+          for (int c = 0; c < 3; c++) {
+            float se = et[c], sb = bt[c];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+              se = fmaf(w[q], __ldg(E + c * cstride + nd[q]), se);
+              sb = fmaf(w[q], __ldg(B + c * cstride + nd[q]), sb);
+            }
+            et[c] = se; bt[c] = sb;
+          }
+        } else if (!b1x && !b1y && b1z) {
+          local_nt++;
+        }
+      } else if (C.n_und > 0) {
+        // lz without the module offset rb: rb of the first module is zero after the shift of
+        // src/solver.cpp:184-185, so it is the first table entry's lz.
+        float lz;
+        if (k_in) lz = fmaf(C.gdz, fz, table[k].lz + (float)und[0].rb);
+        else lz = (float)(C.gamma * (zd_slow + tshift));
+        e = (lz > -C.und0_dist_f) ? 1 : 0;
+        pt.e[p] = e;
+      } else {
+        pt.e[p] = 1;
+      }
+      // Boris rotation and drift (src/solver.cpp:1519-1541) in FP32.
+      float gx = pt.gx[p], gy = pt.gy[p], gz = pt.gz[p];
+      const float mx = fmaf(C.r1, et[0], gx), my = fmaf(C.r1, et[1], gy), mz = fmaf(C.r1, et[2], gz);
+      const float d1 = sqrtf(1.0f + (mx * mx + my * my + mz * mz));
+      const float f = C.r2 / d1;
+      const float px = fmaf(f, my * bt[2] - mz * bt[1], mx);
+      const float py = fmaf(f, mz * bt[0] - mx * bt[2], my);
+      const float pz = fmaf(f, mx * bt[1] - my * bt[0], mz);
+      const float bt2 = bt[0] * bt[0] + bt[1] * bt[1] + bt[2] * bt[2];
+      const float s = 2.0f / (d1 / C.r2 + f * bt2);
+      gx = fmaf(s, py * bt[2] - pz * bt[1], mx) + C.r1 * et[0];
+      gy = fmaf(s, pz * bt[0] - px * bt[2], my) + C.r1 * et[1];
+      gz = fmaf(s, px * bt[1] - py * bt[0], mz) + C.r1 * et[2];
+      pt.gx[p] = gx; pt.gy[p] = gy; pt.gz[p] = gz;
+      const float gg = C.dtb * rsqrtf(1.0f + (gx * gx + gy * gy + gz * gz));
+      fx = fmaf(gg * C.rdx, gx, fx);
+      fy = fmaf(gg * C.rdy, gy, fy);
+      const float dzc = gg * C.rdz * gz;
+      fz += dzc;
+      const float ix = floorf(fx), iy = floorf(fy), iz = floorf(fz);
+      i += (int)ix; j += (int)iy; k += (int)iz;
+      fx -= ix; fy -= iy; fz -= iz;
+      pt.cell[p] = pack_cell(i, j, k);
+      pt.fx[p] = fx; pt.fy[p] = fy; pt.fz[p] = fz;
+      // z-face crossing of the wrapped position (src/solver.cpp:1544-1548), in cells.
+      const int kwn = kw + (int)iz;
+      if (kwn < 0) cross = 1;
+      else if (kwn >= Lk) cross = 2;
+    }
+    pt.cross[p] = cross;
+    local_cross += (cross != 0);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    local_cross += __shfl_down_sync(0xffffffffu, local_cross, o);
+    local_nt += __shfl_down_sync(0xffffffffu, local_nt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (local_cross) atomicAdd(&st->n_cross, local_cross);
+    if (local_nt) atomicAdd(&st->n_transverse, local_nt);
+  }
+}
+
+// The ordered append of z-face copies (src/solver.cpp:1551-1568) and the bunch time advance,
+// for the mixed-form particle arrays (one block).
+__global__ void __launch_bounds__(1024) k_substep_end_f32(ParticlesF32 pt, StateDev* st, double bunch_time_step) {
+  __shared__ long long s_base;
+  __shared__ int s_warp[32];
+  const unsigned long long ncross = st->n_cross;
+  if (ncross) {
+    const long long n = st->n_particles;
+    if (threadIdx.x == 0) s_base = n;
+    __syncthreads();
+    if ((long long)(n + ncross) > st->capacity) {
+      if (threadIdx.x == 0) st->overflow = 1;
+    } else {
+      for (int pass = 1; pass <= 2; pass++) {
+        for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
+          const long long p = c0 + threadIdx.x;
+          const int take = (p < n) && (pt.cross[p] == pass);
+          const unsigned bal = __ballot_sync(0xffffffffu, take);
+          const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+          if (lane == 0) s_warp[warp] = __popc(bal);
+          __syncthreads();
+          int before = 0, total = 0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            if (w < warp) before += s_warp[w];
+            total += s_warp[w];
+          }
+          before += __popc(bal & ((1u << lane) - 1u));
+          if (take) {
+            const long long d = s_base + before;
+            pt.cell[d] = pt.cell[p]; pt.fx[d] = pt.fx[p]; pt.fy[d] = pt.fy[p]; pt.fz[d] = pt.fz[p];
+            pt.gx[d] = pt.gx[p]; pt.gy[d] = pt.gy[p]; pt.gz[d] = pt.gz[p];
+            pt.mcell[d] = pt.mcell[p]; pt.mfx[d] = pt.mfx[p]; pt.mfy[d] = pt.mfy[p]; pt.mfz[d] = pt.mfz[p];
+            pt.q[d] = pt.q[p]; pt.e[d] = pt.e[p]; pt.status[d] = pt.status[p]; pt.cross[d] = 0;
+            pt.id[d] = st->next_id + (d - n);
+          }
+          __syncthreads();
+          if (threadIdx.x == 0) s_base += total;
+          __syncthreads();
+        }
+      }
+      if (threadIdx.x == 0) {
+        st->next_id += s_base - n;
+        st->n_particles = s_base;
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    st->n_cross = 0;
+    st->time_bunch += bunch_time_step;
+    st->n_time_bunch += 1;
+  }
+}
+
+// Erasure of particles whose wrapped z is outside the domain (src/solver.cpp:493-503): with cells,
+// the wrapped cell index always lands inside, so only non-finite states are erased.
+__global__ void __launch_bounds__(256) k_erase_f32(ParticlesF32 pt, StateDev* st) {
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (pt.status[p] & 1) continue;
+    if (!isfinite(pt.gx[p] + pt.gy[p] + pt.gz[p] + pt.fx[p] + pt.fy[p] + pt.fz[p])) {
+      pt.status[p] |= 1;
+      atomicAdd(&st->nonfinite, 1);
+    }
+  }
+}
+
+__global__ void k_save_positions_f32(ParticlesF32 pt, const StateDev* st) {
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    pt.mcell[p] = pt.cell[p]; pt.mfx[p] = pt.fx[p]; pt.mfy[p] = pt.fy[p]; pt.mfz[p] = pt.fz[p];
+  }
+}
+
+// Zigzag deposit (src/fdtd.cpp:38-185) in cell-relative FP32 coordinates: both endpoints are
+// expressed relative to the lower of their two cells along each axis, so the relay point and
+// the half-segment midpoints keep full FP32 resolution at any mesh size.
+struct DepositF32 {
+  int N0, N1, N2;
+  float dx, dy, dz;
+};
+
+__device__ __forceinline__ void deposit_half_f32(float* J, long long cs, long long m, long long sI, long long sK,
+                                                 float qh, float ax, float ay, float az, float jx, float jy, float jz) {
+  const float x1 = 1.0f - ax, x2 = ax, y1 = 1.0f - ay, y2 = ay, z1 = 1.0f - az, z2 = az;
+  const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+  const float wx[8] = {y1 * z1, y1 * z1, y2 * z1, y2 * z1, y1 * z2, y1 * z2, y2 * z2, y2 * z2};
+  const float wy[8] = {x1 * z1, x2 * z1, x1 * z1, x2 * z1, x1 * z2, x2 * z2, x1 * z2, x2 * z2};
+  const float wz[8] = {x1 * y1, x2 * y1, x1 * y2, x2 * y2, x1 * y1, x2 * y1, x1 * y2, x2 * y2};
+  const float qx = qh * jx, qy = qh * jy, qz = qh * jz;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    atomicAdd(J + nd[q], wx[q] * qx);
+    atomicAdd(J + cs + nd[q], wy[q] * qy);
+    atomicAdd(J + 2 * cs + nd[q], wz[q] * qz);
+  }
+}
+
+__device__ __forceinline__ bool inside_f32(const DepositF32& D, int i, int j, int k, float fx, float fy) {
+  return (i >= 1 && i <= D.N0 - 3 && (i > 1 || fx > 0.0f)) && (j >= 1 && j <= D.N1 - 3 && (j > 1 || fy > 0.0f)) &&
+         (k >= 0 && k <= D.N2 - 2);
+}
+
+// Relay point along one axis: returns the relay coordinate relative to `base` (the lower cell).
+__device__ __forceinline__ float relay_axis(int cm, int cp, float fm, float fp, int* base, float* rm, float* rp) {
+  const int b = min(cm, cp);
+  *base = b;
+  *rm = (float)(cm - b) + fm;
+  *rp = (float)(cp - b) + fp;
+  const float lo = (float)(max(cm, cp) - b), hi = 1.0f;
+  return fminf(hi, fmaxf(lo, 0.5f * (*rm + *rp)));
+}
+
+__global__ void __launch_bounds__(256) k_deposit_f32(DepositF32 D, ParticlesF32 pt, StateDev* st, float* J,
+                                                     float* rho, long long cs, long long plane, int P1) {
+  const long long n = st->n_particles;
+  const long long sI = P1, sK = plane;
+  int kmin = 0x7fffffff, kmax = -0x7fffffff;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (pt.status[p] & 1) continue;
+    int ip, jp, kp, im, jm, km;
+    unpack_cell(pt.cell[p], ip, jp, kp);
+    unpack_cell(pt.mcell[p], im, jm, km);
+    kmin = min(kmin, kp);
+    kmax = max(kmax, kp);
+    const float fxp = pt.fx[p], fyp = pt.fy[p], fzp = pt.fz[p];
+    const float fxm = pt.mfx[p], fym = pt.mfy[p], fzm = pt.mfz[p];
+    const bool bp = inside_f32(D, ip, jp, kp, fxp, fyp);
+    const bool bm = inside_f32(D, im, jm, km, fxm, fym);
+    if (!(bp || bm)) continue;
+    int bx, by, bz;
+    float rxm, rxp, rym, ryp, rzm, rzp;
+    const float rx = relay_axis(im, ip, fxm, fxp, &bx, &rxm, &rxp);
+    const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
+    const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
+    const float qh = 0.5f * pt.q[p];
+    if (bp) {
+      const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
+      const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
+                  az = 0.5f * (rzp + rz) - (float)(kp - bz);
+      deposit_half_f32(J, cs, m, sI, sK, qh, ax, ay, az, (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+      if (rho) {
+        const float q = pt.q[p];
+        const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
+        atomicAdd(rho + m, q * x1 * y1 * z1);
+        atomicAdd(rho + m + sI, q * fxp * y1 * z1);
+        atomicAdd(rho + m + 1, q * x1 * fyp * z1);
+        atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
+        atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
+        atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
+        atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
+        atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
+      }
+    }
+    if (bm) {
+      const long long m = (long long)km * plane + (long long)im * P1 + jm;
+      const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
+                  az = 0.5f * (rzm + rz) - (float)(km - bz);
+      deposit_half_f32(J, cs, m, sI, sK, qh, ax, ay, az, (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
+  }
+  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
+    atomicMin(&st->k_lo_next, kmin);
+    atomicMax(&st->k_hi_next, kmax);
+  }
+}
+
+// Records (11 doubles) <-> mixed-form particles.  Cell = floor((x - xmin)/dx) in FP64.
+struct CellMap {
+  double xmin, ymin, zmin, dx, dy, dz;
+};
+
+__global__ void k_records_to_f32(const double* __restrict__ rec, long long n, ParticlesF32 pt, CellMap M) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double* r = rec + 11 * p;
+    auto split = [](double v, int& c, float& f) {
+      const double fl = floor(v);
+      c = (int)fl;
+      f = (float)(v - fl);
+      if (f >= 1.0f) { f = 0.0f; c += 1; }
+    };
+    int i, j, k;
+    float fx, fy, fz;
+    split((r[1] - M.xmin) / M.dx, i, fx);
+    split((r[2] - M.ymin) / M.dy, j, fy);
+    split((r[3] - M.zmin) / M.dz, k, fz);
+    pt.cell[p] = pack_cell(i, j, k);
+    pt.fx[p] = fx; pt.fy[p] = fy; pt.fz[p] = fz;
+    split((r[4] - M.xmin) / M.dx, i, fx);
+    split((r[5] - M.ymin) / M.dy, j, fy);
+    split((r[6] - M.zmin) / M.dz, k, fz);
+    pt.mcell[p] = pack_cell(i, j, k);
+    pt.mfx[p] = fx; pt.mfy[p] = fy; pt.mfz[p] = fz;
+    pt.gx[p] = (float)r[7]; pt.gy[p] = (float)r[8]; pt.gz[p] = (float)r[9];
+    pt.q[p] = (float)r[0];
+    pt.e[p] = r[10] == 1.0 ? 1 : 0;
+    pt.status[p] = 0;
+    pt.cross[p] = 0;
+    pt.id[p] = (int)p;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_f32_to_records(ParticlesF32 pt, const StateDev* st, double* rec, long long cap,
+                                                         long long* n_out, CellMap M) {
+  __shared__ int s_warp[32];
+  __shared__ long long s_base;
+  const long long n = st->n_particles;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
+    const long long p = c0 + threadIdx.x;
+    const int take = (p < n) && !(pt.status[p] & 1);
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      if (w < warp) before += s_warp[w];
+      total += s_warp[w];
+    }
+    before += __popc(bal & ((1u << lane) - 1u));
+    const long long d = s_base + before;
+    if (take && d < cap) {
+      double* r = rec + 11 * d;
+      int i, j, k;
+      unpack_cell(pt.cell[p], i, j, k);
+      r[0] = pt.q[p];
+      r[1] = M.xmin + ((double)i + (double)pt.fx[p]) * M.dx;
+      r[2] = M.ymin + ((double)j + (double)pt.fy[p]) * M.dy;
+      r[3] = M.zmin + ((double)k + (double)pt.fz[p]) * M.dz;
+      unpack_cell(pt.mcell[p], i, j, k);
+      r[4] = M.xmin + ((double)i + (double)pt.mfx[p]) * M.dx;
+      r[5] = M.ymin + ((double)j + (double)pt.mfy[p]) * M.dy;
+      r[6] = M.zmin + ((double)k + (double)pt.mfz[p]) * M.dz;
+      r[7] = pt.gx[p]; r[8] = pt.gy[p]; r[9] = pt.gz[p];
+      r[10] = pt.e[p] ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *n_out = s_base;
+}
+
+}  // namespace mithra

@@ -137,10 +137,14 @@ int run_potential(mithra_ctx* ctx, PotentialArgs<double> p, bool vector) {
   return MITHRA_OK;
 }
 
-int stage_eval_eb(mithra_ctx* ctx) {
+// full = true evaluates every interior plane; otherwise only the particle slab and the planes
+// a power sample reads (the nodes the reference's lazy evaluation can touch).
+int stage_eval_eb(mithra_ctx* ctx, bool full = false) {
   const GridDev& g = ctx->g;
   const double* fn = g.space_charge ? ctx->F[ctx->idx[1]] : nullptr;
-  EBArgs<double> eb{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], fn, ctx->E, ctx->B};
+  EBArgs<double> eb{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], fn, ctx->E64, ctx->B64,
+                    full ? nullptr : ctx->st, ctx->plane_needed,
+                    -1.0 / g.dt, 1.0 / (2.0 * g.dx), 1.0 / (2.0 * g.dy), 1.0 / (2.0 * g.dz)};
   dim3 blk(32, 8), grd((g.N1 - 2 + 31) / 32, (g.N0 - 2 + 7) / 8, g.N2 - 2);
   return timed(ctx, "eval_eb", [&] { k_eval_eb<double><<<grd, blk, 0, ctx->stream>>>(g, eb, 1, g.N2 - 2); });
 }
@@ -149,10 +153,11 @@ int stage_field_update(mithra_ctx* ctx) {
   if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_field_update(ctx);
   const GridDev& g = ctx->g;
   int r;
-  PotentialArgs<double> pa{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], ctx->A[ctx->idx[2]], 3, g.a[4]};
+  const Coeffs<double> k = make_coeffs<double>(g);
+  PotentialArgs<double> pa{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], ctx->A[ctx->idx[2]], 3, g.a[4], k};
   if ((r = run_potential(ctx, pa, true))) return r;
   if (g.space_charge) {
-    PotentialArgs<double> pf{ctx->F[ctx->idx[0]], ctx->F[ctx->idx[1]], ctx->F[ctx->idx[2]], 1, g.a[5]};
+    PotentialArgs<double> pf{ctx->F[ctx->idx[0]], ctx->F[ctx->idx[1]], ctx->F[ctx->idx[2]], 1, g.a[5], k};
     if ((r = run_potential(ctx, pf, false))) return r;
   }
   return stage_eval_eb(ctx);
@@ -162,7 +167,7 @@ int stage_push(mithra_ctx* ctx, int save_rnm) {
   if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_push(ctx, save_rnm);
   int r = timed(ctx, "push", [&] {
     k_push_fp64<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(
-        ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E, ctx->B, ctx->st, save_rnm);
+        ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E64, ctx->B64, ctx->st, save_rnm);
   });
   if (r) return r;
   return timed(ctx, "substep_end", [&] {
@@ -190,7 +195,10 @@ int stage_power(mithra_ctx* ctx) {
     const int blocks = po.dev.N * po.dev.blocks_per_plane;
     const size_t shm = (size_t)kPowerBlock * po.dev.Nl * sizeof(double);
     int r = timed(ctx, "power_sample", [&] {
-      k_power_sample<kPowerBlock><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E, ctx->B, ctx->st);
+      if (ctx->precision == MITHRA_PRECISION_FP64)
+        k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E64, ctx->B64, ctx->st);
+      else
+        k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E, ctx->B, ctx->st);
     });
     if (r) return r;
     const int last = (o + 1 == ctx->power.size());
@@ -280,6 +288,12 @@ int check_state(mithra_ctx* ctx) {
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->st_host->overflow)
     return fail(ctx, MITHRA_ERR_CAPACITY, "particle capacity %lld exceeded by z-face copies", ctx->st_host->capacity);
+  if (ctx->f32.tma_error) {
+    int e = 0;
+    CK(cudaMemcpy(&e, ctx->f32.tma_error, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return fail(ctx, MITHRA_ERR_STATE, "interior stencil: bulk-tensor copy %s (code %d)",
+                       e == 2 ? "refused on an unaligned shared-memory slot" : "wait timed out", e);
+  }
   return MITHRA_OK;
 }
 
@@ -327,11 +341,13 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
     memcpy(g.eE, gd->eE, sizeof g.eE); memcpy(g.fE, gd->fE, sizeof g.fE); memcpy(g.gE, gd->gE, sizeof g.gE);
     memcpy(g.hC, gd->hC, sizeof g.hC);
     g.dt = gd->dt; g.dx = gd->dx; g.dy = gd->dy; g.dz = gd->dz;
+    g.rdx = 1.0 / gd->dx; g.rdy = 1.0 / gd->dy; g.rdz = 1.0 / gd->dz;
     g.xmin = gd->xmin; g.xmax = gd->xmax; g.ymin = gd->ymin; g.ymax = gd->ymax;
     g.zmin = gd->zmin; g.zmax = gd->zmax; g.zp0 = gd->zp0; g.zp1 = gd->zp1; g.Lz = gd->Lz;
     PushDev& P = ctx->P;
     P.dtb = pd->dtb; P.r1 = pd->r1; P.r2 = pd->r2; P.gamma = pd->gamma; P.beta = pd->beta; P.c0 = pd->c0;
     P.dt_shift = pd->dt_shift; P.bunch_time_step = pd->bunch_time_step; P.n_und = 0; P.und0_dist = 0.0;
+    P.inv_r2 = 1.0 / pd->r2;
     CK(dalloc(&ctx->und_dev, kMaxUndulators));
     const size_t nf = (size_t)3 * g.cstride;
     ctx->capacity = std::max<size_t>(particle_capacity, 1);
@@ -355,14 +371,27 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
       int r = fp32_alloc(ctx);
       if (r) return r;
     }
-    CK(dalloc(&ctx->E, nf));
-    CK(dalloc(&ctx->B, nf));
-    CK(cudaMemsetAsync(ctx->E, 0, nf * sizeof(float), ctx->stream));
-    CK(cudaMemsetAsync(ctx->B, 0, nf * sizeof(float), ctx->stream));
+    if (precision == MITHRA_PRECISION_FP64) {
+      CK(dalloc(&ctx->E64, nf));
+      CK(dalloc(&ctx->B64, nf));
+      CK(cudaMemsetAsync(ctx->E64, 0, nf * sizeof(double), ctx->stream));
+      CK(cudaMemsetAsync(ctx->B64, 0, nf * sizeof(double), ctx->stream));
+    } else {
+      CK(dalloc(&ctx->E, nf));
+      CK(dalloc(&ctx->B, nf));
+      CK(cudaMemsetAsync(ctx->E, 0, nf * sizeof(float), ctx->stream));
+      CK(cudaMemsetAsync(ctx->B, 0, nf * sizeof(float), ctx->stream));
+    }
+    CK(dalloc(&ctx->plane_needed, (size_t)g.N2));
+    CK(cudaMemsetAsync(ctx->plane_needed, 0, (size_t)g.N2, ctx->stream));
     CK(dalloc(&ctx->st, 1));
     CK(cudaMallocHost((void**)&ctx->st_host, sizeof(StateDev)));
     memset(ctx->st_host, 0, sizeof(StateDev));
     ctx->st_host->capacity = (long long)ctx->capacity;
+    ctx->st_host->k_lo = 0;
+    ctx->st_host->k_hi = g.N2 - 1;
+    ctx->st_host->k_lo_next = 0x7fffffff;
+    ctx->st_host->k_hi_next = -0x7fffffff;
     CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return MITHRA_OK;
@@ -388,6 +417,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   for (void* p : ps) cudaFree(p);
   fp32_free(ctx);
   cudaFree(ctx->staging);
+  cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
   cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
@@ -425,6 +455,13 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
     U.has_next = u + 1 < n;
     if (u > 0) U.r0_prev = und[u - 1].rb + und[u - 1].length * und[u - 1].lu - U.rb;  // src/beam.cc:35
     if (u + 1 < n) U.r0_next = und[u + 1].rb - U.rb - U.length * U.lu;                  // src/beam.cc:60
+    U.ct_f = (float)U.ct; U.st_f = (float)U.st; U.ku_f = (float)U.ku; U.b0_f = (float)U.b0; U.ul_f = (float)U.ul;
+    U.r0_prev_f = (float)U.r0_prev; U.r0_next_f = (float)U.r0_next;
+  }
+  if (ctx->precision == MITHRA_PRECISION_FP32) {
+    cudaFree(ctx->und_table);
+    ctx->und_table = nullptr;
+    if (n) CK(cudaMalloc(&ctx->und_table, (size_t)n * (ctx->g.N2 + 1) * 2 * sizeof(float)));
   }
   ctx->P.n_und = n;
   ctx->P.und0_dist = n ? und[0].dist : 0.0;
@@ -487,6 +524,20 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
     pw.tw_re = po.tw_re; pw.tw_im = po.tw_im; pw.fdt = po.fdt; pw.partial = po.partial;
     pw.rows = nullptr; pw.row_cap = 0;
     ctx->power.push_back(po);
+  }
+  // Planes whose E/B a power sample reads (cell k and k+1 of each owned plane).
+  {
+    std::vector<uint8_t> flags((size_t)g.N2, 0);
+    for (int o = 0; o < n; o++)
+      for (int k = 0; k < outs[o].N; k++)
+        if (outs[o].z[k] < g.zp1 && outs[o].z[k] >= g.zp0) {
+          double c;
+          modf((outs[o].z[k] - g.zmin) / g.dz, &c);
+          const int kc = (int)c;
+          if (kc >= 0 && kc < g.N2) flags[kc] = 1;
+          if (kc + 1 >= 0 && kc + 1 < g.N2) flags[kc + 1] = 1;
+        }
+    CK(cudaMemcpyAsync(ctx->plane_needed, flags.data(), flags.size(), cudaMemcpyHostToDevice, ctx->stream));
   }
   // Reset the row log.
   CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
@@ -588,9 +639,13 @@ int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
   { int r = mithra::staging(ctx, n * sizeof(float), (void**)&staging); if (r) return r; }
   float* dst[2] = {en, bn};
   const float* srcs[2] = {ctx->E, ctx->B};
+  const double* srcs64[2] = {ctx->E64, ctx->B64};
   for (int l = 0; l < 2; l++) {
     if (!dst[l]) continue;
-    k_soa_to_aos<float, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs[l], staging, 3);
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_soa_to_aos<double, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs64[l], staging, 3);
+    else
+      k_soa_to_aos<float, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs[l], staging, 3);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -616,6 +671,11 @@ int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
   ctx->st_host->n_particles = (long long)n;
   ctx->st_host->n_cross = 0;
   ctx->st_host->overflow = 0;
+  ctx->st_host->k_lo = 0;
+  ctx->st_host->k_hi = ctx->g.N2 - 1;
+  ctx->st_host->k_lo_next = 0x7fffffff;
+  ctx->st_host->k_hi_next = -0x7fffffff;
+  ctx->st_host->next_id = (long long)n;
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->particles_loaded = true;
@@ -690,7 +750,7 @@ int mithra_gpu_field_update(mithra_ctx* ctx) {
 
 int mithra_gpu_field_evaluate(mithra_ctx* ctx) {
   if (!ctx) return MITHRA_ERR_ARG;
-  int r = ctx->precision == MITHRA_PRECISION_FP32 ? fp32_eval_eb(ctx) : stage_eval_eb(ctx);
+  int r = ctx->precision == MITHRA_PRECISION_FP32 ? fp32_eval_eb(ctx, true) : stage_eval_eb(ctx, true);
   if (r) return r;
   return harvest_timers(ctx);
 }
@@ -753,10 +813,12 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
     return check_state(ctx);
   }
   for (int64_t s = 0; s < nsteps; s++) {
-    const int key = ctx->idx[0];
+    const int key = ctx->idx[0] + 3 * ctx->f32.parity;
     if (!ctx->graph[key]) {
       cudaGraph_t graph;
       const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
+      const int saved_parity = ctx->f32.parity;
+      const Fp32State saved_f32 = ctx->f32;
       CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
       ctx->launch_counter = 0;
       r = enqueue_step(ctx);
@@ -766,11 +828,15 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
       if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
       CK(cudaGraphInstantiate(&ctx->graph[key], graph, 0));
       CK(cudaGraphDestroy(graph));
-      // enqueue_step rotated the indices while recording; restore them for the launch below.
+      // enqueue_step rotated the indices (and swapped the particle buffer sets) while recording;
+      // restore them so that the launch below applies those changes exactly once.
       ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
+      ctx->f32 = saved_f32;
+      ctx->f32.parity = saved_parity;
     }
     CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
     rotate(ctx);
+    if (ctx->precision == MITHRA_PRECISION_FP32) fp32_after_step(ctx);
   }
   return check_state(ctx);
 }
@@ -802,11 +868,13 @@ int mithra_gpu_launches_per_step(mithra_ctx* ctx, int* n) {
     // Count by recording one step into a throw-away capture.
     cudaGraph_t graph;
     const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
+    const Fp32State saved_f32 = ctx->f32;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     ctx->launch_counter = 0;
     int r = enqueue_step(ctx);
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
     ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
+    ctx->f32 = saved_f32;
     if (r) return r;
     if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "capture: %s", cudaGetErrorString(ce));
     cudaGraphDestroy(graph);
@@ -835,7 +903,8 @@ int mithra_gpu_run_prelude(mithra_ctx* ctx) {
   if (!(t.time < 0.0)) return MITHRA_OK;
   // No field update happens before time zero, so the lazily evaluated E/B of the reference are
   // those of the initial potentials throughout the prelude.
-  if ((r = stage_eval_eb(ctx))) return r;
+  r = ctx->precision == MITHRA_PRECISION_FP32 ? fp32_eval_eb(ctx, true) : stage_eval_eb(ctx, true);
+  if (r) return r;
   const int ns = n_substeps(ctx);
   while (t.time < 0.0) {
     for (int s = 0; s < ns; s++)

@@ -20,9 +20,16 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
     const double ly = x * U.ct + y * U.st;
     double s_ly, c_ly;
     {
+      // cosh and sinh from one exponential; sinh by its Taylor series where e - 1/e cancels.
       const double kl = U.ku * ly;
-      s_ly = sinh(kl);
-      c_ly = cosh(kl);
+      const double ex = exp(kl), iex = 1.0 / ex;
+      c_ly = 0.5 * (ex + iex);
+      if (fabs(kl) < 0.1) {
+        const double a2 = kl * kl;
+        s_ly = kl * (1.0 + a2 * (1.0 / 6.0) * (1.0 + a2 * (1.0 / 20.0) * (1.0 + a2 * (1.0 / 42.0) * (1.0 + a2 * (1.0 / 72.0)))));
+      } else {
+        s_ly = 0.5 * (ex - iex);
+      }
     }
     double d1, bz;
     if (lz >= 0.0 && lz <= U.ul) {
@@ -58,8 +65,8 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
 // One Solver::bunchUpdate for every particle (src/solver.cpp:1424-1549).
 // save_rnm: also perform `rnm = rnp` first (src/solver.cpp:1311-1312).
 __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const UndDev* __restrict__ und,
-                                                   ParticlesDev<double> pt, const float* __restrict__ E,
-                                                   const float* __restrict__ B, StateDev* st, int save_rnm) {
+                                                   ParticlesDev<double> pt, const double* __restrict__ E,
+                                                   const double* __restrict__ B, StateDev* st, int save_rnm) {
   const long long n = st->n_particles;
   const double timeBunch = st->time_bunch;
   const long long cs = g.cstride;
@@ -81,9 +88,9 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         if (e == 1.0) {
           if (b1x && b1y && b1z) {
             double d1;
-            const double dxr = modf((x - g.xmin) / g.dx, &d1); const int i = (int)d1;
-            const double dyr = modf((y - g.ymin) / g.dy, &d1); const int j = (int)d1;
-            const double dzr = modf((z - g.zmin) / g.dz, &d1); const int k = (int)d1;
+            const double dxr = modf((x - g.xmin) * g.rdx, &d1); const int i = (int)d1;
+            const double dyr = modf((y - g.ymin) * g.rdy, &d1); const int j = (int)d1;
+            const double dzr = modf((z - g.zmin) * g.rdz, &d1); const int k = (int)d1;
             const long long m = node_index(g, k, i, j);
             const long long sI = g.P1, sK = g.plane;
             const double wx0 = 1.0 - dxr, wy0 = 1.0 - dyr, wz0 = 1.0 - dzr;
@@ -95,8 +102,8 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
               double se = et[c], sb = bt[c];
 #pragma unroll
               for (int q = 0; q < 8; q++) {
-                se += w[q] * (double)__ldg(E + c * cs + nd[q]);
-                sb += w[q] * (double)__ldg(B + c * cs + nd[q]);
+                se += w[q] * __ldg(E + c * cs + nd[q]);
+                sb += w[q] * __ldg(B + c * cs + nd[q]);
               }
               et[c] = se; bt[c] = sb;
             }
@@ -114,18 +121,19 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         double gx = pt.gx[p], gy = pt.gy[p], gz = pt.gz[p];
         const double mx = gx + P.r1 * et[0], my = gy + P.r1 * et[1], mz = gz + P.r1 * et[2];
         const double d1 = sqrt(1.0 + (mx * mx + my * my + mz * mz));
-        const double f = P.r2 / d1;
+        const double rd1 = 1.0 / d1;
+        const double f = P.r2 * rd1;
         const double px = f * (my * bt[2] - mz * bt[1]) + mx;
         const double py = f * (mz * bt[0] - mx * bt[2]) + my;
         const double pz = f * (mx * bt[1] - my * bt[0]) + mz;
         const double bt2 = bt[0] * bt[0] + bt[1] * bt[1] + bt[2] * bt[2];
-        const double s = 2.0 / (d1 / P.r2 + P.r2 / d1 * bt2);
+        const double s = 2.0 / (d1 * P.inv_r2 + f * bt2);
         gx = s * (py * bt[2] - pz * bt[1]) + mx + P.r1 * et[0];
         gy = s * (pz * bt[0] - px * bt[2]) + my + P.r1 * et[1];
         gz = s * (px * bt[1] - py * bt[0]) + mz + P.r1 * et[2];
         pt.gx[p] = gx; pt.gy[p] = gy; pt.gz[p] = gz;
         // Drift, src/solver.cpp:1538-1541.
-        const double gg = P.dtb / sqrt(1.0 + (gx * gx + gy * gy + gz * gz));
+        const double gg = P.dtb * rsqrt(1.0 + (gx * gx + gy * gy + gz * gz));
         const double drz = gg * gz;
         pt.x[p] = x + gg * gx; pt.y[p] = y + gg * gy; pt.z[p] = z + drz;
         zr += drz;
@@ -201,10 +209,17 @@ __global__ void __launch_bounds__(1024) k_substep_end(ParticlesDev<T> pt, StateD
 }
 
 // time_ += dt; ++nTime_ (src/solver.cpp:1396-1399).
+// Also hands the particle slab accumulated by this step's deposit to the next step.
 __global__ void k_advance_time(StateDev* st, double dt) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     st->time += dt;
     st->n_time += 1;
+    if (st->k_lo_next <= st->k_hi_next) {
+      st->k_lo = st->k_lo_next;
+      st->k_hi = st->k_hi_next;
+    }
+    st->k_lo_next = 0x7fffffff;
+    st->k_hi_next = -0x7fffffff;
   }
 }
 
@@ -240,14 +255,32 @@ __device__ __forceinline__ void deposit_half(double* J, long long cs, long long 
   }
 }
 
-__global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<double> pt, const StateDev* st,
+// Min/max of particle cells along z, reduced per warp and folded into the state with atomics.
+__device__ __forceinline__ void slab_update(StateDev* st, int kmin, int kmax) {
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
+  }
+  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
+    atomicMin(&st->k_lo_next, kmin);
+    atomicMax(&st->k_hi_next, kmax);
+  }
+}
+
+__global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<double> pt, StateDev* st,
                                                       double* J, double* rho) {
   const long long n = st->n_particles;
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
+  int kmin = 0x7fffffff, kmax = -0x7fffffff;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     if (pt.status[p] & 1) continue;
     const double rp0 = pt.x[p], rp1 = pt.y[p], rp2 = pt.z[p];
+    {
+      const int kc = (int)floor((rp2 - g.zmin) * g.rdz);
+      kmin = min(kmin, kc);
+      kmax = max(kmax, kc);
+    }
     const double rm0 = pt.mx[p], rm1 = pt.my[p], rm2 = pt.mz[p];
     const bool bp = (rp0 < g.xmax - g.dx && rp0 > g.xmin + g.dx && rp1 < g.ymax - g.dy &&
                      rp1 > g.ymin + g.dy && rp2 < g.zp1 && rp2 >= g.zp0);
@@ -255,23 +288,23 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
                      rm1 > g.ymin + g.dy && rm2 < g.zp1 && rm2 >= g.zp0);
     if (!(bp || bm)) continue;
     const double qh = pt.q[p] * 0.5;
-    const int ip = (int)floor((rp0 - g.xmin) / g.dx), jp = (int)floor((rp1 - g.ymin) / g.dy),
-              kp = (int)floor((rp2 - g.zmin) / g.dz);
-    const int im = (int)floor((rm0 - g.xmin) / g.dx), jm = (int)floor((rm1 - g.ymin) / g.dy),
-              km = (int)floor((rm2 - g.zmin) / g.dz);
+    const int ip = (int)floor((rp0 - g.xmin) * g.rdx), jp = (int)floor((rp1 - g.ymin) * g.rdy),
+              kp = (int)floor((rp2 - g.zmin) * g.rdz);
+    const int im = (int)floor((rm0 - g.xmin) * g.rdx), jm = (int)floor((rm1 - g.ymin) * g.rdy),
+              km = (int)floor((rm2 - g.zmin) * g.rdz);
     const double r0 = fmin(min(im, ip) * g.dx + g.dx + g.xmin, fmax(max(im, ip) * g.dx + g.xmin, 0.5 * (rm0 + rp0)));
     const double r1 = fmin(min(jm, jp) * g.dy + g.dy + g.ymin, fmax(max(jm, jp) * g.dy + g.ymin, 0.5 * (rm1 + rp1)));
     const double r2 = fmin(min(km, kp) * g.dz + g.dz + g.zmin, fmax(max(km, kp) * g.dz + g.zmin, 0.5 * (rm2 + rp2)));
     double c;
     if (bp) {
       const long long m = node_index(g, kp, ip, jp);
-      const double dxp = modf((0.5 * (rp0 + r0) - g.xmin) / g.dx, &c);
-      const double dyp = modf((0.5 * (rp1 + r1) - g.ymin) / g.dy, &c);
-      const double dzp = modf((0.5 * (rp2 + r2) - g.zmin) / g.dz, &c);
+      const double dxp = modf((0.5 * (rp0 + r0) - g.xmin) * g.rdx, &c);
+      const double dyp = modf((0.5 * (rp1 + r1) - g.ymin) * g.rdy, &c);
+      const double dzp = modf((0.5 * (rp2 + r2) - g.zmin) * g.rdz, &c);
       deposit_half(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
       if (rho) {
-        const double fx = modf((rp0 - g.xmin) / g.dx, &c), fy = modf((rp1 - g.ymin) / g.dy, &c),
-                     fz = modf((rp2 - g.zmin) / g.dz, &c);
+        const double fx = modf((rp0 - g.xmin) * g.rdx, &c), fy = modf((rp1 - g.ymin) * g.rdy, &c),
+                     fz = modf((rp2 - g.zmin) * g.rdz, &c);
         const double q = pt.q[p];
         const double x1 = 1.0 - fx, y1 = 1.0 - fy, z1 = 1.0 - fz;
         atomicAdd(rho + m, q * x1 * y1 * z1);
@@ -286,12 +319,13 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
     }
     if (bm) {
       const long long m = node_index(g, km, im, jm);
-      const double dxm = modf((0.5 * (rm0 + r0) - g.xmin) / g.dx, &c);
-      const double dym = modf((0.5 * (rm1 + r1) - g.ymin) / g.dy, &c);
-      const double dzm = modf((0.5 * (rm2 + r2) - g.zmin) / g.dz, &c);
+      const double dxm = modf((0.5 * (rm0 + r0) - g.xmin) * g.rdx, &c);
+      const double dym = modf((0.5 * (rm1 + r1) - g.ymin) * g.rdy, &c);
+      const double dzm = modf((0.5 * (rm2 + r2) - g.zmin) * g.rdz, &c);
       deposit_half(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
     }
   }
+  slab_update(st, kmin, kmax);
 }
 
 // rnm = rnp (src/solver.cpp:1311-1312) as a stand-alone stage.

@@ -9,9 +9,9 @@
 
 namespace mithra {
 
-template <int BLOCK>
-__global__ void __launch_bounds__(BLOCK) k_power_sample(GridDev g, PowerDev pw, const float* __restrict__ E,
-                                                        const float* __restrict__ B, const StateDev* st) {
+template <int BLOCK, typename TE>
+__global__ void __launch_bounds__(BLOCK) k_power_sample(GridDev g, PowerDev pw, const TE* __restrict__ E,
+                                                        const TE* __restrict__ B, const StateDev* st) {
   extern __shared__ double s_red[];  // Nl * BLOCK
   const int plane = blockIdx.x / pw.blocks_per_plane;
   const int bip = blockIdx.x % pw.blocks_per_plane;

@@ -1,0 +1,324 @@
+// Tile sort and tiled current deposit of the mixed form.
+//
+// Every field step the particles are counting-sorted by deposit tile (TX x TY x TZ cells).  The
+// deposit then gives one block to each tile: the block accumulates the zigzag currents of its
+// particles in a shared-memory copy of the tile's nodes (with a one-cell halo on each side, since
+// the previous position may lie in a neighbouring cell) and adds that copy to J once.  Compared
+// with one global atomic per particle contribution (48 per particle) this removes most of the
+// traffic to the L2 atomic units; the sort also makes the next push read E/B with locality.
+#pragma once
+#include "device_common.cuh"
+#include "fp32_kernels.cuh"
+
+namespace mithra {
+
+constexpr int TX = 8, TY = 8, TZ = 8;                          // cells per tile (i, j, k)
+constexpr int HX = TX + 3, HY = TY + 3, HZ = TZ + 3;           // nodes per tile incl. halo
+constexpr int TILE_NODES = HX * HY * HZ;
+
+struct TileGrid {
+  int ntx, nty, ntz;   // tiles along i, j, k
+  int n_tiles;         // ntx * nty * ntz
+  int bin_outside;     // particles outside the tiled cell range
+  int bin_erased;      // erased particles (dropped by the sort)
+  int n_bins;          // n_tiles + 2
+};
+
+__device__ __forceinline__ int tile_key(const TileGrid& T, int i, int j, int k) {
+  if (i < 0 || j < 0 || k < 0) return T.bin_outside;
+  const int ti = i / TX, tj = j / TY, tk = k / TZ;
+  if (ti >= T.ntx || tj >= T.nty || tk >= T.ntz) return T.bin_outside;
+  return (tk * T.nty + tj) * T.ntx + ti;
+}
+
+// Pass 1: bin of every particle and its rank inside the bin.
+// Lanes of a warp that share a bin take consecutive ranks from one atomic (__match_any_sync), so
+// after the first sort, when neighbouring particles share tiles, the bin counters see about one
+// atomic per warp and the scatter below writes runs of consecutive slots.
+__global__ void __launch_bounds__(256) k_tile_hist(TileGrid T, ParticlesF32 pt, const StateDev* st, int* counts,
+                                                   int* key, int* rank) {
+  const long long n = st->n_particles;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long n_iter = (n + stride - 1) / stride;
+  const int lane = threadIdx.x & 31;
+  for (long long it = 0; it < n_iter; it++) {
+    const long long p = it * stride + blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = p < n;
+    int b = -1;
+    if (live) {
+      if (pt.status[p] & 1) {
+        b = T.bin_erased;
+      } else {
+        int i, j, k;
+        unpack_cell(pt.cell[p], i, j, k);
+        b = tile_key(T, i, j, k);
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (live && lane == leader) base = atomicAdd(counts + b, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    if (live) {
+      key[p] = b;
+      rank[p] = base + __popc(peers & ((1u << lane) - 1u));
+    }
+  }
+}
+
+// Pass 2: exclusive scan of the bin counts in three short launches: per-1024-bin block scans,
+// a scan of the block totals, and the add-back (which also clears the counts for the next sort
+// and sets the particle count to exclude erased particles, kept in the last bin).
+__device__ __forceinline__ int block_exclusive_scan_1024(int v, int* s_warp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;  // inclusive prefix of warp sums
+  }
+  __syncthreads();
+  const int before = (warp ? s_warp[warp - 1] : 0) + x - v;
+  *total = s_warp[(blockDim.x >> 5) - 1];
+  return before;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int* counts, int* offsets, int* block_sums, int n) {
+  __shared__ int s_warp[32];
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int v = b < n ? counts[b] : 0;
+  int total;
+  const int ex = block_exclusive_scan_1024(v, s_warp, &total);
+  if (b < n) offsets[b] = ex;
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_totals(int* block_sums, int nblocks) {
+  __shared__ int s_warp[32];
+  const int v = threadIdx.x < nblocks ? block_sums[threadIdx.x] : 0;
+  int total;
+  const int ex = block_exclusive_scan_1024(v, s_warp, &total);
+  if (threadIdx.x < nblocks) block_sums[threadIdx.x] = ex;
+  if (threadIdx.x == 0) block_sums[1024] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_add(int* counts, int* offsets, const int* block_sums, int n, int nblocks,
+                                                   StateDev* st) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < n) {
+    offsets[b] += block_sums[blockIdx.x];
+    counts[b] = 0;
+  }
+  if (b == n - 1) {
+    offsets[n] = block_sums[1024];
+    st->n_particles = offsets[n - 1];  // the last bin holds the erased particles
+  }
+}
+
+// Pass 3: scatter every particle to its sorted slot in the other buffer set.
+__global__ void __launch_bounds__(256) k_tile_scatter(ParticlesF32 src, ParticlesF32 dst, const int* key,
+                                                      const int* rank, const int* offsets, int n_bins) {
+  const long long n_in = offsets[n_bins];  // every particle of the unsorted set, erased ones included
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n_in;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long d = (long long)offsets[key[p]] + rank[p];
+    dst.cell[d] = src.cell[p];
+    dst.fx[d] = src.fx[p]; dst.fy[d] = src.fy[p]; dst.fz[d] = src.fz[p];
+    dst.gx[d] = src.gx[p]; dst.gy[d] = src.gy[p]; dst.gz[d] = src.gz[p];
+    dst.mcell[d] = src.mcell[p];
+    dst.mfx[d] = src.mfx[p]; dst.mfy[d] = src.mfy[p]; dst.mfz[d] = src.mfz[p];
+    dst.q[d] = src.q[p]; dst.e[d] = src.e[p]; dst.status[d] = src.status[p]; dst.cross[d] = 0;
+    dst.id[d] = src.id[p];
+  }
+}
+
+// Zigzag contribution of one half segment into the shared tile (falls back to global atomics for
+// nodes outside the tile, which happens only for particles that left their tile's halo).
+__device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, long long plane, int P1, int i0, int j0,
+                                          int k0, int ic, int jc, int kc, float qh, float ax, float ay, float az,
+                                          float jx, float jy, float jz) {
+  const float x1 = 1.0f - ax, x2 = ax, y1 = 1.0f - ay, y2 = ay, z1 = 1.0f - az, z2 = az;
+  const float qx = qh * jx, qy = qh * jy, qz = qh * jz;
+  const int li = ic - i0, lj = jc - j0, lk = kc - k0;  // local node coordinates of the cell origin
+  const bool in_tile = li >= 0 && lj >= 0 && lk >= 0 && li + 1 < HX && lj + 1 < HY && lk + 1 < HZ;
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int di = (q >> 0) & 1, dj = (q >> 1) & 1, dk = (q >> 2) & 1;
+    // weights of src/fdtd.cpp:105-130 for node (i+di, j+dj, k+dk)
+    const float wx = (dj ? y2 : y1) * (dk ? z2 : z1);
+    const float wy = (di ? x2 : x1) * (dk ? z2 : z1);
+    const float wz = (di ? x2 : x1) * (dj ? y2 : y1);
+    if (in_tile) {
+      const int s = ((lk + dk) * HY + (lj + dj)) * HX + (li + di);
+      atomicAdd(sJ + s, wx * qx);
+      atomicAdd(sJ + TILE_NODES + s, wy * qy);
+      atomicAdd(sJ + 2 * TILE_NODES + s, wz * qz);
+    } else {
+      const long long m = (long long)(kc + dk) * plane + (long long)(ic + di) * P1 + (jc + dj);
+      atomicAdd(J + m, wx * qx);
+      atomicAdd(J + cs + m, wy * qy);
+      atomicAdd(J + 2 * cs + m, wz * qz);
+    }
+  }
+}
+
+// One block per tile bin (plus one for the particles outside the tiled range).  Same arithmetic
+// as k_deposit_f32; rho (space charge) is added straight to global memory.
+__global__ void __launch_bounds__(256) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
+                                                       StateDev* st, float* J, float* rho, long long cs,
+                                                       long long plane, int P1) {
+  extern __shared__ float sJ[];  // 3 * TILE_NODES
+  const int b = blockIdx.x;
+  const int beg = offsets[b], end = offsets[b + 1];
+  if (beg == end) return;
+  const bool tiled = b < T.n_tiles;
+  int i0 = 0, j0 = 0, k0 = 0;
+  if (tiled) {
+    const int ti = b % T.ntx, tj = (b / T.ntx) % T.nty, tk = b / (T.ntx * T.nty);
+    i0 = ti * TX - 1; j0 = tj * TY - 1; k0 = tk * TZ - 1;  // halo of one cell below
+    for (int s = threadIdx.x; s < 3 * TILE_NODES; s += blockDim.x) sJ[s] = 0.0f;
+    __syncthreads();
+  }
+  int kmin = 0x7fffffff, kmax = -0x7fffffff;
+  const long long sI = P1, sK = plane;
+  for (int p = beg + threadIdx.x; p < end; p += blockDim.x) {
+    int ip, jp, kp, im, jm, km;
+    unpack_cell(pt.cell[p], ip, jp, kp);
+    unpack_cell(pt.mcell[p], im, jm, km);
+    kmin = min(kmin, kp);
+    kmax = max(kmax, kp);
+    const float fxp = pt.fx[p], fyp = pt.fy[p], fzp = pt.fz[p];
+    const float fxm = pt.mfx[p], fym = pt.mfy[p], fzm = pt.mfz[p];
+    const bool bp = inside_f32(D, ip, jp, kp, fxp, fyp);
+    const bool bm = inside_f32(D, im, jm, km, fxm, fym);
+    if (!(bp || bm)) continue;
+    int bx, by, bz;
+    float rxm, rxp, rym, ryp, rzm, rzp;
+    const float rx = relay_axis(im, ip, fxm, fxp, &bx, &rxm, &rxp);
+    const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
+    const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
+    const float qh = 0.5f * pt.q[p];
+    float* sj = tiled ? sJ : nullptr;
+    if (bp) {
+      const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
+                  az = 0.5f * (rzp + rz) - (float)(kp - bz);
+      if (sj)
+        tile_half(sj, J, cs, plane, P1, i0, j0, k0, ip, jp, kp, qh, ax, ay, az, (rxp - rx) * D.dx, (ryp - ry) * D.dy,
+                  (rzp - rz) * D.dz);
+      else
+        deposit_half_f32(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, ax, ay, az,
+                         (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+      if (rho) {
+        const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
+        const float q = pt.q[p];
+        const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
+        atomicAdd(rho + m, q * x1 * y1 * z1);
+        atomicAdd(rho + m + sI, q * fxp * y1 * z1);
+        atomicAdd(rho + m + 1, q * x1 * fyp * z1);
+        atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
+        atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
+        atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
+        atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
+        atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
+      }
+    }
+    if (bm) {
+      const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
+                  az = 0.5f * (rzm + rz) - (float)(km - bz);
+      if (sj)
+        tile_half(sj, J, cs, plane, P1, i0, j0, k0, im, jm, km, qh, ax, ay, az, (rx - rxm) * D.dx, (ry - rym) * D.dy,
+                  (rz - rzm) * D.dz);
+      else
+        deposit_half_f32(J, cs, (long long)km * plane + (long long)im * P1 + jm, sI, sK, qh, ax, ay, az,
+                         (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
+  }
+  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
+    atomicMin(&st->k_lo_next, kmin);
+    atomicMax(&st->k_hi_next, kmax);
+  }
+  if (!tiled) return;
+  __syncthreads();
+  // Flush: every non-zero tile node is added to J once.
+  for (int s = threadIdx.x; s < TILE_NODES; s += blockDim.x) {
+    const int li = s % HX, lj = (s / HX) % HY, lk = s / (HX * HY);
+    const int gi = i0 + li, gj = j0 + lj, gk = k0 + lk;
+    if (gi < 0 || gj < 0 || gk < 0 || gi >= D.N0 || gj >= D.N1 || gk >= D.N2) continue;
+    const long long m = (long long)gk * plane + (long long)gi * P1 + gj;
+    const float vx = sJ[s], vy = sJ[TILE_NODES + s], vz = sJ[2 * TILE_NODES + s];
+    if (vx != 0.0f) atomicAdd(J + m, vx);
+    if (vy != 0.0f) atomicAdd(J + cs + m, vy);
+    if (vz != 0.0f) atomicAdd(J + 2 * cs + m, vz);
+  }
+}
+
+// Download in creation order: every live particle is written to row `id` of a scratch table with
+// a valid flag; a one-block pass then compacts the valid rows in id order.
+__global__ void __launch_bounds__(256) k_f32_to_rows_by_id(ParticlesF32 pt, const StateDev* st, double* rows,
+                                                           uint8_t* valid, long long id_cap, CellMap M) {
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
+       p += (long long)gridDim.x * blockDim.x) {
+    if (pt.status[p] & 1) continue;
+    const long long id = pt.id[p];
+    if (id < 0 || id >= id_cap) continue;
+    double* r = rows + 11 * id;
+    int i, j, k;
+    unpack_cell(pt.cell[p], i, j, k);
+    r[0] = pt.q[p];
+    r[1] = M.xmin + ((double)i + (double)pt.fx[p]) * M.dx;
+    r[2] = M.ymin + ((double)j + (double)pt.fy[p]) * M.dy;
+    r[3] = M.zmin + ((double)k + (double)pt.fz[p]) * M.dz;
+    unpack_cell(pt.mcell[p], i, j, k);
+    r[4] = M.xmin + ((double)i + (double)pt.mfx[p]) * M.dx;
+    r[5] = M.ymin + ((double)j + (double)pt.mfy[p]) * M.dy;
+    r[6] = M.zmin + ((double)k + (double)pt.mfz[p]) * M.dz;
+    r[7] = pt.gx[p]; r[8] = pt.gy[p]; r[9] = pt.gz[p];
+    r[10] = pt.e[p] ? 1.0 : 0.0;
+    valid[id] = 1;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_compact_rows(const double* rows, const uint8_t* valid, long long id_cap,
+                                                       double* rec, long long cap, long long* n_out) {
+  __shared__ int s_warp[32];
+  __shared__ long long s_base;
+  if (threadIdx.x == 0) s_base = 0;
+  __syncthreads();
+  for (long long c0 = 0; c0 < id_cap; c0 += blockDim.x) {
+    const long long p = c0 + threadIdx.x;
+    const int take = (p < id_cap) && valid[p];
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      if (w < warp) before += s_warp[w];
+      total += s_warp[w];
+    }
+    before += __popc(bal & ((1u << lane) - 1u));
+    const long long d = s_base + before;
+    if (take && d < cap)
+      for (int c = 0; c < 11; c++) rec[11 * d + c] = rows[11 * p + c];
+    __syncthreads();
+    if (threadIdx.x == 0) s_base += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *n_out = s_base;
+}
+
+}  // namespace mithra

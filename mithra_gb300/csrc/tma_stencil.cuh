@@ -1,0 +1,187 @@
+// Interior potential update of the mixed form with TMA-staged z-slabs.
+//
+// Each CTA owns a TJ x TI tile of (j, i) for one component and marches along k over a slab of
+// KS planes.  Planes of A^n (with a one-node halo), A^{n-1} and J are brought into shared memory
+// by cp.async.bulk.tensor under mbarriers: a ring of four A^n planes (k-1, k, k+1 in use, k+2 in
+// flight) and two of A^{n-1} and J.  One thread per tile column computes A^{n+1} for the plane
+// from shared memory (FD: 7 points; NSFD: the 15-point stencil of src/database.cpp:44-72) and
+// stores it with coalesced row writes.  Every byte of A^n, A^{n-1}, J is read from HBM once per
+// slab (plus the thin halos), which is what the 48 B/node roofline assumes.
+//
+// Waits are bounded: a CTA whose barrier does not complete within the iteration limit records
+// the failure in an error word and leaves after a bounded drain, instead of spinning forever.
+#pragma once
+#include <cuda.h>
+
+#include "device_common.cuh"
+
+namespace mithra {
+
+constexpr int TMA_TJ = 32;               // tile width along j (threads along x)
+constexpr int TMA_TI = 16;               // tile height along i
+constexpr int TMA_BW = TMA_TJ + 4;       // box width: j0-1 .. j0+TJ, rounded up to 16 bytes
+constexpr int TMA_BH = TMA_TI + 2;       // A^n box height incl. halo rows
+constexpr int TMA_KS = 64;               // planes per slab
+constexpr unsigned TMA_SPIN_LIMIT = 20000000u;
+
+struct TmaStencilArgs {
+  float* np1;        // A^{n+1} (holds J on entry), SoA with cstride between components
+  int N0, N1, N2, P1;
+  long long plane, cstride;
+  float a0, a1, a2, a3, asrc, al, be;
+  int* error;        // set to 1 when a barrier wait gives up
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+
+// Bounded wait on phase `parity`; returns false when the limit is reached.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, unsigned limit) {
+  for (unsigned it = 0; it < limit; it++) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 4D tiled load (x = j, y = i, z = k, w = component) into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int x, int y, int z, int w,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+      ::"r"(smem_addr(dst)), "l"(map), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_addr(bar))
+      : "memory");
+}
+
+constexpr int TMA_D = 3;                    // plane groups in flight ahead of the one computed
+constexpr int TMA_RAN = TMA_D + 3;          // A^n ring: k-1, k, k+1 in use plus D ahead
+constexpr int TMA_RC = TMA_D + 1;           // A^{n-1} / J ring and barriers
+// Shared-memory slots of bulk-tensor copies start on 128-byte boundaries: slot strides are
+// rounded up to multiples of 128 bytes and the dynamic base is aligned at run time.
+constexpr int TMA_SLOT_AN = ((TMA_BW * TMA_BH * 4 + 127) / 128) * 128;   // bytes per A^n slot
+constexpr int TMA_SLOT_C = ((TMA_BW * TMA_TI * 4 + 127) / 128) * 128;    // bytes per A^{n-1}/J slot
+constexpr int TMA_OFF_AM = TMA_RAN * TMA_SLOT_AN;
+constexpr int TMA_OFF_J = TMA_OFF_AM + TMA_RC * TMA_SLOT_C;
+constexpr int TMA_SMEM_USED = TMA_OFF_J + TMA_RC * TMA_SLOT_C;
+
+template <bool NSFD>
+__global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
+    const __grid_constant__ CUtensorMap map_an,    // A^n, box TMA_BW x TMA_BH
+    const __grid_constant__ CUtensorMap map_anm1,  // A^{n-1}, box TMA_BW x TMA_TI
+    const __grid_constant__ CUtensorMap map_j,     // J (the A^{n+1} buffer), box TMA_BW x TMA_TI
+    TmaStencilArgs a) {
+  extern __shared__ __align__(128) unsigned char s_raw[];
+  unsigned char* s_base = s_raw + ((128u - (smem_addr(s_raw) & 127u)) & 127u);
+  auto an_slot = [&](int r) { return reinterpret_cast<float(*)[TMA_BW]>(s_base + r * TMA_SLOT_AN); };
+  auto am_slot = [&](int r) { return reinterpret_cast<float(*)[TMA_BW]>(s_base + TMA_OFF_AM + r * TMA_SLOT_C); };
+  auto j_slot = [&](int r) { return reinterpret_cast<float(*)[TMA_BW]>(s_base + TMA_OFF_J + r * TMA_SLOT_C); };
+  __shared__ __align__(8) unsigned long long bar[TMA_RC + 1];  // one per group slot; last: prologue
+  __shared__ int s_abort;
+
+  const int tx = threadIdx.x % TMA_TJ, ty = threadIdx.x / TMA_TJ;
+  const int nslab = (a.N2 - 2 + TMA_KS - 1) / TMA_KS;
+  const int comp = blockIdx.z / nslab, slab = blockIdx.z % nslab;
+  const int jb = blockIdx.x * TMA_TJ;   // box origin along j (= j0 - 1, 16-byte aligned)
+  const int ib = blockIdx.y * TMA_TI;   // A^n box origin along i (= i0 - 1)
+  const int k_first = 1 + slab * TMA_KS;
+  const int k_last = min(a.N2 - 2, k_first + TMA_KS - 1);
+  const int j = jb + 1 + tx, i = ib + 1 + ty;
+  const unsigned bytes_an = TMA_BW * TMA_BH * 4, bytes_c = TMA_BW * TMA_TI * 4;
+
+  // Issues a copy only into a 128-byte aligned slot; anything else is recorded as an error and
+  // skipped (the wait on its barrier then times out and the CTA leaves).
+  auto aligned = [&](const void* d) { return (smem_addr(d) & 127u) == 0u; };
+  auto issue_group = [&](int kk) {  // A^n(kk+1), A^{n-1}(kk), J(kk) on barrier kk % RC
+    unsigned long long* b = &bar[kk % TMA_RC];
+    float* d0 = &an_slot((kk + 1) % TMA_RAN)[0][0];
+    float* d1 = &am_slot(kk % TMA_RC)[0][0];
+    float* d2 = &j_slot(kk % TMA_RC)[0][0];
+    if (!(aligned(d0) && aligned(d1) && aligned(d2))) {
+      atomicExch(a.error, 2);
+      s_abort = 1;
+      return;
+    }
+    mbar_expect_tx(b, bytes_an + 2 * bytes_c);
+    tma_load_4d(d0, &map_an, jb, ib, kk + 1, comp, b);
+    tma_load_4d(d1, &map_anm1, jb, ib + 1, kk, comp, b);
+    tma_load_4d(d2, &map_j, jb, ib + 1, kk, comp, b);
+  };
+
+  if (threadIdx.x == 0) {
+    for (int b = 0; b <= TMA_RC; b++) mbar_init(&bar[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+    float* p0 = &an_slot((k_first - 1) % TMA_RAN)[0][0];
+    float* p1 = &an_slot(k_first % TMA_RAN)[0][0];
+    if (aligned(p0) && aligned(p1)) {
+      mbar_expect_tx(&bar[TMA_RC], 2 * bytes_an);
+      tma_load_4d(p0, &map_an, jb, ib, k_first - 1, comp, &bar[TMA_RC]);
+      tma_load_4d(p1, &map_an, jb, ib, k_first, comp, &bar[TMA_RC]);
+      for (int kk = k_first; kk < k_first + TMA_D && kk <= k_last && !s_abort; kk++) issue_group(kk);
+    } else {
+      atomicExch(a.error, 2);
+      s_abort = 1;
+    }
+  }
+  __syncthreads();
+  if (s_abort) return;  // nothing was issued, or copies are in flight only for earlier slots
+  unsigned phases = 0u;  // bit b: parity of the next wait on bar[b]
+  if (!mbar_wait(&bar[TMA_RC], 0, TMA_SPIN_LIMIT)) s_abort = 1;
+
+  float* out = a.np1 + (long long)comp * a.cstride;
+  for (int k = k_first; k <= k_last; k++) {
+    const int g = k % TMA_RC;
+    if (threadIdx.x == 0 && k + TMA_D <= k_last && !s_abort) issue_group(k + TMA_D);  // reuses the slots of plane k-1
+    if (!mbar_wait(&bar[g], (phases >> g) & 1u, TMA_SPIN_LIMIT)) s_abort = 1;
+    phases ^= 1u << g;
+    __syncthreads();
+    if (s_abort) break;
+    if (i <= a.N0 - 2 && j <= a.N1 - 2) {
+      const float(*c)[TMA_BW] = an_slot(k % TMA_RAN);
+      const float(*m)[TMA_BW] = an_slot((k - 1) % TMA_RAN);
+      const float(*p)[TMA_BW] = an_slot((k + 1) % TMA_RAN);
+      const float(*am)[TMA_BW] = am_slot(g);
+      const float(*jj)[TMA_BW] = j_slot(g);
+      const int y = ty + 1, x = tx + 1;
+      const float v = c[y][x];
+      float r;
+      if (NSFD) {
+        const float sx = c[y + 1][x] + c[y - 1][x] + a.be * (p[y + 1][x] + m[y + 1][x] + p[y - 1][x] + m[y - 1][x]);
+        const float sy = c[y][x + 1] + c[y][x - 1] + a.be * (p[y][x + 1] + m[y][x + 1] + p[y][x - 1] + m[y][x - 1]);
+        r = a.a0 * v - am[ty][x] + a.al * (a.a1 * sx + a.a2 * sy) + a.a3 * (p[y][x] + m[y][x]) +
+            a.asrc * jj[ty][x];
+      } else {
+        r = a.a0 * v - am[ty][x] + a.a1 * (c[y + 1][x] + c[y - 1][x]) + a.a2 * (c[y][x + 1] + c[y][x - 1]) +
+            a.a3 * (p[y][x] + m[y][x]) + a.asrc * jj[ty][x];
+      }
+      out[(long long)k * a.plane + (long long)i * a.P1 + j] = r;
+    }
+    __syncthreads();
+  }
+  if (s_abort) {
+    if (threadIdx.x == 0) {
+      atomicExch(a.error, 1);
+      // Bounded drain of copies still in flight into this CTA's shared memory.
+      for (int b = 0; b < TMA_RC; b++) mbar_wait(&bar[b], (phases >> b) & 1u, TMA_SPIN_LIMIT);
+    }
+    __syncthreads();
+  }
+}
+
+constexpr size_t kTmaStencilSmem = (size_t)TMA_SMEM_USED + 128;  // + room to align the base
+
+}  // namespace mithra

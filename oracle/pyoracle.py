@@ -222,15 +222,20 @@ class OracleRun:
     """One single-rank FdTd march on the CPU, state initialised from a meta dict and arrays."""
 
     def __init__(self, meta: dict, an, anm1, anp1, particles, solver: int, order: int,
-                 cap_factor: float = 2.0):
+                 cap_factor: float = 2.0, fn=None, fnm1=None, fnp1=None):
         self.m = dict(meta)
-        self.f = field_params(meta, solver, order)
+        self.sc = fn is not None
+        self.f = field_params(meta, solver, order, 1 if self.sc else 0)
         self.p = push_params(meta)
         self.d = deposit_params(meta)
         nodes = int(meta["N0"]) * int(meta["N1"]) * int(meta["np"])
         self.an = np.ascontiguousarray(an, dtype=np.float64).reshape(nodes * 3).copy()
         self.anm1 = np.ascontiguousarray(anm1, dtype=np.float64).reshape(nodes * 3).copy()
         self.anp1 = np.ascontiguousarray(anp1, dtype=np.float64).reshape(nodes * 3).copy()
+        if self.sc:
+            self.fn = np.ascontiguousarray(fn, dtype=np.float64).reshape(nodes).copy()
+            self.fnm1 = np.ascontiguousarray(fnm1, dtype=np.float64).reshape(nodes).copy()
+            self.fnp1 = np.ascontiguousarray(fnp1, dtype=np.float64).reshape(nodes).copy()
         self.en = np.zeros(nodes * 3, dtype=np.float32)
         self.bn = np.zeros(nodes * 3, dtype=np.float32)
         parts = np.ascontiguousarray(particles, dtype=np.float64).reshape(-1, 11)
@@ -254,9 +259,12 @@ class OracleRun:
 
     def field_update(self):
         lib().mo_field_update(C.byref(self.f), dptr(self.anp1), dptr(self.an), dptr(self.anm1))
+        if self.sc:
+            lib().mo_scalar_update(C.byref(self.f), dptr(self.fnp1), dptr(self.fn), dptr(self.fnm1))
 
     def eval_eb(self):
-        lib().mo_eval_eb(C.byref(self.f), dptr(self.anp1), dptr(self.an), None, fptr(self.en), fptr(self.bn))
+        lib().mo_eval_eb(C.byref(self.f), dptr(self.anp1), dptr(self.an), dptr(self.fn) if self.sc else None,
+                         fptr(self.en), fptr(self.bn))
 
     def push(self):
         nt = C.c_long(0)
@@ -272,7 +280,10 @@ class OracleRun:
 
     def deposit(self):
         self.anp1[:] = 0.0
-        lib().mo_deposit_current(C.byref(self.d), dptr(self.rec), self.n, dptr(self.anp1), None)
+        if self.sc:
+            self.fnp1[:] = 0.0
+        lib().mo_deposit_current(C.byref(self.d), dptr(self.rec), self.n, dptr(self.anp1),
+                                 dptr(self.fnp1) if self.sc else None)
 
     def step(self):
         """One field step, src/solver.cpp:1300-1399 (diagnostic file writers omitted)."""
@@ -292,6 +303,8 @@ class OracleRun:
             zl = m["gamma"] * (self.power.z + m["beta"] * m["c0"] * (self.time_bunch + m["dt_shift"]))
             self.power_rows.append((zl, pg))
         self.anm1, self.an, self.anp1 = self.an, self.anp1, self.anm1
+        if self.sc:
+            self.fnm1, self.fn, self.fnp1 = self.fn, self.fnp1, self.fnm1
         self.deposit()
         self.erase()
         self.time += self.dt

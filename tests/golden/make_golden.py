@@ -47,14 +47,17 @@ def fixtures_for(harness, jobname, tag, with_kats=True):
         r = os.path.join(tmp, "run")
         ld = lambda s, n: np.fromfile(os.path.join(r, "step%d" % s, n + ".bin"))
         keys, vals = meta_arrays(os.path.join(r, "step0", "meta.txt"))
+        sc = os.path.exists(os.path.join(r, "step0", "fn.bin"))
+        extra0 = dict(fn=ld(0, "fn"), fnm1=ld(0, "fnm1"), fnp1=ld(0, "fnp1")) if sc else {}
         np.savez_compressed(os.path.join(dst, "init.npz"), meta_keys=keys, meta_vals=vals,
                             particles=ld(0, "particles").reshape(-1, 11), an=ld(0, "an"), anm1=ld(0, "anm1"),
-                            anp1=ld(0, "anp1"))
+                            anp1=ld(0, "anp1"), **extra0)
+        extra = dict(fn12=ld(12, "fn"), fnm1_12=ld(12, "fnm1"), fnp1_12=ld(12, "fnp1")) if sc else {}
         np.savez_compressed(os.path.join(dst, "run.npz"),
                             an6=ld(6, "an"), anp1_6=ld(6, "anp1"), particles6=ld(6, "particles").reshape(-1, 11),
                             an12=ld(12, "an"), anm1_12=ld(12, "anm1"), anp1_12=ld(12, "anp1"),
                             particles12=ld(12, "particles").reshape(-1, 11),
-                            power=np.fromfile(os.path.join(r, "power.bin")).reshape(12, -1))
+                            power=np.fromfile(os.path.join(r, "power.bin")).reshape(12, -1), **extra)
         if not with_kats:
             return
         meta = pyoracle.read_meta(os.path.join(r, "step0", "meta.txt"))
@@ -117,6 +120,7 @@ def main():
     harness = os.path.abspath(harness)
     fixtures_for(harness, "kat-small.job", "kat-small-fd")
     fixtures_for(harness, "kat-small-nsfd.job", "kat-small-nsfd")
+    fixtures_for(harness, "kat-small-sc.job", "kat-small-sc", with_kats=False)
     print("golden vectors written to", OUT)
 
 

@@ -1,0 +1,93 @@
+"""The mixed-precision form against the FP64 form and the reference's golden vectors.
+
+The mixed form stores fields, currents and particle coordinates in FP32 (particle position as
+integer cell + FP32 offset) and keeps FP64 for the undulator phase and the time state.  Its
+errors against FP64 are stated per quantity; the bounds below are the ones the tests enforce."""
+import numpy as np
+import pytest
+
+import mithra_gb300 as mg
+from tests._golden import TAGS, load, meta
+from tests.conftest import job, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FIELD_STAGE_RTOL = 2e-6   # one field update in FP32, relative to max |A|
+PUSH_RTOL = 2e-5          # one push: E = (A^n - A^{n+1})/dt loses digits to cancellation in FP32
+DEPOSIT_RTOL = 5e-6       # relative L2 of J
+PSAT_RTOL = 0.01          # saturated (peak) radiated power of a full march vs the FP64 form
+
+
+def interior_mask(m):
+    N0, N1, N2 = int(m["N0"]), int(m["N1"]), int(m["np"])
+    sel = np.zeros((N2, N0, N1), dtype=bool)
+    sel[:, 1:-1, 1:-1] = True
+    return np.repeat(sel.ravel(), 3)
+
+
+def scaled_err(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - np.asarray(b, np.float64)).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_fp32_field_update(gpu_available, tag):
+    f = load(tag, "field")
+    s = mg.Setup.from_job(job(TAGS[tag][0]))
+    ctx = mg.Context.from_setup(s, mg.FP32)
+    ctx.upload_fields(f["anp1"], f["an"], f["anm1"])
+    ctx.field_update()
+    anp1, _, _ = ctx.download_fields()
+    assert scaled_err(anp1, f["out_anp1"]) <= FIELD_STAGE_RTOL
+    en, bn = ctx.download_eb()
+    sel = interior_mask(meta(tag))
+    assert scaled_err(en[sel], f["en"][sel]) <= 1e-5
+    assert scaled_err(bn[sel], f["bn"][sel]) <= 1e-5
+
+
+def test_fp32_push(gpu_available):
+    tag = "kat-small-fd"
+    p = load(tag, "push")
+    s = mg.Setup.from_job(job(TAGS[tag][0]))
+    ctx = mg.Context.from_setup(s, mg.FP32)
+    ctx.upload_fields(p["anp1"], p["an"], None)
+    ctx.field_evaluate()
+    ctx.upload_particles(p["particles"])
+    t = ctx.get_time()
+    t.time_bunch = float(p["time_bunch"][0])
+    ctx.set_time(t)
+    ctx.bunch_update()
+    out = ctx.download_particles()
+    ref = p["out"]
+    assert out.shape == ref.shape
+    for col in (1, 2, 3, 7, 8, 9):
+        assert scaled_err(out[:, col], ref[:, col]) <= PUSH_RTOL, col
+
+
+def test_fp32_deposit(gpu_available):
+    tag = "kat-small-fd"
+    d = load(tag, "deposit")
+    s = mg.Setup.from_job(job(TAGS[tag][0]))
+    ctx = mg.Context.from_setup(s, mg.FP32)
+    ctx.upload_particles(d["particles"])
+    ctx.current_update()
+    J, _, _ = ctx.download_fields()
+    assert rel_l2(J, d["J"]) <= DEPOSIT_RTOL
+
+
+def full_march_power(precision, jobname="fel-ir-48x48x384.job"):
+    s = mg.Setup.from_job(job(jobname))
+    fd = mg.FdTd(s, precision=precision)
+    rows = fd.solve()
+    return rows.reshape(-1, 2)
+
+
+@pytest.mark.slow
+def test_fp32_saturation_power_within_one_percent(gpu_available):
+    """Full march of the 48x48x384 job (to the undulator exit) in both forms."""
+    p64 = full_march_power(mg.FP64)
+    p32 = full_march_power(mg.FP32)
+    assert p64.shape == p32.shape
+    P64, P32 = p64[:, 1], p32[:, 1]
+    psat64, psat32 = P64.max(), P32.max()
+    assert psat64 > 0
+    assert abs(psat32 - psat64) / psat64 <= PSAT_RTOL

@@ -152,3 +152,22 @@ def test_config1_100_steps_against_oracle(gpu_available):
     rows = ctx.power_rows().reshape(100, -1)
     ref = np.array([np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)])) for zl, pg in o.power_rows])
     assert_close_scaled(rows, ref, 1e-8, "power rows")
+
+
+def test_space_charge_march_matches_reference(gpu_available):
+    """FdTdSC on the device: A and phi after 12 steps against the reference's own run."""
+    run = load("kat-small-sc", "run")
+    s = mg.Setup.from_job(job("kat-small-sc.job"))
+    ctx = mg.Context.from_setup(s)
+    ctx.run_prelude()
+    ctx.run(12)
+    anp1, an, anm1 = ctx.download_fields()
+    fnp1, fn, fnm1 = ctx.download_scalar()
+    assert rel_l2(an, run["an12"]) <= MARCH_RTOL
+    assert rel_l2(anm1, run["anm1_12"]) <= MARCH_RTOL
+    assert rel_l2(fn, run["fn12"]) <= MARCH_RTOL
+    assert rel_l2(fnm1, run["fnm1_12"]) <= MARCH_RTOL
+    assert rel_l2(fnp1, run["fnp1_12"]) <= MARCH_RTOL
+    assert np.abs(run["fn12"]).max() > 0
+    rows = ctx.power_rows().reshape(12, -1)
+    assert_close_scaled(rows, run["power"], 1e-9, "power rows")

@@ -47,3 +47,14 @@ def test_comment_and_whitespace_rules(tmp_path):
     a = mg.Setup.from_job(job("kat-small.job")).particles()
     b = mg.Setup.from_job(str(p)).particles()
     assert np.array_equal(a, b)
+
+
+def test_space_charge_setup_matches_reference():
+    z = load("kat-small-sc", "init")
+    ref = {str(k): float(v) for k, v in zip(z["meta_keys"], z["meta_vals"])}
+    s = mg.Setup.from_job(job("kat-small-sc.job"))
+    m = s.meta()
+    for k, v in ref.items():
+        assert m[k] == v, k
+    assert s.grid().space_charge == 1
+    assert np.array_equal(s.particles(), z["particles"])

@@ -80,3 +80,22 @@ def test_oracle_deposit_matches_reference():
                                 po.dptr(J), None)
     assert np.array_equal(J, d["J"])
     assert np.count_nonzero(J) > 0
+
+
+def test_oracle_space_charge_march_matches_reference():
+    """FdTdSC: scalar potential leapfrog, rho deposit and -grad(phi) in E, 12 steps."""
+    tag = "kat-small-sc"
+    z = load(tag, "init")
+    m = {str(k): float(v) for k, v in zip(z["meta_keys"], z["meta_vals"])}
+    run = load(tag, "run")
+    r = po.OracleRun(m, z["an"], z["anm1"], z["anp1"], z["particles"], solver=0, order=2,
+                     fn=z["fn"], fnm1=z["fnm1"], fnp1=z["fnp1"])
+    for step in range(1, 13):
+        r.step()
+        zl, pg = r.power_rows[-1]
+        row = np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)]))
+        assert np.array_equal(row, run["power"][step - 1]), "power row %d" % step
+    for a, b in ((r.an, "an12"), (r.anm1, "anm1_12"), (r.anp1, "anp1_12"), (r.fn, "fn12"), (r.fnm1, "fnm1_12"),
+                 (r.fnp1, "fnp1_12"), (r.particles, "particles12")):
+        assert np.array_equal(a, run[b]), b
+    assert np.abs(r.fn).max() > 0
