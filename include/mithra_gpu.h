@@ -145,6 +145,16 @@ int mithra_gpu_bunch_update(mithra_ctx* ctx);
 int mithra_gpu_recycle(mithra_ctx* ctx);
 /* Solver::powerSample (src/radiation.cpp:127-232); the row is appended to the device row log. */
 int mithra_gpu_power_sample(mithra_ctx* ctx);
+/* mithra_gpu_power_sample without any device allocation.  No counterpart in the reference: it
+ * serves callers that cannot allocate device memory at this point (all of it already given to
+ * fields and particles, or no device-wide synchronisation allowed while other streams run).
+ * The per-block partial sums go to one fixed 1 MiB array per device (131072 doubles, shared by
+ * every context on the device and needing no zeroing); an output that needs more
+ * (planes x blocks per plane x frequencies) is refused with MITHRA_ERR_CAPACITY, and so is a
+ * call when the row log is full (drain it with mithra_gpu_power_rows).  The first call on a
+ * device looks up the array's address and may load the module: make one call before any
+ * stream capture.  Calls that overlap in time on one device race on the shared array. */
+int mithra_gpu_power_sample_noalloc(mithra_ctx* ctx);
 /* FdTd::fieldShift (src/fdtd.cpp:806-812). */
 int mithra_gpu_field_shift(mithra_ctx* ctx);
 /* FdTd::currentReset + currentUpdate + currentCommunicate (src/fdtd.cpp:23-225). */

@@ -93,6 +93,7 @@ _SIGS = {
     "mithra_gpu_bunch_update": [_vp],
     "mithra_gpu_recycle": [_vp],
     "mithra_gpu_power_sample": [_vp],
+    "mithra_gpu_power_sample_noalloc": [_vp],
     "mithra_gpu_field_shift": [_vp],
     "mithra_gpu_current_update": [_vp],
     "mithra_gpu_advance_time": [_vp],
@@ -402,6 +403,10 @@ class Context:
 
     def power_sample(self):
         self.call("mithra_gpu_power_sample")
+
+    def power_sample_noalloc(self):
+        """power_sample with no device allocation: partial sums in a fixed per-device array."""
+        self.call("mithra_gpu_power_sample_noalloc")
 
     def field_shift(self):
         self.call("mithra_gpu_field_shift")

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -970,3 +971,89 @@ int mithra_gpu_kernel_times(mithra_ctx* ctx, char* names, size_t name_len, doubl
 }
 
 }  // extern "C"
+
+
+// ---- power sample without allocation ----------------------------------------------------
+//
+// mithra_gpu_power_sample may allocate: it grows the device row log when it is full, and its
+// per-block partial sums live in a buffer of the context.  Some callers cannot allow an
+// allocation at that point: a host loop that has already given the whole of device memory to
+// fields and particles (cudaMalloc would fail), or one that must not stall on the device-wide
+// synchronisation that cudaFree implies while other streams are running.  The variant below
+// keeps the partial sums in a fixed array in device memory that is part of the loaded module,
+// and refuses, with an error, to grow the row log.
+
+namespace {
+
+// Partial sums of one power output: (planes x blocks per plane x frequencies) doubles.  The
+// sample kernel writes every slot that the finish kernel then reads, within the same call, so
+// nothing in this array needs to start at zero.  There is ONE array per device, shared by all
+// contexts on that device: two calls that overlap in time on one device (different contexts,
+// streams or host threads) race on it, and the caller must order them.
+constexpr long long kStaticPartialMax = 1LL << 17;  // 131072 doubles = 1 MiB
+static __device__ __align__(256) double g_static_partial[kStaticPartialMax];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_partial_mu;
+double* g_static_partial_addr[kMaxDevices] = {};
+
+// Device address of g_static_partial on `device`, looked up once per device with that device
+// current.  The first lookup on a device does set-up work in the runtime (it may load the
+// module), so callers should make one call before they start any stream capture.
+int static_partial_address(mithra_ctx* ctx, double** out) {
+  const int device = ctx->device;
+  if (device < 0 || device >= kMaxDevices) return fail(ctx, MITHRA_ERR_ARG, "device %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_static_partial_mu);
+  if (!g_static_partial_addr[device]) {
+    int prev = -1;
+    CK(cudaGetDevice(&prev));
+    if (prev != device) CK(cudaSetDevice(device));
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partial);
+    if (prev != device) CK(cudaSetDevice(prev));
+    if (e != cudaSuccess || !p)
+      return fail(ctx, MITHRA_ERR_CUDA, "cudaGetSymbolAddress(g_static_partial): %s", cudaGetErrorString(e));
+    g_static_partial_addr[device] = static_cast<double*>(p);
+  }
+  *out = g_static_partial_addr[device];
+  return MITHRA_OK;
+}
+
+}  // namespace
+
+extern "C" int mithra_gpu_power_sample_noalloc(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (ctx->power.empty()) return MITHRA_OK;
+  for (const auto& po : ctx->power) {
+    const long long need = (long long)po.dev.N * po.dev.blocks_per_plane * std::max(po.dev.Nl, 1);
+    if (need > kStaticPartialMax)
+      return fail(ctx, MITHRA_ERR_CAPACITY,
+                  "power output needs %lld partial sums (%d planes x %d blocks x %d frequencies); the fixed "
+                  "array holds %lld: use mithra_gpu_power_sample",
+                  need, po.dev.N, po.dev.blocks_per_plane, po.dev.Nl, kStaticPartialMax);
+  }
+  if (ctx->rows_pending + 1 > ctx->row_cap)
+    return fail(ctx, MITHRA_ERR_CAPACITY,
+                "power row log full (%lld rows): drain it with mithra_gpu_power_rows before sampling again",
+                ctx->row_cap);
+  double* partial = nullptr;
+  int r = static_partial_address(ctx, &partial);
+  if (r) return r;
+  ctx->rows_pending += 1;
+  for (size_t o = 0; o < ctx->power.size(); o++) {
+    PowerDev pw = ctx->power[o].dev;  // same output, partial sums redirected to the fixed array
+    pw.partial = partial;
+    const int blocks = pw.N * pw.blocks_per_plane;
+    const size_t shm = (size_t)kPowerBlock * pw.Nl * sizeof(double);
+    if (ctx->precision == MITHRA_PRECISION_FP64)
+      k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E64, ctx->B64, ctx->st);
+    else
+      k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E, ctx->B, ctx->st);
+    const int last = (o + 1 == ctx->power.size());
+    k_power_finish<<<1, 256, 0, ctx->stream>>>(pw, ctx->st, last);
+    ctx->launch_counter += 2;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "launch power_sample (fixed scratch): %s", cudaGetErrorString(e));
+  }
+  return MITHRA_OK;
+}
