@@ -445,10 +445,14 @@ void read_undulator(Cursor& c, Job& J) {
 
 void read_ext_field(Cursor& c, Job& J) {
   c.open("EXTERNAL-FIELD");
+  // One ExtField object is re-initialised for every group (src/datainput.cpp:567): the default
+  // strength is the previous group's a0_, and order_ keeps its last super-Gaussian value.
+  ExtField e;
   do {
     if (c.cur() == "electromagnetic-wave") {
       c.open("electromagnetic-field");
       BeamKeys k;
+      k.a0 = e.a0;
       Signal defaults;
       k.offset = defaults.t0;
       k.pulseLength = defaults.s;
@@ -461,7 +465,6 @@ void read_ext_field(Cursor& c, Job& J) {
         c.next();
       } while (c.cur() != "}");
       Signal s = k.signal();
-      ExtField e;
       init_beam(e, k.type, k.position, k.direction, k.polarization, k.a0, k.radius, k.order, s, true);
       J.extFields.push_back(e);
     }

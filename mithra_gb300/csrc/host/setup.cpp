@@ -686,6 +686,32 @@ void Setup::fill_push(mithra_push_desc* p) const {
   p->n_update_bunch = nUpdateBunch;
 }
 
+namespace {
+// Laser-beam parameters under the keys the reference harness writes for them.
+template <class KV>
+void beam_meta(KV& kv, const std::string& p, const Beam& b) {
+  kv(p + "type", (double)b.seedType);
+  for (int c = 0; c < 3; c++) {
+    kv(p + "pos" + std::to_string(c), b.position[c]);
+    kv(p + "dir" + std::to_string(c), b.direction[c]);
+    kv(p + "pol" + std::to_string(c), b.polarization[c]);
+  }
+  kv(p + "amp", b.amplitude);
+  kv(p + "r0", b.radius.size() > 0 ? b.radius[0] : 0.0);
+  kv(p + "r1", b.radius.size() > 1 ? b.radius[1] : 0.0);
+  kv(p + "o0", b.order.size() > 0 ? b.order[0] : 0);
+  kv(p + "o1", b.order.size() > 1 ? b.order[1] : 0);
+  kv(p + "l", b.l);
+  kv(p + "zR0", b.zR.size() > 0 ? b.zR[0] : 0.0);
+  kv(p + "zR1", b.zR.size() > 1 ? b.zR[1] : 0.0);
+  kv(p + "sig_type", (double)b.signal.type);
+  kv(p + "sig_t0", b.signal.t0); kv(p + "sig_s", b.signal.s); kv(p + "sig_f0", b.signal.f0);
+  kv(p + "sig_cep", b.signal.cep); kv(p + "sig_nR", (double)b.signal.nR);
+  kv(p + "sig_g0", b.signal.sigmaInvG.size() > 0 ? b.signal.sigmaInvG[0] : 0.0);
+  kv(p + "sig_g1", b.signal.sigmaInvG.size() > 1 ? b.signal.sigmaInvG[1] : 0.0);
+}
+}  // namespace
+
 std::string Setup::meta() const {
   std::ostringstream o;
   char buf[96];
@@ -717,7 +743,13 @@ std::string Setup::meta() const {
     const std::string p = "und" + std::to_string(u) + "_";
     kv(p + "k", U.k); kv(p + "lu", U.lu); kv(p + "rb", U.rb); kv(p + "length", U.length);
     kv(p + "dist", U.dist); kv(p + "theta", U.theta); kv(p + "type", (double)U.type);
+    if (U.type == OPTICAL) beam_meta(kv, p + "beam_", U);
   }
+  beam_meta(kv, "seed_", job.seed);
+  kv("seed_gamma", job.seed.gamma); kv("seed_beta", job.seed.beta);
+  kv("seed_c0", job.seed.c0); kv("seed_dt", job.seed.dt);
+  kv("n_ext", (double)job.extFields.size());
+  for (size_t x = 0; x < job.extFields.size(); x++) beam_meta(kv, "ext" + std::to_string(x) + "_", job.extFields[x]);
   kv("n_particles", (double)charges.size());
   kv("n_fel", (double)job.fel.size());
   for (size_t o2 = 0; o2 < power.size(); o2++) {

@@ -13,8 +13,13 @@
 namespace mithra {
 
 constexpr int TX = 8, TY = 8, TZ = 8;                          // cells per tile (i, j, k)
-constexpr int HX = TX + 3, HY = TY + 3, HZ = TZ + 3;           // nodes per tile incl. halo
+constexpr int HX = TX + 3, HZ = TZ + 3;                        // nodes per tile along i, k incl. halo
+// Along j (contiguous in J) a tile row holds 16 nodes starting 4 before the tile's first cell, so
+// each row is four aligned float4 chunks of J: the flush adds whole chunks with vector atomics.
+// Nodes used: first cell - 1 .. first cell + TY + 1 (local 3 .. 13).
+constexpr int HY = 16, JOFF = 4;
 constexpr int TILE_NODES = HX * HY * HZ;
+static_assert(TY + 2 + JOFF <= HY && JOFF % 4 == 0 && HY % 4 == 0, "tile row layout");
 
 struct TileGrid {
   int ntx, nty, ntz;   // tiles along i, j, k
@@ -150,6 +155,7 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
   const float qx = qh * jx, qy = qh * jy, qz = qh * jz;
   const int li = ic - i0, lj = jc - j0, lk = kc - k0;  // local node coordinates of the cell origin
   const bool in_tile = li >= 0 && lj >= 0 && lk >= 0 && li + 1 < HX && lj + 1 < HY && lk + 1 < HZ;
+  // layout: ((k * HX + i) * HY + j), j fastest as in J
 #pragma unroll
   for (int q = 0; q < 8; q++) {
     const int di = (q >> 0) & 1, dj = (q >> 1) & 1, dk = (q >> 2) & 1;
@@ -158,7 +164,7 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
     const float wy = (di ? x2 : x1) * (dk ? z2 : z1);
     const float wz = (di ? x2 : x1) * (dj ? y2 : y1);
     if (in_tile) {
-      const int s = ((lk + dk) * HY + (lj + dj)) * HX + (li + di);
+      const int s = ((lk + dk) * HX + (li + di)) * HY + (lj + dj);
       atomicAdd(sJ + s, wx * qx);
       atomicAdd(sJ + TILE_NODES + s, wy * qy);
       atomicAdd(sJ + 2 * TILE_NODES + s, wz * qz);
@@ -173,7 +179,9 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
 
 // One block per tile bin (plus one for the particles outside the tiled range).  Same arithmetic
 // as k_deposit_f32; rho (space charge) is added straight to global memory.
-__global__ void __launch_bounds__(256) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
+constexpr int kDepositBlock = 128;
+
+__global__ void __launch_bounds__(kDepositBlock) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
                                                        StateDev* st, float* J, float* rho, long long cs,
                                                        long long plane, int P1) {
   extern __shared__ float sJ[];  // 3 * TILE_NODES
@@ -184,8 +192,9 @@ __global__ void __launch_bounds__(256) k_deposit_tiled(DepositF32 D, TileGrid T,
   int i0 = 0, j0 = 0, k0 = 0;
   if (tiled) {
     const int ti = b % T.ntx, tj = (b / T.ntx) % T.nty, tk = b / (T.ntx * T.nty);
-    i0 = ti * TX - 1; j0 = tj * TY - 1; k0 = tk * TZ - 1;  // halo of one cell below
-    for (int s = threadIdx.x; s < 3 * TILE_NODES; s += blockDim.x) sJ[s] = 0.0f;
+    i0 = ti * TX - 1; j0 = tj * TY - JOFF; k0 = tk * TZ - 1;  // halo of one cell below
+    float4* s4 = reinterpret_cast<float4*>(sJ);
+    for (int s = threadIdx.x; s < 3 * TILE_NODES / 4; s += blockDim.x) s4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
   }
   int kmin = 0x7fffffff, kmax = -0x7fffffff;
@@ -252,16 +261,21 @@ __global__ void __launch_bounds__(256) k_deposit_tiled(DepositF32 D, TileGrid T,
   }
   if (!tiled) return;
   __syncthreads();
-  // Flush: every non-zero tile node is added to J once.
-  for (int s = threadIdx.x; s < TILE_NODES; s += blockDim.x) {
-    const int li = s % HX, lj = (s / HX) % HY, lk = s / (HX * HY);
-    const int gi = i0 + li, gj = j0 + lj, gk = k0 + lk;
-    if (gi < 0 || gj < 0 || gk < 0 || gi >= D.N0 || gj >= D.N1 || gk >= D.N2) continue;
-    const long long m = (long long)gk * plane + (long long)gi * P1 + gj;
-    const float vx = sJ[s], vy = sJ[TILE_NODES + s], vz = sJ[2 * TILE_NODES + s];
-    if (vx != 0.0f) atomicAdd(J + m, vx);
-    if (vy != 0.0f) atomicAdd(J + cs + m, vy);
-    if (vz != 0.0f) atomicAdd(J + 2 * cs + m, vz);
+  // Flush: every tile chunk of four nodes with a non-zero value is added to J once, with one
+  // vector atomic; consecutive threads take consecutive chunks of a row.  A chunk lies wholly
+  // inside or wholly outside a padded row of J (both are aligned to four nodes), and only
+  // non-zero chunks, which hold nodes of real cells, are added.
+  const float4* s4 = reinterpret_cast<const float4*>(sJ);
+  constexpr int CH = HY / 4, CHUNKS = TILE_NODES / 4;
+  for (int s = threadIdx.x; s < 3 * CHUNKS; s += blockDim.x) {
+    const int c = s / CHUNKS, r = s % CHUNKS;
+    const int q = r % CH, li = (r / CH) % HX, lk = r / (CH * HX);
+    const int gi = i0 + li, gj = j0 + 4 * q, gk = k0 + lk;
+    if (gi < 0 || gj < 0 || gk < 0 || gi >= D.N0 || gj >= P1 || gk >= D.N2) continue;
+    const float4 v = s4[s];
+    if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
+    const long long m = (long long)c * cs + (long long)gk * plane + (long long)gi * P1 + gj;
+    atomicAdd(reinterpret_cast<float4*>(J + m), v);
   }
 }
 

@@ -94,8 +94,10 @@ static inline double corner_point(const double* h, const double* anp1, const dou
 
 /* One potential (vector with nc = 3 or scalar with nc = 1): the whole sequence of
  * FdTd::fieldUpdate for one rank that owns both z ends. */
+static void seed_inject(const mo_field* f, const mo_seed* seed, double time, double* anp1);
+
 static void potential_update(const mo_field* f, int nc, double asrc, double* anp1, const double* an,
-                             const double* anm1) {
+                             const double* anm1, const mo_seed* seed, double time) {
   const long N0 = f->N0, N1 = f->N1, np = f->np, N1N0 = N1 * N0;
   const long sI = nc * N1, sJ = nc, sK = nc * N1N0;
   const double* jsrc = anp1;  /* the source is read in place: J in anp1_ / rho in fnp1_ */
@@ -113,6 +115,9 @@ static void potential_update(const mo_field* f, int nc, double asrc, double* anp
           anp1[l + c] = v;
         }
       }
+
+  /* TF/SF seed injection, src/fdtd.cpp:307-373 (vector potential only). */
+  if (nc == 3 && seed && fabs(seed->beam.amplitude) > 1.0e-50) seed_inject(f, seed, time, anp1);
 
   /* Faces, src/fdtd.cpp:377-472. */
   for (long j = 1; j < N1 - 1; j++)
@@ -190,11 +195,163 @@ static void potential_update(const mo_field* f, int nc, double asrc, double* anp
 }
 
 void mo_field_update(const mo_field* f, double* anp1, const double* an, const double* anm1) {
-  potential_update(f, 3, f->a[4], anp1, an, anm1);
+  potential_update(f, 3, f->a[4], anp1, an, anm1, NULL, 0.0);
+}
+
+void mo_field_update_seeded(const mo_field* f, const mo_seed* seed, double time, double* anp1, const double* an,
+                            const double* anm1) {
+  potential_update(f, 3, f->a[4], anp1, an, anm1, seed, time);
 }
 
 void mo_scalar_update(const mo_field* f, double* fnp1, const double* fn, const double* fnm1) {
-  potential_update(f, 1, f->a[5], fnp1, fn, fnm1);
+  potential_update(f, 1, f->a[5], fnp1, fn, fnm1, NULL, 0.0);
+}
+
+/* ------------------------------------------------------------------------------------------ */
+/* Seed and laser-beam fields.                                                                 */
+/* ------------------------------------------------------------------------------------------ */
+
+static inline double dot3(const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; }
+static inline void cross3(const double* x, const double* y, double* z) {
+  z[0] = x[1] * y[2] - x[2] * y[1];
+  z[1] = x[2] * y[0] - x[0] * y[2];
+  z[2] = x[0] * y[1] - x[1] * y[0];
+}
+
+/* Signal::self, src/classes.cpp:533-576. */
+static double signal_self(const mo_signal* g, double t, double phase) {
+  const double t0 = g->t0, s = g->s, f0 = g->f0, cep = g->cep, nR = g->nR;
+  if (fabs(t - t0) > 10.0 * s) return 0.0;
+  if (g->type == 0)
+    return -cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * 2.7724 * (t - t0) / (s * s) *
+           exp(-1.3863 * (t - t0) * (t - t0) / (s * s));
+  if (g->type == 1) return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * exp(-1.3863 * pow((t - t0) / s, 2));
+  if (g->type == 2) return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) / cosh((t - t0) / s);
+  if (g->type == 3) {
+    if (t - t0 <= -s / 2.0) return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * exp(-pow((t - t0 + s / 2.0) * f0 / nR, 2));
+    if (t - t0 <= s / 2.0) return cos(2 * MO_PI * f0 * (t - t0) + cep + phase);
+    return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * exp(-pow((t - t0 - s / 2.0) * f0 / nR, 2));
+  }
+  if (g->type == 4) {
+    const double env = pow((1.0 + pow((t - t0) / g->sig0, 2)) * (1.0 + pow((t - t0) / g->sig1, 2)), 0.25);
+    if (t - t0 <= -s / 2.0)
+      return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * env * exp(-pow((t - t0 + s / 2.0) * f0 / nR, 2));
+    if (t - t0 <= s / 2.0) return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * env;
+    return cos(2 * MO_PI * f0 * (t - t0) + cep + phase) * env * exp(-pow((t - t0 - s / 2.0) * f0 / nR, 2));
+  }
+  return 0.0;
+}
+
+void mo_seed_fields(const mo_seed* sd, const double r[3], double time, double a[3]) {
+  const mo_beam* s = &sd->beam;
+  const double c0 = sd->c0;
+  double rl[3] = {r[0], r[1], sd->gamma * (r[2] + sd->beta * c0 * (time + sd->dt))};
+  double tl = sd->gamma * (time + sd->dt + sd->beta / c0 * r[2]);
+  double rv[3] = {rl[0] - s->position[0], rl[1] - s->position[1], rl[2] - s->position[2]};
+  double z = dot3(rv, s->direction);
+  tl -= z / c0;
+  double p = 0.0, tsignal, x, y, yv[3];
+  if (s->type == 0) {
+    tsignal = signal_self(&s->signal, tl, p);
+    if (fabs(tsignal) < 1.0e-6) a[0] = a[1] = a[2] = 0.0;
+    else for (int c = 0; c < 3; c++) a[c] = s->amplitude * tsignal * s->polarization[c];
+  } else if (s->type == 1) {
+    tsignal = signal_self(&s->signal, tl, p);
+    x = dot3(rv, s->polarization);
+    cross3(s->direction, s->polarization, yv);
+    y = dot3(rv, yv);
+    if (fabs(tsignal) < 1.0e-6 || fabs(x) > s->radius[0] || fabs(y) > s->radius[1]) a[0] = a[1] = a[2] = 0.0;
+    else for (int c = 0; c < 3; c++) a[c] = s->amplitude * tsignal * s->polarization[c];
+  } else if (s->type == 2 || s->type == 3) {
+    tsignal = signal_self(&s->signal, tl, p);
+    if (fabs(tsignal) < 1.0e-6) {
+      a[0] = a[1] = a[2] = 0.0;
+    } else {
+      x = dot3(rv, s->polarization);
+      cross3(s->direction, s->polarization, yv);
+      y = dot3(rv, yv);
+      double l = c0 / s->signal.f0;
+      double zRp = MO_PI * s->radius[0] * s->radius[0] / l;
+      double wrp = sqrt(1.0 + z * z / (zRp * zRp));
+      double zRs = MO_PI * s->radius[1] * s->radius[1] / l;
+      double wrs = sqrt(1.0 + z * z / (zRs * zRs));
+      if (s->type == 2) {
+        p = 0.5 * (atan(z / zRp) + atan(z / zRs) - MO_PI) - MO_PI * z / l * (pow(x / (zRp * wrp), 2) + pow(y / (zRs * wrs), 2));
+        tsignal = signal_self(&s->signal, tl, p);
+        double t = exp(-pow(x / (s->radius[0] * wrp), 2) - pow(y / (s->radius[1] * wrs), 2)) / sqrt(wrs * wrp) * s->amplitude;
+        for (int c = 0; c < 3; c++) a[c] = t * tsignal * s->polarization[c];
+      } else {
+        for (int i = -s->order[0]; i <= s->order[0]; i++)
+          for (int j = -s->order[1]; j <= s->order[1]; j++) {
+            p = 0.5 * (atan(z / zRp) + atan(z / zRs) - MO_PI) - MO_PI * z / l * (pow(x / (zRp * wrp), 2) + pow(y / (zRs * wrs), 2));
+            tsignal = signal_self(&s->signal, tl, p);
+            double t = exp(-pow(x / (s->radius[0] * wrp), 2) - pow(y / (s->radius[1] * wrs), 2)) / sqrt(wrs * wrp) * s->amplitude;
+            for (int c = 0; c < 3; c++) a[c] += t * tsignal * s->polarization[c];
+          }
+      }
+    }
+  }
+  a[2] *= sd->gamma;
+}
+
+/* TF/SF seed injection of FdTd::fieldUpdate for one rank owning both z ends
+ * (src/fdtd.cpp:307-373, KI = 2, KF = np - 2).  atemp is carried from call to call as in the
+ * reference, which matters only for seeds that accumulate into it. */
+static void seed_inject(const mo_field* f, const mo_seed* seed, double time, double* anp1) {
+  const long N0 = f->N0, N1 = f->N1, np = f->np, N1N0 = N1 * N0;
+  double atemp[3] = {0.0, 0.0, 0.0};
+  const long KI = 2, KF = np - 2;
+#define MO_RC(mm, out)                                              \
+  do {                                                               \
+    long k_ = (mm) / N1N0, i_ = ((mm) % N1N0) / N1;                  \
+    long j_ = (mm) - (N1N0 * k_ + N1 * i_);                          \
+    (out)[0] = f->xmin + i_ * f->dx;                                 \
+    (out)[1] = f->ymin + j_ * f->dy;                                 \
+    (out)[2] = f->zmin + (k_ + f->k0) * f->dz;                       \
+  } while (0)
+#define MO_ADD(m, sgn, coef)                                                   \
+  do {                                                                         \
+    for (int c = 0; c < 3; c++) anp1[3 * (m) + c] sgn## = (coef) * atemp[c];  \
+  } while (0)
+  double rc[3];
+  for (long j = 2; j < N1 - 2; j++)
+    for (long k = KI; k < KF; k++) {
+      long m = N1N0 * k + N1 * 1 + j;
+      MO_RC(m + N1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[1]);
+      m = N1N0 * k + N1 * 2 + j;
+      MO_RC(m - N1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[1]);
+      m = N1N0 * k + N1 * (N0 - 2) + j;
+      MO_RC(m - N1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[1]);
+      m = N1N0 * k + N1 * (N0 - 3) + j;
+      MO_RC(m + N1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[1]);
+    }
+  for (long i = 2; i < N0 - 2; i++)
+    for (long k = KI; k < KF; k++) {
+      long m = N1N0 * k + N1 * i + 1;
+      MO_RC(m + 1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[2]);
+      m = N1N0 * k + N1 * i + 2;
+      MO_RC(m - 1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[2]);
+      m = N1N0 * k + N1 * i + N1 - 2;
+      MO_RC(m - 1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[2]);
+      m = N1N0 * k + N1 * i + N1 - 3;
+      MO_RC(m + 1, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[2]);
+    }
+  for (long i = 2; i < N0 - 2; i++)
+    for (long j = 2; j < N1 - 2; j++) {
+      long m = N1N0 * 1 + N1 * i + j;
+      MO_RC(m + N1N0, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[3]);
+      m = N1N0 * 2 + N1 * i + j;
+      MO_RC(m - N1N0, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[3]);
+    }
+  for (long i = 2; i < N0 - 2; i++)
+    for (long j = 2; j < N1 - 2; j++) {
+      long m = N1N0 * (np - 2) + N1 * i + j;
+      MO_RC(m - N1N0, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, -, f->a[3]);
+      m = N1N0 * (np - 3) + N1 * i + j;
+      MO_RC(m + N1N0, rc); mo_seed_fields(seed, rc, time, atemp); MO_ADD(m, +, f->a[3]);
+    }
+#undef MO_RC
+#undef MO_ADD
 }
 
 /* FdTd::fieldEvaluate, src/fdtd.cpp:818-845 (SC: src/fdtdSC.cpp:1110-1140).  FieldVector::dv
@@ -259,13 +416,201 @@ static inline double mo_pmod(double a, double b) {
   return x;
 }
 
-/* Solver::undulatorField for STATIC modules (src/solver.cpp:1798-1824) and
+/* The per-call state of one laser-beam evaluation (the fields of UpdateBunchParallel that the
+ * beam functions of src/beam.cc:80-496 use). */
+typedef struct {
+  double rv[3], z, tl, tlm, p0;
+  double eT[3], bT[3];
+} beam_state;
+
+static inline void set3(double* d, double a, const double* v) { for (int c = 0; c < 3; c++) d[c] = a * v[c]; }
+static inline void add3(double* d, double a, const double* v) { for (int c = 0; c < 3; c++) d[c] += a * v[c]; }
+
+/* Solver::planeWave .. standingSuperGaussianBeam, src/beam.cc:80-496.  For the super-gaussian
+ * standing beam the reference reads an unset ubp.l (src/beam.cc:466); s->l (l_) is used here. */
+static void beam_fields(const mo_beam* s, double c0, beam_state* u) {
+  const int type = s->type;
+  double ts, tsm, tse, tsb, x = 0.0, y = 0.0, yv[3], x0, y0, wrp, wrs, atanP, atanS, t, p1, af;
+  double ex[3], ez[3], by[3], bz[3];
+  if (type == 0 || type == 1 || type == 4 || type == 5) {
+    if (type == 1 || type == 5) {
+      x = dot3(u->rv, s->polarization);
+      cross3(s->direction, s->polarization, yv);
+      y = dot3(u->rv, yv);
+    }
+    if (type == 5 && pow(x / s->radius[0], 2) + pow(y / s->radius[1], 2) > 1.0) goto zero;
+    if (type == 0 || type == 1) {
+      ts = signal_self(&s->signal, u->tl, u->p0);
+      if (fabs(ts) < 1.0e-6) goto zero;
+      if (type == 1 && pow(x / s->radius[0], 2) + pow(y / s->radius[1], 2) > 1.0) goto zero;
+      set3(u->eT, s->amplitude * ts, s->polarization);
+      cross3(s->direction, s->polarization, u->bT);
+      set3(u->bT, s->amplitude * ts / c0, u->bT);
+      return;
+    }
+    ts = signal_self(&s->signal, u->tl, u->p0);
+    tsm = signal_self(&s->signal, u->tlm, u->p0);
+    tse = ts - tsm;
+    tsb = ts + tsm;
+    if (fabs(tse) < 1.0e-6 && fabs(tsb) < 1.0e-6) goto zero;
+    set3(u->eT, s->amplitude * tse, s->polarization);
+    cross3(s->direction, s->polarization, u->bT);
+    set3(u->bT, s->amplitude * tsb / c0, u->bT);
+    return;
+  }
+  x = dot3(u->rv, s->polarization);
+  cross3(s->direction, s->polarization, yv);
+  y = dot3(u->rv, yv);
+  wrp = sqrt(1.0 + u->z * u->z / (s->zR[0] * s->zR[0]));
+  wrs = sqrt(1.0 + u->z * u->z / (s->zR[1] * s->zR[1]));
+  if (type == 2 || type == 6) {
+    x0 = x / wrp;
+    y0 = y / wrs;
+    if (fabs(x0) > 4.0 * s->radius[0] || fabs(y0) > 4.0 * s->radius[1]) goto zero;
+    ts = signal_self(&s->signal, u->tl, u->p0);
+    if (type == 2) {
+      if (fabs(ts) < 1.0e-6) goto zero;
+    } else {
+      tsm = signal_self(&s->signal, u->tlm, u->p0);
+      tse = ts - tsm;
+      tsb = ts + tsm;
+      if (fabs(tse) < 1.0e-6 && fabs(tsb) < 1.0e-6) goto zero;
+    }
+    atanP = atan(u->z / s->zR[0]);
+    atanS = atan(u->z / s->zR[1]);
+    u->p0 = 0.5 * (atanP + atanS) - MO_PI * u->z / s->l * (pow(x0 / s->zR[0], 2) + pow(y0 / s->zR[1], 2));
+    t = exp(-pow(x0 / s->radius[0], 2) - pow(y0 / s->radius[1], 2)) / sqrt(wrs * wrp);
+    t *= s->amplitude;
+    if (type == 2) {
+      p1 = u->p0 - MO_PI / 2.0;
+      ts = signal_self(&s->signal, u->tl, p1);
+      set3(ex, t * ts, s->polarization);
+      set3(by, t * ts / c0, yv);
+      p1 = u->p0 + atanP;
+      ts = signal_self(&s->signal, u->tl, p1);
+      set3(ez, t * (-x0 / s->zR[0]) * ts, s->direction);
+      p1 = u->p0 + atanS;
+      ts = signal_self(&s->signal, u->tl, p1);
+      set3(bz, t * (-y0 / s->zR[1]) / c0 * ts, s->direction);
+    } else {
+      p1 = u->p0 - MO_PI / 2.0;
+      ts = signal_self(&s->signal, u->tl, p1);
+      p1 = u->p0 - MO_PI / 2.0;
+      tsm = signal_self(&s->signal, u->tlm, p1);
+      set3(ex, t * (ts - tsm), s->polarization);
+      set3(by, t / c0 * (ts + tsm), yv);
+      p1 = u->p0 + atanP;
+      ts = signal_self(&s->signal, u->tl, p1);
+      p1 = -p1;
+      tsm = signal_self(&s->signal, u->tlm, p1);
+      set3(ez, t * (-x0 / s->zR[0]) * (ts - tsm), s->direction);
+      p1 = u->p0 + atanS;
+      ts = signal_self(&s->signal, u->tl, p1);
+      p1 = -p1;
+      tsm = signal_self(&s->signal, u->tlm, p1);
+      set3(bz, t * (-y0 / s->zR[1]) / c0 * (ts - tsm), s->direction);
+    }
+    for (int c = 0; c < 3; c++) { u->eT[c] = ex[c]; u->eT[c] += ez[c]; u->bT[c] = by[c]; u->bT[c] += bz[c]; }
+    return;
+  }
+  /* super-gaussian (3) and its standing variant (7) */
+  if ((fabs(x) - s->order[0] * s->radius[0]) > 4.0 * s->radius[0] * wrp ||
+      (fabs(y) - s->order[1] * s->radius[1]) > 4.0 * s->radius[1] * wrs)
+    goto zero;
+  ts = signal_self(&s->signal, u->tl, u->p0);
+  if (type == 3) {
+    if (fabs(ts) < 1.0e-6) goto zero;
+  } else {
+    tsm = signal_self(&s->signal, u->tlm, u->p0);
+    tse = ts - tsm;
+    tsb = ts + tsm;
+    if (fabs(tse) < 1.0e-6 && fabs(tsb) < 1.0e-6) goto zero;
+  }
+  atanP = atan(u->z / s->zR[0]);
+  atanS = atan(u->z / s->zR[1]);
+  af = s->amplitude / sqrt(wrs * wrp);
+  for (int c = 0; c < 3; c++) ex[c] = ez[c] = bz[c] = by[c] = 0.0;
+  for (int i = -s->order[0]; i <= s->order[0]; i++)
+    for (int j = -s->order[1]; j <= s->order[1]; j++) {
+      x0 = (x - i * s->radius[0]) / wrp;
+      y0 = (y - j * s->radius[1]) / wrs;
+      if (fabs(x0) > 4.0 * s->radius[0] || fabs(y0) > 4.0 * s->radius[1]) continue;
+      u->p0 = 0.5 * (atanP + atanS) - MO_PI * u->z / s->l * (pow(x0 / s->zR[0], 2) + pow(y / s->zR[1], 2));
+      t = af * exp(-pow(x0 / s->radius[0], 2) - pow(y0 / s->radius[1], 2));
+      if (type == 3) {
+        p1 = u->p0 - MO_PI / 2.0;
+        ts = signal_self(&s->signal, u->tl, p1);
+        add3(ex, t * ts, s->polarization);
+        add3(by, t * ts / c0, yv);
+        p1 = u->p0 + atanP;
+        ts = signal_self(&s->signal, u->tl, p1);
+        add3(ez, t * (-x0 / s->zR[0]) * ts, s->direction);
+        p1 = u->p0 + atanS;
+        ts = signal_self(&s->signal, u->tl, p1);
+        add3(bz, t * (-y0 / s->zR[1]) * ts / c0, s->direction);
+      } else {
+        p1 = u->p0 - MO_PI / 2.0;
+        ts = signal_self(&s->signal, u->tl, p1);
+        p1 = u->p0 - MO_PI / 2.0;
+        tsm = signal_self(&s->signal, u->tlm, p1);
+        add3(ex, t * (ts - tsm), s->polarization);
+        add3(by, t * (ts + tsm) / c0, yv);
+        p1 = u->p0 + atanP;
+        ts = signal_self(&s->signal, u->tl, p1);
+        p1 = -p1;
+        tsm = signal_self(&s->signal, u->tlm, p1);
+        add3(ez, t * (-x0 / s->zR[0]) * (ts - tsm), s->direction);
+        p1 = u->p0 + atanS;
+        ts = signal_self(&s->signal, u->tl, p1);
+        p1 = -p1;
+        tsm = signal_self(&s->signal, u->tlm, p1);
+        add3(bz, t * (-y0 / s->zR[1]) * (ts - tsm) / c0, s->direction);
+      }
+    }
+  for (int c = 0; c < 3; c++) { u->eT[c] = ex[c]; u->eT[c] += ez[c]; u->bT[c] = by[c]; u->bT[c] += bz[c]; }
+  return;
+zero:
+  for (int c = 0; c < 3; c++) u->eT[c] = u->bT[c] = 0.0;
+}
+
+/* The boost of a lab-frame beam field into the bunch frame, added to bt/et
+ * (src/solver.cpp:1870-1877, :1937-1944). */
+static inline void boost_add(const mo_push* p, const beam_state* u, double* bt, double* et) {
+  bt[0] += p->gamma * (u->bT[0] + p->beta / p->c0 * u->eT[1]);
+  bt[1] += p->gamma * (u->bT[1] - p->beta / p->c0 * u->eT[0]);
+  bt[2] += u->bT[2];
+  et[0] += p->gamma * (u->eT[0] - p->beta * p->c0 * u->bT[1]);
+  et[1] += p->gamma * (u->eT[1] + p->beta * p->c0 * u->bT[0]);
+  et[2] += u->eT[2];
+}
+
+/* One laser beam at the lab point of bunch-frame r and timeBunch: rv, z, tl and tlm of
+ * src/solver.cpp:1829-1840 and :1890-1904.  The optical-undulator branch of the reference
+ * never sets tlm (standing beams there read a stale value); t0 + z/c0 is used for both. */
+static void beam_at(const mo_push* p, const mo_beam* s, double timeBunch, const double* r, beam_state* u) {
+  double rl[3] = {r[0], r[1], p->gamma * (r[2] + p->beta * p->c0 * (timeBunch + p->dt_shift))};
+  double t0 = p->gamma * (timeBunch + p->dt_shift + p->beta / p->c0 * r[2]);
+  for (int c = 0; c < 3; c++) u->rv[c] = rl[c] - s->position[c];
+  u->z = dot3(u->rv, s->direction);
+  u->tl = t0 - u->z / p->c0;
+  u->tlm = t0 + u->z / p->c0;
+  u->p0 = 0.0;
+  beam_fields(s, p->c0, u);
+}
+
+/* Solver::undulatorField (src/solver.cpp:1798-1880): static modules with
  * Solver::staticUndulator (src/beam.cc:14-76).  ub_.b0/ku/ct/st are recomputed per module per
  * particle in the reference; the values are the same every time. */
 static void static_undulators(const mo_push* p, double timeBunch, const double* r, double* bt,
                               double* et) {
   for (int u = 0; u < p->n_und; u++) {
     const mo_undulator* U = &p->und[u];
+    if (U->type == 1) {
+      beam_state st;
+      beam_at(p, &U->beam, timeBunch, r, &st);
+      boost_add(p, &st, bt, et);
+      continue;
+    }
     if (U->type != 0) continue;
     double b0 = (U->lu != 0.0) ? 9.109e-31 * p->c0 * 2 * MO_PI / U->lu * U->k / 1.602e-19 : 0.0;
     double ku = (U->lu != 0.0) ? 2 * MO_PI / U->lu : 0.0;
@@ -345,7 +690,12 @@ static int push_one(const mo_push* p, double timeBunch, double* q, const float* 
 
   double bt[3] = {0.0, 0.0, 0.0}, et[3] = {0.0, 0.0, 0.0};
   static_undulators(p, timeBunch, rnp, bt, et);
-  /* externalField (src/solver.cpp:1886-1947) adds nothing without EXTERNAL-FIELD entries. */
+  /* Solver::externalField, src/solver.cpp:1886-1947. */
+  for (int x = 0; x < p->n_ext; x++) {
+    beam_state st;
+    beam_at(p, &p->ext[x], timeBunch, rnp, &st);
+    boost_add(p, &st, bt, et);
+  }
 
   if (*e == 1.0) {
     if (b1x && b1y && b1z) {

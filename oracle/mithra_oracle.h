@@ -25,6 +25,32 @@ extern "C" {
 
 #define MO_REC 11          /* doubles per particle record */
 #define MO_MAX_UND 64
+#define MO_MAX_EXT 16
+
+/* Signal (src/classes.h:159-195): type 0 neumann, 1 gaussian, 2 secant, 3 flat-top,
+ * 4 inverse-gaussian; cep in radians, f0 = 1/l as set by Signal::initialize. */
+typedef struct {
+  int type;
+  double t0, s, f0, cep, nR, sig0, sig1;
+} mo_signal;
+
+/* The laser-beam part shared by Seed, optical Undulator and ExtField (src/classes.h:201-462).
+ * type: SeedType 0 plane-wave, 1 truncated plane-wave, 2 gaussian, 3 super-gaussian,
+ * 4..7 their standing variants.  l and zR are the members l_, zR_ set by initialize. */
+typedef struct {
+  int type;
+  double position[3], direction[3], polarization[3];
+  double amplitude, radius[2];
+  int order[2];
+  double l, zR[2];
+  mo_signal signal;
+} mo_beam;
+
+/* Seed with the frame parameters that Seed::fields uses (src/classes.cpp:740-855). */
+typedef struct {
+  mo_beam beam;
+  double gamma, beta, c0, dt;
+} mo_seed;
 
 typedef struct {
   int N0, N1, np, k0;       /* nodes along x, y, and along z in this domain */
@@ -37,11 +63,13 @@ typedef struct {
   double eE[5], fE[5], gE[5];
   double hC[17];
   double dt, dx, dy, dz;
+  double xmin, ymin, zmin;  /* node (0,0,0) position, for the TF/SF seed points rc(m) */
 } mo_field;
 
 typedef struct {
-  int type;                 /* 0 static */
+  int type;                 /* 0 static, 1 optical */
   double k, lu, rb, length, dist, theta;
+  mo_beam beam;             /* the optical undulator's laser beam */
 } mo_undulator;
 
 typedef struct {
@@ -53,6 +81,8 @@ typedef struct {
   double gamma, beta, c0, dt_shift;  /* gamma_, beta_, c0_, dt_ */
   int n_und;
   mo_undulator und[MO_MAX_UND];
+  int n_ext;                /* EXTERNAL-FIELD entries (src/solver.cpp:1886-1947) */
+  mo_beam ext[MO_MAX_EXT];
 } mo_push;
 
 typedef struct {
@@ -78,6 +108,16 @@ typedef struct {
  * of A (J is read from anp1 in place), Mur faces, and for order 2 edges and corners. */
 void mo_field_update(const mo_field* f, double* anp1, const double* an, const double* anm1);
 
+/* mo_field_update with the TF/SF injection of the seed (src/fdtd.cpp:307-373) between the
+ * interior update and the Mur boundaries; `time` is time_ of the step.  seed == NULL or an
+ * amplitude not above 1e-50 injects nothing, as in the reference. */
+void mo_field_update_seeded(const mo_field* f, const mo_seed* seed, double time, double* anp1, const double* an,
+                            const double* anm1);
+
+/* Seed::fields (src/classes.cpp:740-855) at one bunch-frame point.  `a` is an accumulator as
+ * in the reference: plane-wave and gaussian seeds overwrite it, the super-gaussian adds to it. */
+void mo_seed_fields(const mo_seed* s, const double r[3], double time, double a[3]);
+
 /* The scalar-potential counterpart used with space charge (src/fdtdSC.cpp:260-1087):
  * interior update with rho read from fnp1 in place, Mur faces, edges, corners. */
 void mo_scalar_update(const mo_field* f, double* fnp1, const double* fn, const double* fnm1);
@@ -88,8 +128,9 @@ void mo_scalar_update(const mo_field* f, double* fnp1, const double* fn, const d
 void mo_eval_eb(const mo_field* f, const double* anp1, const double* an, const double* fn,
                 float* en, float* bn);
 
-/* One Solver::bunchUpdate over all particles (src/solver.cpp:1424-1576) with the static
- * undulator field (src/solver.cpp:1798-1880, src/beam.cc:14-76).  Particles that cross a z
+/* One Solver::bunchUpdate over all particles (src/solver.cpp:1424-1576) with the undulator
+ * fields (static: src/solver.cpp:1798-1824, src/beam.cc:14-76; optical: src/solver.cpp:1825-1878)
+ * and the external fields (src/solver.cpp:1886-1947, src/beam.cc:80-496).  Particles that cross a z
  * face are appended again, as the single-rank self-exchange does (src/solver.cpp:1544-1568).
  * Returns the new particle count (<= cap), or -1 when cap would be exceeded. */
 long mo_push_substep(const mo_push* p, double timeBunch, double* rec, long n, long cap,

@@ -50,6 +50,25 @@ def build_reference(ref_src: str = "/root/reference/src", jobs: int = 8) -> str 
     return os.path.join(HERE, "_ref", "ref_harness")
 
 
+MO_MAX_EXT = 16
+
+
+class MoSignal(C.Structure):
+    _fields_ = [("type", C.c_int), ("t0", C.c_double), ("s", C.c_double), ("f0", C.c_double),
+                ("cep", C.c_double), ("nR", C.c_double), ("sig0", C.c_double), ("sig1", C.c_double)]
+
+
+class MoBeam(C.Structure):
+    _fields_ = [("type", C.c_int), ("position", C.c_double * 3), ("direction", C.c_double * 3),
+                ("polarization", C.c_double * 3), ("amplitude", C.c_double), ("radius", C.c_double * 2),
+                ("order", C.c_int * 2), ("l", C.c_double), ("zR", C.c_double * 2), ("signal", MoSignal)]
+
+
+class MoSeed(C.Structure):
+    _fields_ = [("beam", MoBeam), ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double),
+                ("dt", C.c_double)]
+
+
 class MoField(C.Structure):
     _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("np", C.c_int), ("k0", C.c_int),
                 ("solver", C.c_int), ("order", C.c_int), ("space_charge", C.c_int),
@@ -57,12 +76,13 @@ class MoField(C.Structure):
                 ("bB", C.c_double * 5), ("cB", C.c_double * 5), ("dB", C.c_double * 5),
                 ("eE", C.c_double * 5), ("fE", C.c_double * 5), ("gE", C.c_double * 5),
                 ("hC", C.c_double * 17),
-                ("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double)]
+                ("dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double)]
 
 
 class MoUndulator(C.Structure):
     _fields_ = [("type", C.c_int), ("k", C.c_double), ("lu", C.c_double), ("rb", C.c_double),
-                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double)]
+                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double), ("beam", MoBeam)]
 
 
 class MoPush(C.Structure):
@@ -72,7 +92,8 @@ class MoPush(C.Structure):
                 ("Lz", C.c_double), ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
                 ("dtb", C.c_double), ("r1", C.c_double), ("r2", C.c_double),
                 ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double), ("dt_shift", C.c_double),
-                ("n_und", C.c_int), ("und", MoUndulator * MO_MAX_UND)]
+                ("n_und", C.c_int), ("und", MoUndulator * MO_MAX_UND),
+                ("n_ext", C.c_int), ("ext", MoBeam * MO_MAX_EXT)]
 
 
 class MoDeposit(C.Structure):
@@ -103,6 +124,8 @@ def lib():
         P = C.POINTER
         d, f, l = P(C.c_double), P(C.c_float), C.c_long
         _lib.mo_field_update.argtypes = [P(MoField), d, d, d]
+        _lib.mo_field_update_seeded.argtypes = [P(MoField), P(MoSeed), C.c_double, d, d, d]
+        _lib.mo_seed_fields.argtypes = [P(MoSeed), d, C.c_double, d]
         _lib.mo_scalar_update.argtypes = [P(MoField), d, d, d]
         _lib.mo_eval_eb.argtypes = [P(MoField), d, d, d, f, f]
         _lib.mo_push_substep.argtypes = [P(MoPush), C.c_double, d, l, l, f, f, P(C.c_long)]
@@ -138,6 +161,33 @@ def read_meta(path: str) -> dict:
     return out
 
 
+def beam_params(m: dict, prefix: str, out: MoBeam) -> MoBeam:
+    """A laser beam (seed, optical undulator or external field) from the meta keys `prefix*`."""
+    g = lambda k: m.get(prefix + k, 0.0)
+    out.type = int(g("type"))
+    for c in range(3):
+        out.position[c], out.direction[c], out.polarization[c] = g("pos%d" % c), g("dir%d" % c), g("pol%d" % c)
+    out.amplitude = g("amp")
+    out.radius[0], out.radius[1] = g("r0"), g("r1")
+    out.order[0], out.order[1] = int(g("o0")), int(g("o1"))
+    out.l, out.zR[0], out.zR[1] = g("l"), g("zR0"), g("zR1")
+    sg = out.signal
+    sg.type = int(g("sig_type"))
+    sg.t0, sg.s, sg.f0, sg.cep, sg.nR = g("sig_t0"), g("sig_s"), g("sig_f0"), g("sig_cep"), g("sig_nR")
+    sg.sig0, sg.sig1 = g("sig_g0"), g("sig_g1")
+    return out
+
+
+def seed_params(m: dict) -> MoSeed | None:
+    """The seed, or None when it injects nothing (|amplitude| <= 1e-50, src/fdtd.cpp:307)."""
+    if abs(m.get("seed_amp", 0.0)) <= 1.0e-50:
+        return None
+    sd = MoSeed()
+    beam_params(m, "seed_", sd.beam)
+    sd.gamma, sd.beta, sd.c0, sd.dt = m["seed_gamma"], m["seed_beta"], m["seed_c0"], m["seed_dt"]
+    return sd
+
+
 def field_params(m: dict, solver: int, order: int, space_charge: int = 0) -> MoField:
     f = MoField()
     f.N0, f.N1, f.np, f.k0 = int(m["N0"]), int(m["N1"]), int(m["np"]), int(m.get("k0", 0))
@@ -152,6 +202,7 @@ def field_params(m: dict, solver: int, order: int, space_charge: int = 0) -> MoF
     for i in range(17):
         f.hC[i] = m["hC%d" % i]
     f.dt, f.dx, f.dy, f.dz = m["dt"], m["dx"], m["dy"], m["dz"]
+    f.xmin, f.ymin, f.zmin = m["xmin"], m["ymin"], m["zmin"]
     return f
 
 
@@ -170,6 +221,13 @@ def push_params(m: dict) -> MoPush:
         U.type = int(m["und%d_type" % u])
         U.k, U.lu, U.rb = m["und%d_k" % u], m["und%d_lu" % u], m["und%d_rb" % u]
         U.length, U.dist, U.theta = m["und%d_length" % u], m["und%d_dist" % u], m["und%d_theta" % u]
+        if U.type == 1:
+            beam_params(m, "und%d_beam_" % u, U.beam)
+    p.n_ext = int(m.get("n_ext", 0))
+    if p.n_ext > MO_MAX_EXT:
+        raise ValueError("at most %d external fields" % MO_MAX_EXT)
+    for x in range(p.n_ext):
+        beam_params(m, "ext%d_" % x, p.ext[x])
     return p
 
 
@@ -226,6 +284,7 @@ class OracleRun:
         self.m = dict(meta)
         self.sc = fn is not None
         self.f = field_params(meta, solver, order, 1 if self.sc else 0)
+        self.seed = seed_params(meta)
         self.p = push_params(meta)
         self.d = deposit_params(meta)
         nodes = int(meta["N0"]) * int(meta["N1"]) * int(meta["np"])
@@ -258,7 +317,11 @@ class OracleRun:
         return self.rec[: self.n]
 
     def field_update(self):
-        lib().mo_field_update(C.byref(self.f), dptr(self.anp1), dptr(self.an), dptr(self.anm1))
+        if self.seed is not None:
+            lib().mo_field_update_seeded(C.byref(self.f), C.byref(self.seed), self.time, dptr(self.anp1),
+                                         dptr(self.an), dptr(self.anm1))
+        else:
+            lib().mo_field_update(C.byref(self.f), dptr(self.anp1), dptr(self.an), dptr(self.anm1))
         if self.sc:
             lib().mo_scalar_update(C.byref(self.f), dptr(self.fnp1), dptr(self.fn), dptr(self.fnm1))
 

@@ -93,6 +93,31 @@ static void load_particles(const std::string& path, std::list<Charge>& q) {
 
 static void meta_line(FILE* f, const char* k, double v) { fprintf(f, "%s %.17g\n", k, v); }
 
+/* The laser-beam members shared by Seed, Undulator and ExtField (src/classes.h:201-462). */
+template <class B>
+static void beam_meta(FILE* f, const std::string& p, B& b) {
+  auto kv = [&](const std::string& k, double v) { meta_line(f, (p + k).c_str(), v); };
+  kv("type", (double)b.seedType_);
+  for (int c = 0; c < 3; c++) {
+    kv("pos" + std::to_string(c), b.position_[c]);
+    kv("dir" + std::to_string(c), b.direction_[c]);
+    kv("pol" + std::to_string(c), b.polarization_[c]);
+  }
+  kv("amp", b.amplitude_);
+  kv("r0", b.radius_.size() > 0 ? b.radius_[0] : 0.0);
+  kv("r1", b.radius_.size() > 1 ? b.radius_[1] : 0.0);
+  kv("o0", b.order_.size() > 0 ? b.order_[0] : 0);
+  kv("o1", b.order_.size() > 1 ? b.order_[1] : 0);
+  kv("l", b.l_);
+  kv("zR0", b.zR_.size() > 0 ? b.zR_[0] : 0.0);
+  kv("zR1", b.zR_.size() > 1 ? b.zR_[1] : 0.0);
+  kv("sig_type", (double)b.signal_.signalType_);
+  kv("sig_t0", b.signal_.t0_); kv("sig_s", b.signal_.s_); kv("sig_f0", b.signal_.f0_);
+  kv("sig_cep", b.signal_.cep_); kv("sig_nR", (double)b.signal_.nR_);
+  kv("sig_g0", b.signal_.sigmaInvG_.size() > 0 ? b.signal_.sigmaInvG_[0] : 0.0);
+  kv("sig_g1", b.signal_.sigmaInvG_.size() > 1 ? b.signal_.sigmaInvG_[1] : 0.0);
+}
+
 static void dump_meta(Solver* s, const std::string& path) {
   FILE* f = fopen(path.c_str(), "w");
   meta_line(f, "N0", s->N0_); meta_line(f, "N1", s->N1_); meta_line(f, "N2", s->N2_); meta_line(f, "np", s->np_);
@@ -135,7 +160,13 @@ static void dump_meta(Solver* s, const std::string& path) {
     snprintf(k, 64, "und%zu_dist", u); meta_line(f, k, s->undulator_[u].dist_);
     snprintf(k, 64, "und%zu_theta", u); meta_line(f, k, s->undulator_[u].theta_);
     snprintf(k, 64, "und%zu_type", u); meta_line(f, k, (double)s->undulator_[u].type_);
+    if (s->undulator_[u].type_ == OPTICAL) beam_meta(f, "und" + std::to_string(u) + "_beam_", s->undulator_[u]);
   }
+  beam_meta(f, "seed_", s->seed_);
+  meta_line(f, "seed_gamma", s->seed_.gamma_); meta_line(f, "seed_beta", s->seed_.beta_);
+  meta_line(f, "seed_c0", s->seed_.c0_); meta_line(f, "seed_dt", s->seed_.dt_);
+  meta_line(f, "n_ext", (double)s->extField_.size());
+  for (size_t x = 0; x < s->extField_.size(); x++) beam_meta(f, "ext" + std::to_string(x) + "_", s->extField_[x]);
   meta_line(f, "n_particles", (double)s->chargeVectorn_.size());
   meta_line(f, "n_fel", (double)s->FEL_.size());
   for (size_t j = 0; j < s->FEL_.size(); j++) {

@@ -121,6 +121,9 @@ def main():
     fixtures_for(harness, "kat-small.job", "kat-small-fd")
     fixtures_for(harness, "kat-small-nsfd.job", "kat-small-nsfd")
     fixtures_for(harness, "kat-small-sc.job", "kat-small-sc", with_kats=False)
+    fixtures_for(harness, "kat-small-seed.job", "kat-small-seed", with_kats=False)
+    fixtures_for(harness, "kat-small-ext.job", "kat-small-ext", with_kats=False)
+    fixtures_for(harness, "kat-small-optical.job", "kat-small-optical", with_kats=False)
     print("golden vectors written to", OUT)
 
 

@@ -3,14 +3,14 @@ import numpy as np
 import pytest
 
 import mithra_gb300 as mg
-from tests._golden import TAGS, load, meta
+from tests._golden import BEAM_TAGS, TAGS, load, meta
 from tests.conftest import job
 
 
-@pytest.mark.parametrize("tag", sorted(TAGS))
+@pytest.mark.parametrize("tag", sorted(TAGS) + sorted(BEAM_TAGS))
 def test_setup_matches_reference(tag):
     ref = meta(tag)
-    s = mg.Setup.from_job(job(TAGS[tag][0]))
+    s = mg.Setup.from_job(job({**TAGS, **BEAM_TAGS}[tag][0]))
     m = s.meta()
     for k, v in ref.items():
         assert k in m, k
@@ -58,3 +58,11 @@ def test_space_charge_setup_matches_reference():
         assert m[k] == v, k
     assert s.grid().space_charge == 1
     assert np.array_equal(s.particles(), z["particles"])
+
+
+def test_seed_fill_matches_reference():
+    """Initial seed fill of A^n and A^{n-1} (src/solver.cpp:828-839) from the host set-up."""
+    z = load("kat-small-seed", "init")
+    anp1, an, anm1 = mg.Setup.from_job(job("kat-small-seed.job")).fields()
+    assert np.abs(z["an"]).max() > 0
+    assert np.array_equal(an, z["an"]) and np.array_equal(anm1, z["anm1"])

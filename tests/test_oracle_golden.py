@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from tests._golden import TAGS, load, meta
+from tests._golden import BEAM_TAGS, TAGS, load, meta
 
 
 @pytest.mark.parametrize("tag", sorted(TAGS))
@@ -99,3 +99,31 @@ def test_oracle_space_charge_march_matches_reference():
                  (r.fnp1, "fnp1_12"), (r.particles, "particles12")):
         assert np.array_equal(a, run[b]), b
     assert np.abs(r.fn).max() > 0
+
+
+@pytest.mark.parametrize("tag", sorted(BEAM_TAGS))
+def test_oracle_beam_march_matches_reference(tag):
+    """Seed injection through the TF/SF planes, external laser fields and the optical undulator:
+    12 steps against the reference's own run, bit for bit."""
+    m = meta(tag)
+    init, run = load(tag, "init"), load(tag, "run")
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=BEAM_TAGS[tag][1], order=2)
+    for step in range(1, 13):
+        r.step()
+        zl, pg = r.power_rows[-1]
+        row = np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)]))
+        assert np.array_equal(row, run["power"][step - 1]), "power row %d" % step
+    for a, b in ((r.an, "an12"), (r.anm1, "anm1_12"), (r.anp1, "anp1_12"), (r.particles, "particles12")):
+        assert np.array_equal(a, run[b]), b
+
+
+def test_oracle_seed_injection_is_active():
+    """The seed job's march differs from the same march without the injection."""
+    tag = "kat-small-seed"
+    m = meta(tag)
+    init, run = load(tag, "init"), load(tag, "run")
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=1, order=2)
+    r.seed = None
+    for _ in range(12):
+        r.step()
+    assert not np.array_equal(r.an, run["an12"])
