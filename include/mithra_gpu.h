@@ -40,6 +40,7 @@ extern "C" {
 
 #define MITHRA_MAX_UNDULATORS 64
 #define MITHRA_MAX_POWER_OUTPUTS 8
+#define MITHRA_MAX_EXT_FIELDS 16
 
 typedef struct mithra_ctx mithra_ctx;
 
@@ -72,10 +73,36 @@ typedef struct {
   double n_update_bunch;       /* nUpdateBunch_ (the substep loop runs while t < this) */
 } mithra_push_desc;
 
-/* One undulator module after Solver::setSimulationParameters (sorted, rb shifted). */
+/* A laser beam after Seed/Undulator/ExtField::initialize (src/classes.cpp:646-735, :1007-1075,
+ * :1162-1260): the members of those classes that the field evaluation reads. */
+typedef struct {
+  int32_t type;                /* SeedType: 0 plane-wave, 1 truncated plane-wave, 2 gaussian,
+                                  3 super-gaussian, 4..7 the standing variants of 0..3 */
+  double position[3], direction[3], polarization[3];
+  double amplitude;            /* amplitude_ */
+  double radius[2];            /* radius_ */
+  int32_t order[2];            /* order_ */
+  double wavelength;           /* l_ */
+  double rayleigh[2];          /* zR_ */
+  int32_t signal_type;         /* 0 neumann, 1 gaussian, 2 secant-hyperbolic, 3 flat-top,
+                                  4 inverse-gaussian */
+  double signal_t0, signal_s, signal_f0, signal_cep, signal_nr;  /* Signal t0_, s_, f0_, cep_, nR_ */
+  double signal_sigma[2];      /* Signal sigmaInvG_ */
+} mithra_beam_desc;
+
+/* The seed of FdTd::fieldUpdate's TF/SF injection (src/fdtd.cpp:307-373, Seed::fields
+ * src/classes.cpp:740-855) with the frame members of Seed. */
+typedef struct {
+  mithra_beam_desc beam;
+  double gamma, beta, c0, dt;  /* Seed gamma_, beta_, c0_, dt_ */
+} mithra_seed_desc;
+
+/* One undulator module after Solver::setSimulationParameters (sorted, rb shifted).  An optical
+ * undulator (type 1) also carries its laser beam. */
 typedef struct {
   int32_t type;                /* 0 static, 1 optical */
   double k, lu, rb, length, dist, theta;
+  mithra_beam_desc beam;       /* used when type == 1 */
 } mithra_undulator_desc;
 
 /* One radiation-power output (src/radiation.cpp:18-121). */
@@ -108,6 +135,13 @@ int mithra_gpu_synchronize(mithra_ctx* ctx);
 
 /* Undulator modules, replacing the parsed std::vector<Undulator> (src/solver.h:224). */
 int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und, int n);
+/* The seed injected through the total-field/scattered-field planes every field update
+ * (Solver::seed_, src/solver.h:223; src/fdtd.cpp:307-373).  An amplitude not above 1e-50, or
+ * seed == NULL, injects nothing, as in the reference. */
+int mithra_gpu_set_seed(mithra_ctx* ctx, const mithra_seed_desc* seed);
+/* External laser fields acting on the particles (Solver::extField_, src/solver.h:225;
+ * Solver::externalField, src/solver.cpp:1886-1947).  At most MITHRA_MAX_EXT_FIELDS. */
+int mithra_gpu_set_external_fields(mithra_ctx* ctx, const mithra_beam_desc* fields, int n);
 /* Radiation-power outputs, replacing Solver::initializePowerSample's rp_ (src/radiation.cpp:18-121). */
 int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outputs, int n);
 
@@ -201,6 +235,8 @@ int mithra_setup_destroy(mithra_setup* s);
 int mithra_setup_grid(const mithra_setup* s, mithra_grid_desc* grid);
 int mithra_setup_push(const mithra_setup* s, mithra_push_desc* push);
 int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, int cap, int* n);
+int mithra_setup_seed(const mithra_setup* s, mithra_seed_desc* seed);
+int mithra_setup_external_fields(const mithra_setup* s, mithra_beam_desc* fields, int cap, int* n);
 int mithra_setup_time(const mithra_setup* s, mithra_time_state* t);
 int mithra_setup_particles(const mithra_setup* s, double* rec, size_t cap, size_t* n);
 int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double* anm1);

@@ -25,6 +25,7 @@ __all__ = ["Setup", "Context", "FdTd", "FdTdSC", "MithraError", "PinnedArray", "
 FP64 = 0
 FP32 = 1
 MAX_UND = 64
+MAX_EXT = 16
 
 
 class MithraError(RuntimeError):
@@ -50,9 +51,23 @@ class PushDesc(C.Structure):
                 ("n_update_bunch", C.c_double)]
 
 
+class BeamDesc(C.Structure):
+    _fields_ = [("type", C.c_int32), ("position", C.c_double * 3), ("direction", C.c_double * 3),
+                ("polarization", C.c_double * 3), ("amplitude", C.c_double), ("radius", C.c_double * 2),
+                ("order", C.c_int32 * 2), ("wavelength", C.c_double), ("rayleigh", C.c_double * 2),
+                ("signal_type", C.c_int32), ("signal_t0", C.c_double), ("signal_s", C.c_double),
+                ("signal_f0", C.c_double), ("signal_cep", C.c_double), ("signal_nr", C.c_double),
+                ("signal_sigma", C.c_double * 2)]
+
+
+class SeedDesc(C.Structure):
+    _fields_ = [("beam", BeamDesc), ("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double),
+                ("dt", C.c_double)]
+
+
 class UndulatorDesc(C.Structure):
     _fields_ = [("type", C.c_int32), ("k", C.c_double), ("lu", C.c_double), ("rb", C.c_double),
-                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double)]
+                ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double), ("beam", BeamDesc)]
 
 
 class PowerDesc(C.Structure):
@@ -76,6 +91,8 @@ _SIGS = {
     "mithra_gpu_last_error": [_vp, C.c_char_p, C.c_size_t],
     "mithra_gpu_synchronize": [_vp],
     "mithra_gpu_set_undulators": [_vp, _P(UndulatorDesc), C.c_int],
+    "mithra_gpu_set_seed": [_vp, C.c_void_p],
+    "mithra_gpu_set_external_fields": [_vp, _P(BeamDesc), C.c_int],
     "mithra_gpu_set_power": [_vp, _P(PowerDesc), C.c_int],
     "mithra_gpu_upload_fields": [_vp, _dp, _dp, _dp],
     "mithra_gpu_download_fields": [_vp, _dp, _dp, _dp],
@@ -111,6 +128,8 @@ _SIGS = {
     "mithra_setup_grid": [_vp, _P(GridDesc)],
     "mithra_setup_push": [_vp, _P(PushDesc)],
     "mithra_setup_undulators": [_vp, _P(UndulatorDesc), C.c_int, _P(C.c_int)],
+    "mithra_setup_seed": [_vp, _P(SeedDesc)],
+    "mithra_setup_external_fields": [_vp, _P(BeamDesc), C.c_int, _P(C.c_int)],
     "mithra_setup_time": [_vp, _P(TimeState)],
     "mithra_setup_particles": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_fields": [_vp, _dp, _dp, _dp],
@@ -203,6 +222,17 @@ class Setup:
         p = PushDesc()
         lib().mithra_setup_push(self._h, C.byref(p))
         return p
+
+    def seed(self) -> "SeedDesc":
+        sd = SeedDesc()
+        lib().mithra_setup_seed(self._h, C.byref(sd))
+        return sd
+
+    def external_fields(self):
+        arr = (BeamDesc * MAX_EXT)()
+        n = C.c_int()
+        lib().mithra_setup_external_fields(self._h, arr, MAX_EXT, C.byref(n))
+        return [arr[i] for i in range(n.value)]
 
     def undulators(self):
         arr = (UndulatorDesc * MAX_UND)()
@@ -298,6 +328,14 @@ class Context:
     def set_undulators(self, und):
         arr = (UndulatorDesc * max(1, len(und)))(*und)
         self.call("mithra_gpu_set_undulators", arr, len(und))
+
+    def set_seed(self, seed):
+        """The TF/SF seed (a SeedDesc), or None for none."""
+        self.call("mithra_gpu_set_seed", C.byref(seed) if seed is not None else None)
+
+    def set_external_fields(self, fields):
+        arr = (BeamDesc * max(1, len(fields)))(*fields)
+        self.call("mithra_gpu_set_external_fields", arr, len(fields))
 
     def set_power(self, outputs):
         """outputs: list of dicts with N, Nl, Nf, pc, z, tw_re, tw_im (numpy float64)."""

@@ -61,6 +61,11 @@ struct mithra_ctx {
   mithra_push_desc push_desc{};
   std::vector<mithra::UndDev> und_host;
   mithra::UndDev* und_dev = nullptr;
+  std::vector<mithra::BeamDev> opt_beams;  // laser beams of the optical undulators, in module order
+  std::vector<mithra::BeamDev> ext_beams;  // external fields
+  mithra::BeamDev* beams_dev = nullptr;    // opt_beams then ext_beams
+  mithra::SeedDev seed{};
+  bool seed_active = false;
   double* A[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of A (SoA)
   double* F[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of phi
   mithra::ParticlesDev<double> pt{};
@@ -134,6 +139,9 @@ int timed(mithra_ctx* ctx, const char* name, Fn fn) {
   if (ctx->timing) return timer_end(ctx, slot, a, b);
   return MITHRA_OK;
 }
+
+// TF/SF injection of the seed into the new vector potential (float or double storage).
+int stage_seed(mithra_ctx* ctx, void* anp1);
 
 // Mixed-precision form (fp32_form.cu).
 int fp32_alloc(mithra_ctx* ctx);

@@ -36,8 +36,32 @@ __host__ __device__ inline long long node_index(const GridDev& g, int k, int i, 
   return (long long)k * g.plane + (long long)i * g.P1 + j;
 }
 
+// Laser beams (evaluated in beam_fields.cuh).
+struct SignalDev {  // Signal (src/classes.h:159-195); cep in radians, f0 = 1 / wavelength
+  int type;         // 0 neumann, 1 gaussian, 2 secant-hyperbolic, 3 flat-top, 4 inverse-gaussian
+  double t0, s, f0, cep, nR, g0, g1;
+};
+
+struct BeamDev {  // the laser-beam members shared by Seed, Undulator and ExtField
+  int type;       // SeedType: 0 plane, 1 truncated plane, 2 gaussian, 3 super-gaussian, 4..7 standing
+  double pos[3], dir[3], pol[3];
+  double yv[3];   // cross(direction, polarization)
+  double amplitude, r0, r1;
+  int o0, o1;
+  double l, zR0, zR1;
+  SignalDev sig;
+};
+
+struct SeedDev {
+  BeamDev b;
+  double gamma, beta, c0, dt;  // Seed::gamma_, beta_, c0_, dt_
+  double l, zRp, zRs;          // c0 / f0 and the two Rayleigh lengths of Seed::fields
+  double a1, a2, a3;           // uf_.a[1..3], the TF/SF coefficients
+};
+
 struct UndDev {
   int type;
+  int beam;  // optical modules: index of the laser beam in PushDev::beams, else -1
   double k, lu, rb, length, dist, theta;
   // Per-module constants of Solver::undulatorField (src/solver.cpp:1805-1812), computed on
   // the host with the reference's expressions so that they are bit-identical.
@@ -53,6 +77,10 @@ struct PushDev {
   double inv_r2;  // 1 / r2
   int n_und;
   double und0_dist;
+  // Laser beams acting on the particles: optical undulators (indexed by UndDev::beam) and,
+  // from ext0 on, the n_ext external fields.
+  const BeamDev* beams;
+  int ext0, n_ext, n_opt;
 };
 
 // Device-resident time and bookkeeping state of one context.  The kernels advance it

@@ -26,6 +26,8 @@ PushF32 push_constants(const mithra_ctx* ctx) {
   C.und0_dist = P.und0_dist;
   C.gamma_f = (float)P.gamma; C.bc_f = (float)(P.beta * P.c0); C.gdz = (float)(P.gamma * g.dz);
   C.zmin_f = (float)g.zmin; C.dz_f = (float)g.dz; C.und0_dist_f = (float)P.und0_dist;
+  C.P64 = P;
+  C.xmin_d = g.xmin; C.ymin_d = g.ymin; C.dxd = g.dx; C.dyd = g.dy;
   return C;
 }
 
@@ -106,6 +108,7 @@ int run_potential_f32(mithra_ctx* ctx, PotentialArgs<float> p, bool vector) {
     r = timed(ctx, vector ? "potential_interior_fd" : "scalar_interior_fd",
               [&] { k_potential_interior<float, false><<<grd, blk, 0, ctx->stream>>>(g, p); });
   if (r) return r;
+  if (vector && ctx->seed_active && (r = stage_seed(ctx, p.np1))) return r;
   r = timed(ctx, vector ? "potential_faces" : "scalar_faces", [&] {
     k_potential_faces<float><<<grid_stride_blocks(ctx, nfaces, 256), 256, 0, ctx->stream>>>(g, p);
   });

@@ -6,6 +6,7 @@
 // phase ku*lz must be exact to ~1e-7 rad) is formed and range-reduced in FP64, and the time
 // state stays FP64.  Everything else runs on the FP32 pipes.
 #pragma once
+#include "beam_fields.cuh"
 #include "device_common.cuh"
 
 namespace mithra {
@@ -69,6 +70,8 @@ struct PushF32 {
   double und0_dist;
   float gamma_f, bc_f, gdz;      // gamma, beta*c0 and gamma*dz in FP32
   float zmin_f, dz_f, und0_dist_f;
+  PushDev P64;                   // FP64 parameters for the laser beams (optical undulators, external fields)
+  double xmin_d, ymin_d, dxd, dyd;
 };
 
 // Static undulator field (src/solver.cpp:1798-1824, src/beam.cc:14-76).
@@ -192,6 +195,17 @@ __global__ void __launch_bounds__(256) k_push_f32(PushF32 C, const UndDev* __res
       const bool k_in = (k >= 0 && k <= C.N2);
       const double zd_slow = k_in ? 0.0 : C.zmin + ((double)k + (double)fz) * C.dzd;
       undulator_f32(und, table, C.n_und, C.N2, C.gdz, k, fz, zd_slow, tshift, C.gamma, x, y, bt, et, C.gamma_f, C.bc_f);
+      if (C.P64.n_opt + C.P64.n_ext > 0) {
+        // Laser beams in FP64: their phase, like the undulator's, is a large lab-frame coordinate.
+        const double xd = C.xmin_d + ((double)i + (double)fx) * C.dxd;
+        const double yd = C.ymin_d + ((double)j + (double)fy) * C.dyd;
+        const double zd = C.zmin + ((double)k + (double)fz) * C.dzd;
+        double b64[3] = {0.0, 0.0, 0.0}, e64[3] = {0.0, 0.0, 0.0};
+        for (int u = 0; u < C.n_und; u++)
+          if (und[u].type == 1 && und[u].beam >= 0) beam_add(C.P64.beams[und[u].beam], C.P64, tb, xd, yd, zd, b64, e64);
+        for (int xf = 0; xf < C.P64.n_ext; xf++) beam_add(C.P64.beams[C.P64.ext0 + xf], C.P64, tb, xd, yd, zd, b64, e64);
+        for (int c = 0; c < 3; c++) { bt[c] += (float)b64[c]; et[c] += (float)e64[c]; }
+      }
       uint8_t e = pt.e[p];
       if (e) {
         if (b1x && b1y && b1z) {

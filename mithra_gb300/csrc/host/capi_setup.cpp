@@ -55,6 +55,50 @@ int mithra_setup_push(const mithra_setup* s, mithra_push_desc* p) {
   return MITHRA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+mithra_beam_desc beam_desc(const mithra::host::Beam& b) {
+  mithra_beam_desc d{};
+  d.type = (int32_t)b.seedType;
+  for (int c = 0; c < 3; c++) {
+    d.position[c] = b.position[c];
+    d.direction[c] = b.direction[c];
+    d.polarization[c] = b.polarization[c];
+  }
+  d.amplitude = b.amplitude;
+  for (int c = 0; c < 2; c++) {
+    d.radius[c] = c < (int)b.radius.size() ? b.radius[c] : 0.0;
+    d.order[c] = c < (int)b.order.size() ? b.order[c] : 0;
+    d.rayleigh[c] = c < (int)b.zR.size() ? b.zR[c] : 0.0;
+    d.signal_sigma[c] = c < (int)b.signal.sigmaInvG.size() ? b.signal.sigmaInvG[c] : 0.0;
+  }
+  d.wavelength = b.l;
+  d.signal_type = (int32_t)b.signal.type;
+  d.signal_t0 = b.signal.t0; d.signal_s = b.signal.s; d.signal_f0 = b.signal.f0;
+  d.signal_cep = b.signal.cep; d.signal_nr = (double)b.signal.nR;
+  return d;
+}
+}  // namespace
+
+extern "C" {
+
+int mithra_setup_seed(const mithra_setup* s, mithra_seed_desc* seed) {
+  if (!s || !seed) return MITHRA_ERR_ARG;
+  const auto& S = s->s.job.seed;
+  seed->beam = beam_desc(S);
+  seed->gamma = S.gamma; seed->beta = S.beta; seed->c0 = S.c0; seed->dt = S.dt;
+  return MITHRA_OK;
+}
+
+int mithra_setup_external_fields(const mithra_setup* s, mithra_beam_desc* fields, int cap, int* n) {
+  if (!s || !n) return MITHRA_ERR_ARG;
+  const auto& X = s->s.job.extFields;
+  *n = (int)X.size();
+  for (int x = 0; x < std::min<int>(cap, (int)X.size()); x++) fields[x] = beam_desc(X[x]);
+  return MITHRA_OK;
+}
+
 int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, int cap, int* n) {
   if (!s || !n) return MITHRA_ERR_ARG;
   const auto& U = s->s.job.undulators;
@@ -67,6 +111,7 @@ int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, i
     und[u].length = (double)U[u].length;
     und[u].dist = U[u].dist;
     und[u].theta = U[u].theta;
+    und[u].beam = beam_desc(U[u]);
   }
   return MITHRA_OK;
 }
@@ -143,6 +188,14 @@ int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int devic
   int nu = 0;
   if ((r = mithra_setup_undulators(s, und.data(), (int)und.size(), &nu))) return bail(r);
   if ((r = mithra_gpu_set_undulators(ctx, und.data(), nu))) return bail(r);
+  mithra_seed_desc seed;
+  if ((r = mithra_setup_seed(s, &seed)) || (r = mithra_gpu_set_seed(ctx, &seed))) return bail(r);
+  std::vector<mithra_beam_desc> ext(S.job.extFields.size());
+  int nx = 0;
+  if ((r = mithra_setup_external_fields(s, ext.data(), (int)ext.size(), &nx))) return bail(r);
+  if (nx > MITHRA_MAX_EXT_FIELDS)
+    return bail(MITHRA_ERR_ARG);
+  if ((r = mithra_gpu_set_external_fields(ctx, ext.data(), nx))) return bail(r);
   std::vector<mithra_power_desc> pw;
   for (const auto& pc : S.power) {
     mithra_power_desc d;

@@ -122,6 +122,7 @@ int run_potential(mithra_ctx* ctx, PotentialArgs<double> p, bool vector) {
     r = timed(ctx, vector ? "potential_interior_fd" : "scalar_interior_fd",
               [&] { k_potential_interior<double, false><<<grd, blk, 0, ctx->stream>>>(g, p); });
   if (r) return r;
+  if (vector && ctx->seed_active && (r = stage_seed(ctx, p.np1))) return r;
   r = timed(ctx, vector ? "potential_faces" : "scalar_faces", [&] {
     k_potential_faces<double><<<grid_stride_blocks(ctx, nfaces, 256), 256, 0, ctx->stream>>>(g, p);
   });
@@ -284,6 +285,40 @@ int ensure_rows(mithra_ctx* ctx, long long extra) {
   return MITHRA_OK;
 }
 
+BeamDev beam_from_desc(const mithra_beam_desc& d) {
+  BeamDev b{};
+  b.type = d.type;
+  for (int c = 0; c < 3; c++) { b.pos[c] = d.position[c]; b.dir[c] = d.direction[c]; b.pol[c] = d.polarization[c]; }
+  // cross(direction, polarization), src/fieldvector.h:197-204
+  b.yv[0] = b.dir[1] * b.pol[2] - b.dir[2] * b.pol[1];
+  b.yv[1] = b.dir[2] * b.pol[0] - b.dir[0] * b.pol[2];
+  b.yv[2] = b.dir[0] * b.pol[1] - b.dir[1] * b.pol[0];
+  b.amplitude = d.amplitude; b.r0 = d.radius[0]; b.r1 = d.radius[1]; b.o0 = d.order[0]; b.o1 = d.order[1];
+  b.l = d.wavelength; b.zR0 = d.rayleigh[0]; b.zR1 = d.rayleigh[1];
+  b.sig.type = d.signal_type; b.sig.t0 = d.signal_t0; b.sig.s = d.signal_s; b.sig.f0 = d.signal_f0;
+  b.sig.cep = d.signal_cep; b.sig.nR = d.signal_nr; b.sig.g0 = d.signal_sigma[0]; b.sig.g1 = d.signal_sigma[1];
+  return b;
+}
+
+// Uploads the module table and the laser beams (optical undulators first, then the external
+// fields) and points the push parameters at them.
+int upload_beams(mithra_ctx* ctx) {
+  std::vector<BeamDev> all(ctx->opt_beams);
+  all.insert(all.end(), ctx->ext_beams.begin(), ctx->ext_beams.end());
+  PushDev& P = ctx->P;
+  P.n_opt = (int)ctx->opt_beams.size();
+  P.ext0 = P.n_opt;
+  P.n_ext = (int)ctx->ext_beams.size();
+  P.beams = all.empty() ? nullptr : ctx->beams_dev;
+  if (!all.empty())
+    CK(cudaMemcpyAsync(ctx->beams_dev, all.data(), all.size() * sizeof(BeamDev), cudaMemcpyHostToDevice, ctx->stream));
+  if (P.n_und)
+    CK(cudaMemcpyAsync(ctx->und_dev, ctx->und_host.data(), P.n_und * sizeof(UndDev), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  invalidate_graphs(ctx);
+  return MITHRA_OK;
+}
+
 int check_state(mithra_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
@@ -299,6 +334,27 @@ int check_state(mithra_ctx* ctx) {
 }
 
 }  // namespace
+
+namespace mithra {
+
+int stage_seed(mithra_ctx* ctx, void* anp1) {
+  const GridDev& g = ctx->g;
+  if (g.N0 < 5 || g.N1 < 5 || g.N2 < 5) return MITHRA_OK;  // no TF/SF planes inside the domain
+  for (int dir = 0; dir < 3; dir++) {
+    const long long items = (long long)((dir == 0) ? g.N1 - 4 : g.N0 - 4) * ((dir == 2) ? g.N1 - 4 : g.N2 - 4);
+    const int blocks = grid_stride_blocks(ctx, items, 256);
+    int r = timed(ctx, "seed_inject", [&] {
+      if (ctx->precision == MITHRA_PRECISION_FP64)
+        k_seed_inject<double><<<blocks, 256, 0, ctx->stream>>>(g, ctx->seed, (double*)anp1, ctx->st, dir);
+      else
+        k_seed_inject<float><<<blocks, 256, 0, ctx->stream>>>(g, ctx->seed, (float*)anp1, ctx->st, dir);
+    });
+    if (r) return r;
+  }
+  return MITHRA_OK;
+}
+
+}  // namespace mithra
 
 
 // ---- C ABI ----------------------------------------------------------------------------------
@@ -349,7 +405,9 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
     P.dtb = pd->dtb; P.r1 = pd->r1; P.r2 = pd->r2; P.gamma = pd->gamma; P.beta = pd->beta; P.c0 = pd->c0;
     P.dt_shift = pd->dt_shift; P.bunch_time_step = pd->bunch_time_step; P.n_und = 0; P.und0_dist = 0.0;
     P.inv_r2 = 1.0 / pd->r2;
+    P.beams = nullptr; P.ext0 = 0; P.n_ext = 0; P.n_opt = 0;
     CK(dalloc(&ctx->und_dev, kMaxUndulators));
+    CK(dalloc(&ctx->beams_dev, kMaxUndulators + MITHRA_MAX_EXT_FIELDS));
     const size_t nf = (size_t)3 * g.cstride;
     ctx->capacity = std::max<size_t>(particle_capacity, 1);
     if (precision == MITHRA_PRECISION_FP64) {
@@ -419,7 +477,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   fp32_free(ctx);
   cudaFree(ctx->staging);
   cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
-  cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev);
+  cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
     void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
@@ -441,6 +499,7 @@ int mithra_gpu_synchronize(mithra_ctx* ctx) {
 int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und, int n) {
   if (!ctx || n < 0 || n > MITHRA_MAX_UNDULATORS || (n && !und)) return MITHRA_ERR_ARG;
   ctx->und_host.assign(n, UndDev{});
+  ctx->opt_beams.clear();
   const double c0 = ctx->P.c0;
   for (int u = 0; u < n; u++) {
     UndDev& U = ctx->und_host[u];
@@ -458,6 +517,11 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
     if (u + 1 < n) U.r0_next = und[u + 1].rb - U.rb - U.length * U.lu;                  // src/beam.cc:60
     U.ct_f = (float)U.ct; U.st_f = (float)U.st; U.ku_f = (float)U.ku; U.b0_f = (float)U.b0; U.ul_f = (float)U.ul;
     U.r0_prev_f = (float)U.r0_prev; U.r0_next_f = (float)U.r0_next;
+    U.beam = -1;
+    if (U.type == 1) {
+      U.beam = (int)ctx->opt_beams.size();
+      ctx->opt_beams.push_back(beam_from_desc(und[u].beam));
+    }
   }
   if (ctx->precision == MITHRA_PRECISION_FP32) {
     cudaFree(ctx->und_table);
@@ -466,10 +530,37 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
   }
   ctx->P.n_und = n;
   ctx->P.und0_dist = n ? und[0].dist : 0.0;
-  if (n) CK(cudaMemcpyAsync(ctx->und_dev, ctx->und_host.data(), n * sizeof(UndDev), cudaMemcpyHostToDevice, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  return upload_beams(ctx);
+}
+
+int mithra_gpu_set_seed(mithra_ctx* ctx, const mithra_seed_desc* sd) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  ctx->seed_active = sd && fabs(sd->beam.amplitude) > 1.0e-50;  // src/fdtd.cpp:307
+  if (!ctx->seed_active) {
+    invalidate_graphs(ctx);
+    return MITHRA_OK;
+  }
+  if (sd->beam.type < 0 || sd->beam.type > 7) return fail(ctx, MITHRA_ERR_ARG, "seed beam type %d", sd->beam.type);
+  SeedDev& S = ctx->seed;
+  S.b = beam_from_desc(sd->beam);
+  S.gamma = sd->gamma; S.beta = sd->beta; S.c0 = sd->c0; S.dt = sd->dt;
+  // Seed::fields, src/classes.cpp:790-796: wavelength and Rayleigh lengths (same expressions).
+  S.l = S.c0 / S.b.sig.f0;
+  S.zRp = kPI * S.b.r0 * S.b.r0 / S.l;
+  S.zRs = kPI * S.b.r1 * S.b.r1 / S.l;
+  S.a1 = ctx->g.a[1]; S.a2 = ctx->g.a[2]; S.a3 = ctx->g.a[3];
   invalidate_graphs(ctx);
   return MITHRA_OK;
+}
+
+int mithra_gpu_set_external_fields(mithra_ctx* ctx, const mithra_beam_desc* fields, int n) {
+  if (!ctx || n < 0 || n > MITHRA_MAX_EXT_FIELDS || (n && !fields)) return MITHRA_ERR_ARG;
+  ctx->ext_beams.clear();
+  for (int x = 0; x < n; x++) {
+    if (fields[x].type < 0 || fields[x].type > 7) return fail(ctx, MITHRA_ERR_ARG, "external field %d: beam type %d", x, fields[x].type);
+    ctx->ext_beams.push_back(beam_from_desc(fields[x]));
+  }
+  return upload_beams(ctx);
 }
 
 int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) {

@@ -2,20 +2,24 @@
 // static-undulator field), the single-domain z-face exchange, particle erasure and the
 // zigzag current deposit.
 #pragma once
+#include "beam_fields.cuh"
 #include "device_common.cuh"
 
 namespace mithra {
 
-// Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
-// Solver::staticUndulator (src/beam.cc:14-76).  Adds the lab-frame undulator field, boosted
-// into the bunch frame, to bt/et.
+// Solver::undulatorField (src/solver.cpp:1798-1880): static modules with
+// Solver::staticUndulator (src/beam.cc:14-76), optical modules as laser beams.  Adds the lab-frame
+// undulator field, boosted into the bunch frame, to bt/et.
 __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
                                                        const PushDev& P, double timeBunch,
                                                        double x, double y, double z,
                                                        double* bt, double* et) {
   for (int u = 0; u < n_und; u++) {
     const UndDev& U = und[u];
-    if (U.type != 0) continue;
+    if (U.type != 0) {
+      if (U.type == 1 && U.beam >= 0) beam_add(P.beams[U.beam], P, timeBunch, x, y, z, bt, et);
+      continue;
+    }
     const double lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift)) - U.rb;
     const double ly = x * U.ct + y * U.st;
     double s_ly, c_ly;
@@ -84,6 +88,7 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         const bool b1z = (z < g.zp1 && z >= g.zp0);
         double bt[3] = {0.0, 0.0, 0.0}, et[3] = {0.0, 0.0, 0.0};
         static_undulator_field(und, P.n_und, P, timeBunch, x, y, z, bt, et);
+        for (int xf = 0; xf < P.n_ext; xf++) beam_add(P.beams[P.ext0 + xf], P, timeBunch, x, y, z, bt, et);
         double e = pt.e[p];
         if (e == 1.0) {
           if (b1x && b1y && b1z) {

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import mithra_gb300 as mg
-from tests._golden import TAGS, load, meta
+from tests._golden import BEAM_TAGS, TAGS, load, meta
 from tests.conftest import job, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -16,6 +16,7 @@ FIELD_STAGE_RTOL = 2e-6   # one field update in FP32, relative to max |A|
 PUSH_RTOL = 2e-5          # one push: E = (A^n - A^{n+1})/dt loses digits to cancellation in FP32
 DEPOSIT_RTOL = 5e-6       # relative L2 of J
 PSAT_RTOL = 0.01          # saturated (peak) radiated power of a full march vs the FP64 form
+BEAM_MARCH_RTOL = 2e-4    # A after 12 steps with seed / laser fields, relative L2 vs the reference
 
 
 def interior_mask(m):
@@ -91,3 +92,18 @@ def test_fp32_saturation_power_within_one_percent(gpu_available):
     psat64, psat32 = P64.max(), P32.max()
     assert psat64 > 0
     assert abs(psat32 - psat64) / psat64 <= PSAT_RTOL
+
+
+@pytest.mark.parametrize("tag", sorted(BEAM_TAGS))
+def test_fp32_beam_march(gpu_available, tag):
+    """Seed, external fields and optical undulator in the mixed form: laser phases in FP64,
+    fields in FP32; 12 steps against the reference's FP64 run."""
+    run = load(tag, "run")
+    ctx = mg.Context.from_setup(mg.Setup.from_job(job(BEAM_TAGS[tag][0])), mg.FP32)
+    ctx.run_prelude()
+    ctx.run(12)
+    anp1, an, anm1 = ctx.download_fields()
+    err = rel_l2(an, run["an12"])
+    print("%s: FP32 A relative L2 after 12 steps %.3e" % (tag, err))
+    assert err <= BEAM_MARCH_RTOL
+    assert ctx.download_particles().shape == run["particles12"].shape

@@ -9,7 +9,7 @@ import pytest
 
 import mithra_gb300 as mg
 from oracle import pyoracle as po
-from tests._golden import TAGS, load, meta
+from tests._golden import BEAM_TAGS, TAGS, load, meta
 from tests.conftest import job, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -169,5 +169,26 @@ def test_space_charge_march_matches_reference(gpu_available):
     assert rel_l2(fnm1, run["fnm1_12"]) <= MARCH_RTOL
     assert rel_l2(fnp1, run["fnp1_12"]) <= MARCH_RTOL
     assert np.abs(run["fn12"]).max() > 0
+    rows = ctx.power_rows().reshape(12, -1)
+    assert_close_scaled(rows, run["power"], 1e-9, "power rows")
+
+
+@pytest.mark.parametrize("tag", sorted(BEAM_TAGS))
+def test_beam_march_matches_reference(gpu_available, tag):
+    """TF/SF seed injection, external laser fields and the optical undulator on the device:
+    12 graph-replayed steps against the reference's own run."""
+    run = load(tag, "run")
+    ctx = mg.Context.from_setup(mg.Setup.from_job(job(BEAM_TAGS[tag][0])))
+    ctx.run_prelude()
+    ctx.run(12)
+    anp1, an, anm1 = ctx.download_fields()
+    assert rel_l2(an, run["an12"]) <= MARCH_RTOL
+    assert rel_l2(anm1, run["anm1_12"]) <= MARCH_RTOL
+    assert rel_l2(anp1, run["anp1_12"]) <= MARCH_RTOL
+    parts = ctx.download_particles()
+    ref = run["particles12"]
+    assert parts.shape == ref.shape
+    for col in range(11):
+        assert_close_scaled(parts[:, col], ref[:, col], 1e-10, "particle column %d" % col)
     rows = ctx.power_rows().reshape(12, -1)
     assert_close_scaled(rows, run["power"], 1e-9, "power rows")
