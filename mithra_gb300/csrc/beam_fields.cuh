@@ -236,4 +236,13 @@ __host__ __device__ inline void beam_add(const BeamDev& s, const PushDev& P, dou
   et[2] += eT[2];
 }
 
+// Every laser beam acting on a particle: the optical undulator modules in module order, then the
+// external fields.
+__device__ __forceinline__ void laser_beams_add(const PushDev& P, const UndDev* __restrict__ und, int n_und,
+                                             double timeBunch, double x, double y, double z, double* bt, double* et) {
+  for (int u = 0; u < n_und; u++)
+    if (und[u].type == 1 && und[u].beam >= 0) beam_add(P.beams[und[u].beam], P, timeBunch, x, y, z, bt, et);
+  for (int xf = 0; xf < P.n_ext; xf++) beam_add(P.beams[P.ext0 + xf], P, timeBunch, x, y, z, bt, et);
+}
+
 }  // namespace mithra

@@ -273,8 +273,13 @@ int fp32_push(mithra_ctx* ctx, int save_rnm) {
     if (r) return r;
   }
   r = timed(ctx, "push", [&] {
-    k_push_f32<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(
-        C, ctx->und_dev, table, ctx->f32.pt, ctx->E, ctx->B, g.cstride, g.plane, g.P1, ctx->st, save_rnm);
+    const int blocks = grid_stride_blocks(ctx, (long long)ctx->capacity, 256);
+    if (C.P64.n_opt + C.P64.n_ext > 0)
+      k_push_f32<true><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, ctx->B, g.cstride,
+                                                        g.plane, g.P1, ctx->st, save_rnm);
+    else
+      k_push_f32<false><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, ctx->B, g.cstride,
+                                                         g.plane, g.P1, ctx->st, save_rnm);
   });
   if (r) return r;
   return timed(ctx, "substep_end", [&] {

@@ -167,7 +167,10 @@ __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, co
 // One bunch substep (src/solver.cpp:1424-1549) in the mixed form.  Positions are (cell, offset)
 // in cell units; the owned-domain test of the reference (wrapped z in [zp0, zp1)) is always true
 // for one domain and is folded into the crossing test.
-__global__ void __launch_bounds__(256) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
+// BEAMS: the job defines optical undulators or external fields (a separate instantiation keeps
+// the FP64 laser-beam code, and its registers, out of the common kernel).
+template <bool BEAMS>
+__global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
                                                   const UndTableEntry* __restrict__ table, ParticlesF32 pt,
                                                   const float* __restrict__ E, const float* __restrict__ B,
                                                   long long cstride, long long plane, int P1, StateDev* st,
@@ -195,15 +198,13 @@ __global__ void __launch_bounds__(256) k_push_f32(PushF32 C, const UndDev* __res
       const bool k_in = (k >= 0 && k <= C.N2);
       const double zd_slow = k_in ? 0.0 : C.zmin + ((double)k + (double)fz) * C.dzd;
       undulator_f32(und, table, C.n_und, C.N2, C.gdz, k, fz, zd_slow, tshift, C.gamma, x, y, bt, et, C.gamma_f, C.bc_f);
-      if (C.P64.n_opt + C.P64.n_ext > 0) {
+      if (BEAMS) {
         // Laser beams in FP64: their phase, like the undulator's, is a large lab-frame coordinate.
         const double xd = C.xmin_d + ((double)i + (double)fx) * C.dxd;
         const double yd = C.ymin_d + ((double)j + (double)fy) * C.dyd;
         const double zd = C.zmin + ((double)k + (double)fz) * C.dzd;
         double b64[3] = {0.0, 0.0, 0.0}, e64[3] = {0.0, 0.0, 0.0};
-        for (int u = 0; u < C.n_und; u++)
-          if (und[u].type == 1 && und[u].beam >= 0) beam_add(C.P64.beams[und[u].beam], C.P64, tb, xd, yd, zd, b64, e64);
-        for (int xf = 0; xf < C.P64.n_ext; xf++) beam_add(C.P64.beams[C.P64.ext0 + xf], C.P64, tb, xd, yd, zd, b64, e64);
+        laser_beams_add(C.P64, und, C.n_und, tb, xd, yd, zd, b64, e64);
         for (int c = 0; c < 3; c++) { bt[c] += (float)b64[c]; et[c] += (float)e64[c]; }
       }
       uint8_t e = pt.e[p];

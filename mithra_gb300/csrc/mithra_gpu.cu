@@ -168,8 +168,13 @@ int stage_field_update(mithra_ctx* ctx) {
 int stage_push(mithra_ctx* ctx, int save_rnm) {
   if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_push(ctx, save_rnm);
   int r = timed(ctx, "push", [&] {
-    k_push_fp64<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(
-        ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E64, ctx->B64, ctx->st, save_rnm);
+    const int blocks = grid_stride_blocks(ctx, (long long)ctx->capacity, 256);
+    if (ctx->P.n_opt + ctx->P.n_ext > 0)
+      k_push_fp64<true><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E64, ctx->B64,
+                                                         ctx->st, save_rnm);
+    else
+      k_push_fp64<false><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E64, ctx->B64,
+                                                          ctx->st, save_rnm);
   });
   if (r) return r;
   return timed(ctx, "substep_end", [&] {

@@ -7,19 +7,17 @@
 
 namespace mithra {
 
-// Solver::undulatorField (src/solver.cpp:1798-1880): static modules with
-// Solver::staticUndulator (src/beam.cc:14-76), optical modules as laser beams.  Adds the lab-frame
-// undulator field, boosted into the bunch frame, to bt/et.
+// Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
+// Solver::staticUndulator (src/beam.cc:14-76).  Adds the lab-frame undulator field, boosted
+// into the bunch frame, to bt/et.  Optical modules are laser beams (laser_beams_add), added
+// after the static ones.
 __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
                                                        const PushDev& P, double timeBunch,
                                                        double x, double y, double z,
                                                        double* bt, double* et) {
   for (int u = 0; u < n_und; u++) {
     const UndDev& U = und[u];
-    if (U.type != 0) {
-      if (U.type == 1 && U.beam >= 0) beam_add(P.beams[U.beam], P, timeBunch, x, y, z, bt, et);
-      continue;
-    }
+    if (U.type != 0) continue;  // optical modules: laser_beams_add
     const double lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift)) - U.rb;
     const double ly = x * U.ct + y * U.st;
     double s_ly, c_ly;
@@ -68,6 +66,8 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
 
 // One Solver::bunchUpdate for every particle (src/solver.cpp:1424-1549).
 // save_rnm: also perform `rnm = rnp` first (src/solver.cpp:1311-1312).
+// BEAMS: the job defines optical undulators or external fields (see k_push_f32).
+template <bool BEAMS>
 __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const UndDev* __restrict__ und,
                                                    ParticlesDev<double> pt, const double* __restrict__ E,
                                                    const double* __restrict__ B, StateDev* st, int save_rnm) {
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         const bool b1z = (z < g.zp1 && z >= g.zp0);
         double bt[3] = {0.0, 0.0, 0.0}, et[3] = {0.0, 0.0, 0.0};
         static_undulator_field(und, P.n_und, P, timeBunch, x, y, z, bt, et);
-        for (int xf = 0; xf < P.n_ext; xf++) beam_add(P.beams[P.ext0 + xf], P, timeBunch, x, y, z, bt, et);
+        if (BEAMS) laser_beams_add(P, und, P.n_und, timeBunch, x, y, z, bt, et);
         double e = pt.e[p];
         if (e == 1.0) {
           if (b1x && b1y && b1z) {

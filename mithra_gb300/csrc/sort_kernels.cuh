@@ -181,7 +181,7 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
 // as k_deposit_f32; rho (space charge) is added straight to global memory.
 constexpr int kDepositBlock = 128;
 
-__global__ void __launch_bounds__(kDepositBlock) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
+__global__ void __launch_bounds__(kDepositBlock, 8) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
                                                        StateDev* st, float* J, float* rho, long long cs,
                                                        long long plane, int P1) {
   extern __shared__ float sJ[];  // 3 * TILE_NODES
