@@ -68,6 +68,7 @@ struct mithra_ctx {
   bool seed_active = false;
   double* A[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of A (SoA)
   double* F[3] = {nullptr, nullptr, nullptr};  // FP64 form: three time levels of phi
+  double* Jedge = nullptr;  // FP64 form: current of the deposit in edge form (k_deposit_fp64)
   mithra::ParticlesDev<double> pt{};
   mithra::Fp32State f32{};
   float* E = nullptr;  // mixed form: E and B, 3 components, cstride apart

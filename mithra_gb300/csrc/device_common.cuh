@@ -94,6 +94,7 @@ struct StateDev {
   unsigned long long n_transverse;  // particles outside the transverse domain (diagnostic)
   int overflow;                     // set when appended copies would exceed the capacity
   int nonfinite;
+  int j_edges;  // FP64 form: the current of the last deposit is held in edge form (see k_deposit_fp64)
   long long n_power_rows;
   long long power_row_cap;
   // z-slab (cells) occupied by particles: E/B are evaluated only where a gather can read them.

@@ -38,6 +38,10 @@ struct PotentialArgs {
   int ncomp;     // 3 for A, 1 for phi
   T asrc;        // a[4] for J, a[5] for rho
   Coeffs<T> k;
+  // FP64 vector potential: when st->j_edges is set, the source is the edge-form current of the
+  // deposit, J_c(node) = Je_c(node) + Je_c(node - unit step along c), instead of np1.
+  const T* jedge = nullptr;
+  StateDev* st = nullptr;
 };
 
 // Interior update, AdvanceField::advanceMagneticPotentialFD/NSFD and the scalar variants
@@ -53,19 +57,27 @@ __global__ void __launch_bounds__(256) k_potential_interior(GridDev g, Potential
   const long long m = node_index(g, k, i, j);
   const long long sI = g.P1, sK = g.plane;
   const T a0 = p.k.a0, a1 = p.k.a1, a2 = p.k.a2, a3 = p.k.a3, as = p.asrc;
+  const bool edges = p.jedge != nullptr && p.st->j_edges;
   for (int c = 0; c < p.ncomp; c++) {
     const T* an = p.n + c * g.cstride;
     const T* am = p.nm1 + c * g.cstride;
     T* ap = p.np1 + c * g.cstride;
+    T src;
+    if (edges) {
+      const T* je = p.jedge + c * g.cstride;
+      src = je[m] + je[m - (c == 0 ? sI : c == 1 ? 1 : sK)];
+    } else {
+      src = ap[m];
+    }
     T v;
     if (NSFD) {
       const T al = p.k.al, be = p.k.be;
       T sx = an[m + sI] + an[m - sI] + be * (an[m + sI + sK] + an[m + sI - sK] + an[m - sI + sK] + an[m - sI - sK]);
       T sy = an[m + 1] + an[m - 1] + be * (an[m + 1 + sK] + an[m + 1 - sK] + an[m - 1 + sK] + an[m - 1 - sK]);
-      v = a0 * an[m] - am[m] + al * (a1 * sx + a2 * sy) + a3 * (an[m + sK] + an[m - sK]) + as * ap[m];
+      v = a0 * an[m] - am[m] + al * (a1 * sx + a2 * sy) + a3 * (an[m + sK] + an[m - sK]) + as * src;
     } else {
       v = a0 * an[m] - am[m] + a1 * (an[m + sI] + an[m - sI]) + a2 * (an[m + 1] + an[m - 1]) +
-          a3 * (an[m + sK] + an[m - sK]) + as * ap[m];
+          a3 * (an[m + sK] + an[m - sK]) + as * src;
     }
     ap[m] = v;
   }
@@ -88,6 +100,8 @@ __global__ void __launch_bounds__(256) k_potential_faces(GridDev g, PotentialArg
   const long long nz = (long long)(g.N0 - 2) * (g.N1 - 2);
   const long long total = 2 * (nx + ny + nz);
   const long long sI = g.P1, sK = g.plane;
+  // The interior update has consumed the edge-form current: A^{n+1} now fills np1.
+  if (p.st && blockIdx.x == 0 && threadIdx.x == 0) p.st->j_edges = 0;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
     long long m, in, o1, o2;
@@ -277,6 +291,32 @@ __global__ void k_soa_to_aos(GridDev g, const Tdev* __restrict__ src, Thost* __r
     const int i = (int)(ki % g.N0), k = (int)(ki / g.N0);
     const long long m = node_index(g, k, i, j);
     for (int c = 0; c < ncomp; c++) dst[r * ncomp + c] = (Thost)src[c * g.cstride + m];
+  }
+}
+
+}  // namespace mithra
+
+namespace mithra {
+
+// Node values of an edge-form current (the inverse view of k_deposit_fp64's layout):
+// J_c(node) = Je_c(node) + Je_c(node - unit step along c), the second term only where that
+// neighbour exists.
+static __global__ void __launch_bounds__(256) k_materialize_j(GridDev g, const double* __restrict__ je, double* __restrict__ J) {
+  const long long nodes = (long long)g.N0 * g.N1 * g.N2;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 3 * nodes;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(t / nodes);
+    long long r = t % nodes;
+    const int j = (int)(r % g.N1); r /= g.N1;
+    const int i = (int)(r % g.N0);
+    const int k = (int)(r / g.N0);
+    const long long m = node_index(g, k, i, j);
+    const double* e = je + c * g.cstride;
+    double v = e[m];
+    if (c == 0 && i > 0) v += e[m - g.P1];
+    if (c == 1 && j > 0) v += e[m - 1];
+    if (c == 2 && k > 0) v += e[m - g.plane];
+    J[c * g.cstride + m] = v;
   }
 }
 

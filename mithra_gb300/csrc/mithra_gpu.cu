@@ -156,7 +156,7 @@ int stage_field_update(mithra_ctx* ctx) {
   const GridDev& g = ctx->g;
   int r;
   const Coeffs<double> k = make_coeffs<double>(g);
-  PotentialArgs<double> pa{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], ctx->A[ctx->idx[2]], 3, g.a[4], k};
+  PotentialArgs<double> pa{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], ctx->A[ctx->idx[2]], 3, g.a[4], k, ctx->Jedge, ctx->st};
   if ((r = run_potential(ctx, pa, true))) return r;
   if (g.space_charge) {
     PotentialArgs<double> pf{ctx->F[ctx->idx[0]], ctx->F[ctx->idx[1]], ctx->F[ctx->idx[2]], 1, g.a[5], k};
@@ -225,7 +225,7 @@ void rotate(mithra_ctx* ctx) {
 int stage_current(mithra_ctx* ctx) {
   if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_current(ctx);
   const GridDev& g = ctx->g;
-  double* J = ctx->A[ctx->idx[0]];
+  double* J = ctx->Jedge;  // edge form; the field update reads it (PotentialArgs::jedge)
   CK(cudaMemsetAsync(J, 0, (size_t)3 * g.cstride * sizeof(double), ctx->stream));
   double* rho = nullptr;
   if (g.space_charge) {
@@ -416,6 +416,8 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
     const size_t nf = (size_t)3 * g.cstride;
     ctx->capacity = std::max<size_t>(particle_capacity, 1);
     if (precision == MITHRA_PRECISION_FP64) {
+      CK(dalloc(&ctx->Jedge, nf));
+      CK(cudaMemsetAsync(ctx->Jedge, 0, nf * sizeof(double), ctx->stream));
       for (int b = 0; b < 3; b++) {
         CK(dalloc(&ctx->A[b], nf));
         CK(cudaMemsetAsync(ctx->A[b], 0, nf * sizeof(double), ctx->stream));
@@ -482,7 +484,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   fp32_free(ctx);
   cudaFree(ctx->staging);
   cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
-  cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev);
+  cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev); cudaFree(ctx->Jedge);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
     void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
@@ -662,6 +664,10 @@ int mithra_gpu_upload_fields(mithra_ctx* ctx, const double* anp1, const double* 
       k_aos_to_soa<float, double><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, staging, fp32_field(ctx, l), 3);
     CK(cudaGetLastError());
   }
+  if (anp1 && ctx->precision == MITHRA_PRECISION_FP64) {  // anp1 now holds the current in node form
+    static const int zero = 0;
+    CK(cudaMemcpyAsync(&ctx->st->j_edges, &zero, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   return MITHRA_OK;
 }
@@ -673,6 +679,16 @@ int mithra_gpu_download_fields(mithra_ctx* ctx, double* anp1, double* an, double
   double* staging = nullptr;
   { int r = mithra::staging(ctx, n * sizeof(double), (void**)&staging); if (r) return r; }
   double* dst[3] = {anp1, an, anm1};
+  if (anp1 && ctx->precision == MITHRA_PRECISION_FP64) {
+    // A current still in edge form is returned in the reference's node form (J in anp1_).
+    int edges = 0;
+    CK(cudaMemcpyAsync(&edges, &ctx->st->j_edges, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (edges) {
+      k_materialize_j<<<grid_stride_blocks(ctx, (long long)n, 256), 256, 0, ctx->stream>>>(g, ctx->Jedge, ctx->A[ctx->idx[0]]);
+      CK(cudaGetLastError());
+    }
+  }
   for (int l = 0; l < 3; l++) {
     if (!dst[l]) continue;
     if (ctx->precision == MITHRA_PRECISION_FP64)

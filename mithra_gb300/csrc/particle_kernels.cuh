@@ -244,20 +244,29 @@ __global__ void __launch_bounds__(256) k_erase_outside(GridDev g, ParticlesDev<T
 // FdTd::currentUpdate, zigzag (Umeda) deposit (src/fdtd.cpp:38-185), FP64 atomics into J
 // (the anp1 buffer, zeroed before).  With rho != nullptr also the charge deposit of
 // src/fdtdSC.cpp:140-161.
-__device__ __forceinline__ void deposit_half(double* J, long long cs, long long m, long long sI, long long sK,
-                                             double qh, double dxh, double dyh, double dzh, double jx,
-                                             double jy, double jz) {
+// The same half segment in edge form.  The reference adds one value to both ends of a cell edge
+// (Jx to nodes i and i+1 with weights of y and z only, src/fdtd.cpp:105-130, and likewise Jy, Jz),
+// so each value is added once, to the edge's lower node, into Je; the node current is
+// Je(node) + Je(node - unit step), formed where it is read.  12 atomics instead of 24.
+__device__ __forceinline__ void deposit_half_edges(double* Je, long long cs, long long m, long long sI, long long sK,
+                                                   double qh, double dxh, double dyh, double dzh, double jx,
+                                                   double jy, double jz) {
   const double x1 = 1.0 - dxh, x2 = dxh, y1 = 1.0 - dyh, y2 = dyh, z1 = 1.0 - dzh, z2 = dzh;
-  const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
-  const double wx[8] = {y1 * z1, y1 * z1, y2 * z1, y2 * z1, y1 * z2, y1 * z2, y2 * z2, y2 * z2};
-  const double wy[8] = {x1 * z1, x2 * z1, x1 * z1, x2 * z1, x1 * z2, x2 * z2, x1 * z2, x2 * z2};
-  const double wz[8] = {x1 * y1, x2 * y1, x1 * y2, x2 * y2, x1 * y1, x2 * y1, x1 * y2, x2 * y2};
-#pragma unroll
-  for (int q = 0; q < 8; q++) {
-    atomicAdd(J + nd[q], qh * wx[q] * jx);
-    atomicAdd(J + cs + nd[q], qh * wy[q] * jy);
-    atomicAdd(J + 2 * cs + nd[q], qh * wz[q] * jz);
-  }
+  const double qx = qh * jx, qy = qh * jy, qz = qh * jz;
+  atomicAdd(Je + m, qx * (y1 * z1));
+  atomicAdd(Je + m + 1, qx * (y2 * z1));
+  atomicAdd(Je + m + sK, qx * (y1 * z2));
+  atomicAdd(Je + m + 1 + sK, qx * (y2 * z2));
+  double* Jy = Je + cs;
+  atomicAdd(Jy + m, qy * (x1 * z1));
+  atomicAdd(Jy + m + sI, qy * (x2 * z1));
+  atomicAdd(Jy + m + sK, qy * (x1 * z2));
+  atomicAdd(Jy + m + sI + sK, qy * (x2 * z2));
+  double* Jz = Je + 2 * cs;
+  atomicAdd(Jz + m, qz * (x1 * y1));
+  atomicAdd(Jz + m + sI, qz * (x2 * y1));
+  atomicAdd(Jz + m + 1, qz * (x1 * y2));
+  atomicAdd(Jz + m + sI + 1, qz * (x2 * y2));
 }
 
 // Min/max of particle cells along z, reduced per warp and folded into the state with atomics.
@@ -272,10 +281,12 @@ __device__ __forceinline__ void slab_update(StateDev* st, int kmin, int kmax) {
   }
 }
 
+// J: the edge-form current buffer (zeroed by the caller); rho: node charge, or null.
 __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<double> pt, StateDev* st,
                                                       double* J, double* rho) {
   const long long n = st->n_particles;
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->j_edges = 1;  // J is written in edge form
   int kmin = 0x7fffffff, kmax = -0x7fffffff;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
@@ -306,7 +317,7 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
       const double dxp = modf((0.5 * (rp0 + r0) - g.xmin) * g.rdx, &c);
       const double dyp = modf((0.5 * (rp1 + r1) - g.ymin) * g.rdy, &c);
       const double dzp = modf((0.5 * (rp2 + r2) - g.zmin) * g.rdz, &c);
-      deposit_half(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
+      deposit_half_edges(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
       if (rho) {
         const double fx = modf((rp0 - g.xmin) * g.rdx, &c), fy = modf((rp1 - g.ymin) * g.rdy, &c),
                      fz = modf((rp2 - g.zmin) * g.rdz, &c);
@@ -327,7 +338,7 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
       const double dxm = modf((0.5 * (rm0 + r0) - g.xmin) * g.rdx, &c);
       const double dym = modf((0.5 * (rm1 + r1) - g.ymin) * g.rdy, &c);
       const double dzm = modf((0.5 * (rm2 + r2) - g.zmin) * g.rdz, &c);
-      deposit_half(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
+      deposit_half_edges(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
     }
   }
   slab_update(st, kmin, kmax);
