@@ -9,6 +9,7 @@
 //   * particles are structure-of-arrays (position, momentum, previous position, charge, entry
 //     flag), plus a status byte (bit 0: erased) and a crossing byte written by the push.
 #pragma once
+#include <cstring>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -170,8 +171,77 @@ __device__ __forceinline__ bool eb_plane_wanted(int k, const StateDev* st, const
   return false;
 }
 
+// Conversions between double and float done on the integer pipes.  GB300 issues FP64 work at a
+// small fraction of its FP32 rate and a hardware F2F conversion costs about two FP64 slots, while
+// E/B evaluation of the FP64 form converts 18 times per node (the reference stores E, B as
+// float).  Both functions are exact: round-to-nearest-even for double -> float, bit widening for
+// float -> double; zero is handled here, subnormal/inf/nan go to the hardware conversion.
+__host__ __device__ __forceinline__ unsigned long long bits_of(double x) {
+#ifdef __CUDA_ARCH__
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+__host__ __device__ __forceinline__ double double_of(unsigned long long u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+#endif
+}
+__host__ __device__ __forceinline__ unsigned bits_of(float x) {
+#ifdef __CUDA_ARCH__
+  return __float_as_uint(x);
+#else
+  unsigned u;
+  memcpy(&u, &x, 4);
+  return u;
+#endif
+}
+__host__ __device__ __forceinline__ float float_of(unsigned u) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  float x;
+  memcpy(&x, &u, 4);
+  return x;
+#endif
+}
+
+__host__ __device__ __forceinline__ float to_float_rn(double x) {
+  const unsigned long long u = bits_of(x);
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  const unsigned sign = hi & 0x80000000u;
+  if (e >= 897u && e <= 1150u) {  // a normal float before rounding (float exponent 1..254)
+    unsigned r = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu, half = 0x10000000u;
+    r += (rem > half) | ((rem == half) & (r & 1u));  // a carry into the exponent is correct, up to inf
+    return float_of(sign | r);
+  }
+  if (((hi & 0x7fffffffu) | lo) == 0u) return float_of(sign);  // +-0
+  return (float)x;
+}
+
+__host__ __device__ __forceinline__ double to_double(float f) {
+  const unsigned b = bits_of(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  if (e != 0u && e != 255u) {
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return double_of(((unsigned long long)hi << 32) | ((unsigned long long)(b & 7u) << 29));
+  }
+  if ((b & 0x7fffffffu) == 0u) return double_of((unsigned long long)(b & 0x80000000u) << 32);  // +-0
+  return (double)f;
+}
+
 // pmod, src/stdinclude.cpp:88-93.
 __device__ __forceinline__ double pmod_d(double a, double b) {
+  if (a >= 0.0 && a < b) return a;  // fmod is exact and returns a here
   double x = fmod(a, b);
   x += (x < 0.0) ? b : 0.0;
   return x;

@@ -232,14 +232,14 @@ __global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_l
   float e[3], b[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    float ef = (float)((double)A1[c * cs + m] * rmdt);
-    ef = (float)((double)ef - (double)A0[c * cs + m] * rmdt);
+    float ef = to_float_rn((double)A1[c * cs + m] * rmdt);
+    ef = to_float_rn(to_double(ef) - (double)A0[c * cs + m] * rmdt);
     e[c] = ef;
   }
   if (p.fn) {
-    e[0] = (float)((double)e[0] - ((double)p.fn[m + sI] - (double)p.fn[m - sI]) * rdx2);
-    e[1] = (float)((double)e[1] - ((double)p.fn[m + 1] - (double)p.fn[m - 1]) * rdy2);
-    e[2] = (float)((double)e[2] - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
+    e[0] = to_float_rn(to_double(e[0]) - ((double)p.fn[m + sI] - (double)p.fn[m - sI]) * rdx2);
+    e[1] = to_float_rn(to_double(e[1]) - ((double)p.fn[m + 1] - (double)p.fn[m - 1]) * rdy2);
+    e[2] = to_float_rn(to_double(e[2]) - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
   }
   const T *X0 = A0, *Y0 = A0 + cs, *Z0 = A0 + 2 * cs, *X1 = A1, *Y1 = A1 + cs, *Z1 = A1 + 2 * cs;
   // 0.5 * (curl A^n + curl A^{n+1}) with the two levels summed first.
@@ -250,19 +250,22 @@ __global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_l
               (((double)Z0[m + sI] + Z1[m + sI]) - ((double)Z0[m - sI] + Z1[m - sI])) * hx;
   double bz = (((double)Y0[m + sI] + Y1[m + sI]) - ((double)Y0[m - sI] + Y1[m - sI])) * hx -
               (((double)X0[m + 1] + X1[m + 1]) - ((double)X0[m - 1] + X1[m - 1])) * hy;
-  b[0] = (float)bx; b[1] = (float)by; b[2] = (float)bz;
+  b[0] = to_float_rn(bx); b[1] = to_float_rn(by); b[2] = to_float_rn(bz);
+  T eo[3], bo[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    p.E[c * cs + m] = (T)e[c];
-    p.B[c * cs + m] = (T)b[c];
+    eo[c] = (T)to_double(e[c]);
+    bo[c] = (T)to_double(b[c]);
+    p.E[c * cs + m] = eo[c];
+    p.B[c * cs + m] = bo[c];
   }
   if (k == 1) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = (T)e[c]; p.B[c * cs + m - sK] = (T)b[c]; }
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = eo[c]; p.B[c * cs + m - sK] = bo[c]; }
   }
   if (k == g.N2 - 2) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = (T)e[c]; p.B[c * cs + m + sK] = (T)b[c]; }
+    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = eo[c]; p.B[c * cs + m + sK] = bo[c]; }
   }
 }
 

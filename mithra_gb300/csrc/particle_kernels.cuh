@@ -22,14 +22,16 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
     const double ly = x * U.ct + y * U.st;
     double s_ly, c_ly;
     {
-      // cosh and sinh from one exponential; sinh by its Taylor series where e - 1/e cancels.
+      // cosh and sinh: Taylor series for |ku ly| < 0.1 (truncation below 1e-19 relative; the FP64
+      // pipe is the bound of this kernel), else from one exponential.
       const double kl = U.ku * ly;
-      const double ex = exp(kl), iex = 1.0 / ex;
-      c_ly = 0.5 * (ex + iex);
       if (fabs(kl) < 0.1) {
         const double a2 = kl * kl;
         s_ly = kl * (1.0 + a2 * (1.0 / 6.0) * (1.0 + a2 * (1.0 / 20.0) * (1.0 + a2 * (1.0 / 42.0) * (1.0 + a2 * (1.0 / 72.0)))));
+        c_ly = 1.0 + a2 * 0.5 * (1.0 + a2 * (1.0 / 12.0) * (1.0 + a2 * (1.0 / 30.0) * (1.0 + a2 * (1.0 / 56.0) * (1.0 + a2 * (1.0 / 90.0)))));
       } else {
+        const double ex = exp(kl), iex = 1.0 / ex;
+        c_ly = 0.5 * (ex + iex);
         s_ly = 0.5 * (ex - iex);
       }
     }
