@@ -36,6 +36,7 @@ WORKLOADS = {
     "fel-98x98x1026": "fel-98x98x1026.job",  # profiling case (about 1 GB on the device)
 }
 METRIC = "cell+particle updates/s"
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
 
 # Algorithmic bytes per unit (each array element counted once, halo re-reads free).
 # Units: interior node for the field kernels, particle for the particle kernels.
@@ -58,6 +59,8 @@ def parse_args():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp32-compare", action="store_true",
+                    help="with --precision fp64, skip the mixed-form run reported under fp32_form")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -303,6 +306,14 @@ def run_gpu(args, dist):
                 "traffic": (tr * unit_count if tr else None),
                 "avg_launch_ms": dom_ms / dom_launches, "share": dom_ms / total_k}
     kernels = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k} for k, v in kt.items()}
+    # The FP64 form is bound by GB300's FP64 pipe, not by HBM: its dominant kernel is also placed
+    # against the FP64 rate (FLOPs per unit counted by ncu on the profiling case, FMA = 2).
+    fp64_pipe = None
+    flop = traffic_table().get("fp64_flop_per_unit", {}).get(dominant) if args.precision == "fp64" else None
+    if flop:
+        tflops = flop * unit_count / (dom_ms / dom_launches / 1e3) / 1e12
+        fp64_pipe = {"kernel": dominant, "flop_per_unit": flop, "achieved": tflops, "peak": FP64_NOMINAL_TFLOPS,
+                     "unit": "TFLOP/s", "frac": tflops / FP64_NOMINAL_TFLOPS, "peak_source": "nominal"}
 
     # End to end through the public API with host buffers: upload the initial state from pinned
     # host memory, march K steps, read the power rows back.
@@ -333,6 +344,19 @@ def run_gpu(args, dist):
     launches = ctx.launches_per_step() * args.steps
     ctx.close()
 
+    # "FP32 vs FP64": the mixed form on the same workload and step count.
+    fp32_form = None
+    if args.precision == "fp64" and not args.no_fp32_compare:
+        c32 = mg.Context.from_setup(setup, mg.FP32, device=dist.local)
+        c32.run_prelude()
+        c32.run(args.warmup)
+        c32.synchronize()
+        dist.barrier()
+        ms32 = dist.max(c32.run_timed(args.steps))
+        c32.close()
+        v32 = dist.world * units * args.steps / (ms32 / 1e3)
+        fp32_form = {"value": v32, "unit": METRIC, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value}
+
     if dist.rank != 0:
         return
     cpu = None
@@ -349,6 +373,8 @@ def run_gpu(args, dist):
         "cell_updates_per_s": dist.world * nodes * args.steps / (ms_max / 1e3),
         "particle_pushes_per_s": dist.world * pushes * args.steps / (ms_max / 1e3),
         "roofline": roof,
+        "fp64_pipe": fp64_pipe,
+        "fp32_form": fp32_form,
         "kernels": kernels,
         "gpu_launches": launches,
         "clocks": clk.summary(),
