@@ -177,6 +177,13 @@ int mithra_gpu_save_positions(mithra_ctx* ctx);
 int mithra_gpu_bunch_update(mithra_ctx* ctx);
 /* Solver::recycleParticles (src/solver.cpp:493-503). */
 int mithra_gpu_recycle(mithra_ctx* ctx);
+/* Solver::bunchSample (src/solver.cpp:1582-1635) over the particles of this domain: row[0] =
+ * timeBunch_, row[1..3] <r>, row[4..6] <gb>, row[7..9] rms r, row[10..12] rms gb (charge-weighted;
+ * compensated FP64 sums). */
+int mithra_gpu_bunch_sample(mithra_ctx* ctx, double* row);
+/* Bunching factor |sum q exp(i k z)| / sum q at wavenumber k (bunch-frame z), the quantity read
+ * from the reference's bunch dumps (Solver::bunchProfile, src/solver.cpp:1763-1792). */
+int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b);
 /* Solver::powerSample (src/radiation.cpp:127-232); the row is appended to the device row log. */
 int mithra_gpu_power_sample(mithra_ctx* ctx);
 /* mithra_gpu_power_sample without any device allocation.  No counterpart in the reference: it

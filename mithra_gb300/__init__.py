@@ -111,6 +111,8 @@ _SIGS = {
     "mithra_gpu_recycle": [_vp],
     "mithra_gpu_power_sample": [_vp],
     "mithra_gpu_power_sample_noalloc": [_vp],
+    "mithra_gpu_bunch_sample": [_vp, _dp],
+    "mithra_gpu_bunching_factor": [_vp, C.c_double, _dp],
     "mithra_gpu_field_shift": [_vp],
     "mithra_gpu_current_update": [_vp],
     "mithra_gpu_advance_time": [_vp],
@@ -441,6 +443,18 @@ class Context:
 
     def power_sample(self):
         self.call("mithra_gpu_power_sample")
+
+    def bunch_sample(self) -> np.ndarray:
+        """Solver::bunchSample row: timeBunch, <r>(3), <gb>(3), rms r(3), rms gb(3)."""
+        row = np.zeros(13)
+        self.call("mithra_gpu_bunch_sample", dptr(row))
+        return row
+
+    def bunching_factor(self, k: float) -> float:
+        """|sum q exp(i k z)| / sum q over the particles of the domain (bunch-frame z)."""
+        b = np.zeros(1)
+        self.call("mithra_gpu_bunching_factor", float(k), dptr(b))
+        return float(b[0])
 
     def power_sample_noalloc(self):
         """power_sample with no device allocation: partial sums in a fixed per-device array."""

@@ -94,6 +94,8 @@ struct mithra_ctx {
   int sm_count = 152;
   int launches_per_step = 0;
   int launch_counter = 0;
+  void* diag_partial = nullptr;  // bunch diagnostics: per-block compensated sums (allocated on first use)
+  double* diag_out = nullptr;
   void* staging = nullptr;  // device staging buffer for host-layout transfers
   size_t staging_bytes = 0;
 };

@@ -1,0 +1,141 @@
+// Bunch diagnostics on the device: the moments of Solver::bunchSample (src/solver.cpp:1582-1635)
+// and the bunching factor |sum q exp(i k z)| / sum q (the quantity FEL studies read from the
+// bunch dumps of Solver::bunchProfile, src/solver.cpp:1763-1792).
+//
+// Sums are FP64 and compensated: every thread keeps a Neumaier sum per quantity, warps and blocks
+// combine (sum, compensation) pairs with an error-free two-sum, and one block adds the block
+// results in block order.  The result does not depend on the particle order beyond the last
+// bits, and is reproducible for a fixed launch shape.
+#pragma once
+#include "device_common.cuh"
+
+namespace mithra {
+
+constexpr int kDiagBlock = 256;
+constexpr int kDiagMaxBlocks = 1024;
+constexpr int kDiagValues = 13;  // q, q r (3), q r^2 (3), q gb (3), q gb^2 (3)
+
+struct CSum {
+  double s, c;
+};
+
+__device__ __forceinline__ void csum_add(CSum& a, double v) {  // Neumaier
+  const double t = a.s + v;
+  a.c += (fabs(a.s) >= fabs(v)) ? (a.s - t) + v : (v - t) + a.s;
+  a.s = t;
+}
+
+__device__ __forceinline__ CSum csum_merge(CSum a, CSum b) {
+  CSum r;
+  r.s = a.s + b.s;
+  const double bb = r.s - a.s;
+  r.c = a.c + b.c + ((a.s - (r.s - bb)) + (b.s - bb));
+  return r;
+}
+
+// Block-level reduction of NV compensated sums; thread 0 writes them to out[blockIdx.x * NV ...].
+template <int NV>
+__device__ __forceinline__ void csum_block_store(CSum* v, double2* out) {
+  __shared__ double2 sh[kDiagBlock / 32][NV];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      CSum w{__shfl_down_sync(0xffffffffu, v[q].s, o), __shfl_down_sync(0xffffffffu, v[q].c, o)};
+      v[q] = csum_merge(v[q], w);
+    }
+    if (lane == 0) sh[warp][q] = make_double2(v[q].s, v[q].c);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < NV; q++) {
+      CSum a{sh[0][q].x, sh[0][q].y};
+      for (int w = 1; w < kDiagBlock / 32; w++) a = csum_merge(a, CSum{sh[w][q].x, sh[w][q].y});
+      out[blockIdx.x * NV + q] = make_double2(a.s, a.c);
+    }
+  }
+}
+
+// Particle position (and gamma*beta) in FP64 for either particle form.
+struct DiagParticles {
+  // FP64 form
+  const double *x, *y, *z, *gx, *gy, *gz, *q;
+  // mixed form
+  const long long* cell;
+  const float *fx, *fy, *fz, *gxf, *gyf, *gzf, *qf;
+  const uint8_t* status;
+  double xmin, ymin, zmin, dx, dy, dz;
+  __device__ __forceinline__ void get(long long p, double* r, double* g, double& qq) const {
+    if (x) {
+      r[0] = x[p]; r[1] = y[p]; r[2] = z[p];
+      g[0] = gx[p]; g[1] = gy[p]; g[2] = gz[p];
+      qq = q[p];
+    } else {
+      int i, j, k;
+      unpack_cell(cell[p], i, j, k);
+      r[0] = xmin + ((double)i + (double)fx[p]) * dx;
+      r[1] = ymin + ((double)j + (double)fy[p]) * dy;
+      r[2] = zmin + ((double)k + (double)fz[p]) * dz;
+      g[0] = gxf[p]; g[1] = gyf[p]; g[2] = gzf[p];
+      qq = qf[p];
+    }
+  }
+};
+
+// particleInProcessor, src/solver.cpp:2292-2296.
+__device__ __forceinline__ bool in_processor(const GridDev& g, double z) {
+  const double zr = pmod_d(z - g.zmin, g.Lz) + g.zmin;
+  return zr >= g.zp0 && zr < g.zp1;
+}
+
+__global__ void __launch_bounds__(kDiagBlock) k_bunch_moments(GridDev g, DiagParticles P, const StateDev* st,
+                                                              double2* partial) {
+  CSum v[kDiagValues];
+#pragma unroll
+  for (int q = 0; q < kDiagValues; q++) v[q] = CSum{0.0, 0.0};
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    if (P.status[p] & 1) continue;
+    double r[3], gb[3], q;
+    P.get(p, r, gb, q);
+    if (!in_processor(g, r[2])) continue;
+    csum_add(v[0], q);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      csum_add(v[1 + c], q * r[c]);
+      csum_add(v[4 + c], r[c] * r[c] * q);
+      csum_add(v[7 + c], q * gb[c]);
+      csum_add(v[10 + c], gb[c] * gb[c] * q);
+    }
+  }
+  csum_block_store<kDiagValues>(v, partial);
+}
+
+__global__ void __launch_bounds__(kDiagBlock) k_bunching(GridDev g, DiagParticles P, const StateDev* st, double k,
+                                                         double2* partial) {
+  CSum v[3] = {{0.0, 0.0}, {0.0, 0.0}, {0.0, 0.0}};
+  const long long n = st->n_particles;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    if (P.status[p] & 1) continue;
+    double r[3], gb[3], q;
+    P.get(p, r, gb, q);
+    if (!in_processor(g, r[2])) continue;
+    double sn, cs;
+    sincos(k * r[2], &sn, &cs);
+    csum_add(v[0], q);
+    csum_add(v[1], q * cs);
+    csum_add(v[2], q * sn);
+  }
+  csum_block_store<3>(v, partial);
+}
+
+// Adds the block results in block order; out[q] = compensated total of quantity q.
+__global__ void k_diag_finish(const double2* partial, int nblocks, int nv, double* out) {
+  const int q = threadIdx.x;
+  if (q >= nv) return;
+  CSum a{0.0, 0.0};
+  for (int b = 0; b < nblocks; b++) a = csum_merge(a, CSum{partial[b * nv + q].x, partial[b * nv + q].y});
+  out[q] = a.s + a.c;
+}
+
+}  // namespace mithra

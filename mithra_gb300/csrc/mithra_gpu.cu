@@ -20,6 +20,7 @@
 #include "field_kernels.cuh"
 #include "particle_kernels.cuh"
 #include "power_kernels.cuh"
+#include "diag_kernels.cuh"
 
 using namespace mithra;
 
@@ -485,6 +486,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   cudaFree(ctx->staging);
   cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
   cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev); cudaFree(ctx->Jedge);
+  cudaFree(ctx->diag_partial); cudaFree(ctx->diag_out);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
     void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
@@ -1055,6 +1057,81 @@ int mithra_gpu_power_rows(mithra_ctx* ctx, double* out, size_t cap_values, size_
   CK(cudaMemcpyAsync(&ctx->st->n_power_rows, &ctx->st_host->n_power_rows, sizeof(long long), cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->rows_pending = 0;
+  return MITHRA_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+DiagParticles diag_particles(const mithra_ctx* ctx) {
+  DiagParticles P{};
+  const GridDev& g = ctx->g;
+  P.xmin = g.xmin; P.ymin = g.ymin; P.zmin = g.zmin; P.dx = g.dx; P.dy = g.dy; P.dz = g.dz;
+  if (ctx->precision == MITHRA_PRECISION_FP64) {
+    const ParticlesDev<double>& t = ctx->pt;
+    P.x = t.x; P.y = t.y; P.z = t.z; P.gx = t.gx; P.gy = t.gy; P.gz = t.gz; P.q = t.q; P.status = t.status;
+  } else {
+    const ParticlesF32& t = ctx->f32.pt;
+    P.cell = t.cell; P.fx = t.fx; P.fy = t.fy; P.fz = t.fz; P.gxf = t.gx; P.gyf = t.gy; P.gzf = t.gz; P.qf = t.q;
+    P.status = t.status;
+  }
+  return P;
+}
+
+// Runs one diagnostic reduction (`launch` issues the block kernel) and copies nv totals to out.
+template <typename F>
+int diag_reduce(mithra_ctx* ctx, int nv, F launch, double* out, int* nblocks_out) {
+  if (!ctx->diag_partial) {
+    CK(cudaMalloc(&ctx->diag_partial, (size_t)kDiagMaxBlocks * 16 * sizeof(double2)));
+    CK(cudaMalloc(&ctx->diag_out, 16 * sizeof(double)));
+  }
+  const int nb = std::min(kDiagMaxBlocks, grid_stride_blocks(ctx, (long long)ctx->capacity, kDiagBlock));
+  launch(nb);
+  k_diag_finish<<<1, 32, 0, ctx->stream>>>((const double2*)ctx->diag_partial, nb, nv, ctx->diag_out);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, ctx->diag_out, nv * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (nblocks_out) *nblocks_out = nb;
+  return MITHRA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mithra_gpu_bunch_sample(mithra_ctx* ctx, double* row) {
+  if (!ctx || !row) return MITHRA_ERR_ARG;
+  double s[kDiagValues];
+  const DiagParticles P = diag_particles(ctx);
+  int r = diag_reduce(ctx, kDiagValues, [&](int nb) {
+    k_bunch_moments<<<nb, kDiagBlock, 0, ctx->stream>>>(ctx->g, P, ctx->st, (double2*)ctx->diag_partial);
+  }, s, nullptr);
+  if (r) return r;
+  mithra_time_state t;
+  if ((r = mithra_gpu_get_time(ctx, &t))) return r;
+  // Solver::bunchSample, src/solver.cpp:1613-1634: means, then sqrt(<v^2> - <v>^2).
+  const double qT = s[0];
+  row[0] = t.time_bunch;
+  for (int c = 0; c < 3; c++) {
+    const double rT = s[1 + c] / qT, r2T = s[4 + c] / qT, gbT = s[7 + c] / qT, gb2T = s[10 + c] / qT;
+    row[1 + c] = rT;
+    row[4 + c] = gbT;
+    row[7 + c] = sqrt(r2T - rT * rT);
+    row[10 + c] = sqrt(gb2T - gbT * gbT);
+  }
+  return MITHRA_OK;
+}
+
+int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b) {
+  if (!ctx || !b) return MITHRA_ERR_ARG;
+  double s[3];
+  const DiagParticles P = diag_particles(ctx);
+  int r = diag_reduce(ctx, 3, [&](int nb) {
+    k_bunching<<<nb, kDiagBlock, 0, ctx->stream>>>(ctx->g, P, ctx->st, k, (double2*)ctx->diag_partial);
+  }, s, nullptr);
+  if (r) return r;
+  *b = (s[0] != 0.0) ? sqrt(s[1] * s[1] + s[2] * s[2]) / s[0] : 0.0;
   return MITHRA_OK;
 }
 

@@ -957,3 +957,47 @@ void mo_power_sample(const mo_power* p, unsigned nTime, const float* en, const f
     kz++;
   }
 }
+
+/* ------------------------------------------------------------------------------------------ */
+/* Bunch diagnostics.                                                                          */
+/* ------------------------------------------------------------------------------------------ */
+
+/* particleInProcessor, src/solver.cpp:2292-2296. */
+static int in_processor(double zmin, double Lz, double zp0, double zp1, double z) {
+  double zr = mo_pmod(z - zmin, Lz) + zmin;
+  return (zr >= zp0) && (zr < zp1);
+}
+
+void mo_bunch_sample(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double* out) {
+  double q = 0.0, r[3] = {0, 0, 0}, r2[3] = {0, 0, 0}, gb[3] = {0, 0, 0}, gb2[3] = {0, 0, 0};
+  for (long i = 0; i < n; i++) {
+    const double* c = rec + MO_REC * i;
+    if (!in_processor(zmin, Lz, zp0, zp1, c[3])) continue;
+    q += c[0];
+    for (int l = 0; l < 3; l++) r[l] += c[0] * c[1 + l];
+    for (int l = 0; l < 3; l++) gb[l] += c[0] * c[7 + l];
+    for (int l = 0; l < 3; l++) {
+      r2[l] += c[1 + l] * c[1 + l] * c[0];
+      gb2[l] += c[7 + l] * c[7 + l] * c[0];
+    }
+  }
+  for (int l = 0; l < 3; l++) {
+    double rT = r[l] / q, r2T = r2[l] / q, gbT = gb[l] / q, gb2T = gb2[l] / q;
+    out[l] = rT;
+    out[3 + l] = gbT;
+    out[6 + l] = sqrt(r2T - rT * rT);
+    out[9 + l] = sqrt(gb2T - gbT * gbT);
+  }
+}
+
+double mo_bunching_factor(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double k) {
+  double q = 0.0, cr = 0.0, ci = 0.0;
+  for (long i = 0; i < n; i++) {
+    const double* c = rec + MO_REC * i;
+    if (!in_processor(zmin, Lz, zp0, zp1, c[3])) continue;
+    q += c[0];
+    cr += c[0] * cos(k * c[3]);
+    ci += c[0] * sin(k * c[3]);
+  }
+  return q != 0.0 ? sqrt(cr * cr + ci * ci) / q : 0.0;
+}

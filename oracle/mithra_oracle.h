@@ -149,6 +149,13 @@ long mo_erase_outside(double zmin, double Lz, double zp0, double zp1, double* re
  * slot.  Writes N*Nl powers into pG. */
 void mo_power_sample(const mo_power* p, unsigned nTime, const float* en, const float* bn, double* pG);
 
+/* Solver::bunchSample (src/solver.cpp:1582-1635) for one domain: out[0..2] <r>, [3..5] <gb>,
+ * [6..8] rms r, [9..11] rms gb, summed in particle order as the reference does. */
+void mo_bunch_sample(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double* out);
+
+/* |sum q exp(i k z)| / sum q over the particles of the domain, in particle order. */
+double mo_bunching_factor(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double k);
+
 /* Thread count used by the parallel loops (1 = serial, bitwise reproduction of the reference). */
 void mo_set_threads(int n);
 int mo_get_threads(void);

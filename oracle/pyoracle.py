@@ -135,6 +135,10 @@ def lib():
         _lib.mo_erase_outside.restype = l
         _lib.mo_power_sample.argtypes = [P(MoPower), C.c_uint, f, f, d]
         _lib.mo_set_threads.argtypes = [C.c_int]
+        dd = C.c_double
+        _lib.mo_bunch_sample.argtypes = [dd, dd, dd, dd, d, l, d]
+        _lib.mo_bunching_factor.argtypes = [dd, dd, dd, dd, d, l, dd]
+        _lib.mo_bunching_factor.restype = dd
     return _lib
 
 
@@ -372,3 +376,16 @@ class OracleRun:
         self.erase()
         self.time += self.dt
         self.n_time += 1
+
+
+def bunch_sample(m: dict, rec) -> np.ndarray:
+    """Solver::bunchSample moments (12 values) of particle records in the reference's order."""
+    rec = np.ascontiguousarray(rec, dtype=np.float64)
+    out = np.zeros(12)
+    lib().mo_bunch_sample(m["zmin"], m["Lz"], m["zp0"], m["zp1"], dptr(rec), rec.shape[0], dptr(out))
+    return out
+
+
+def bunching_factor(m: dict, rec, k: float) -> float:
+    rec = np.ascontiguousarray(rec, dtype=np.float64)
+    return lib().mo_bunching_factor(m["zmin"], m["Lz"], m["zp0"], m["zp1"], dptr(rec), rec.shape[0], float(k))

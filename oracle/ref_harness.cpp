@@ -16,8 +16,11 @@
  *   push    JOB IN OUT              load an/anp1/particles/timeBunch, one Solver::bunchUpdate
  *   deposit JOB IN OUT              load particles, currentReset + currentUpdate (+ currentCommunicate)
  *   power   JOB IN OUT K            K calls of Solver::powerSample on loaded field pairs
+ *   bunch   JOB IN OUT              Solver::bunchSample moments of loaded particles
  */
+#include <cmath>
 #include <cstdio>
+#include <fstream>
 #include <cstdlib>
 #include <cstring>
 #include <string>
@@ -359,6 +362,23 @@ int main(int argc, char** argv) {
     if (mesh.spaceCharge_) dump_scalar_field(jp(out, "fnp1.bin"), s->fnp1_);
     s->currentCommunicate();
     dump_particles(jp(out, "particles.bin"), s->chargeVectorn_);
+  } else if (mode == "bunch") {
+    // Solver::bunchSample on loaded particles; the moments it writes (4 digits) are dumped here
+    // at full precision from its own sb_ members: <r>, <gb>, rms r, rms gb.
+    std::string in = argv[3], out = argv[4];
+    mkdir(out.c_str(), 0755);
+    load_particles(jp(in, "particles.bin"), s->chargeVectorn_);
+    std::ofstream sink("/dev/null");
+    s->sb_.file = &sink;
+    s->bunchSample();
+    std::vector<double> v(12);
+    for (int l = 0; l < 3; l++) {
+      v[l] = s->sb_.rT[l];
+      v[3 + l] = s->sb_.gbT[l];
+      v[6 + l] = sqrt(s->sb_.r2T[l] - s->sb_.rT[l] * s->sb_.rT[l]);
+      v[9 + l] = sqrt(s->sb_.gb2T[l] - s->sb_.gbT[l] * s->sb_.gbT[l]);
+    }
+    write_raw(jp(out, "bunch.bin"), v.data(), v.size() * 8);
   } else if (mode == "power") {
     std::string in = argv[3], out = argv[4];
     int K = atoi(argv[5]);

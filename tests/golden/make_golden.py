@@ -36,6 +36,16 @@ def run(harness, *args, cwd):
                    stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
 
 
+def bunch_fixture(harness, job, dst, tmp, parts):
+    """Solver::bunchSample moments of the step-12 particles of the march."""
+    bin_ = os.path.join(tmp, "bunch_in")
+    os.makedirs(bin_, exist_ok=True)
+    parts.tofile(os.path.join(bin_, "particles.bin"))
+    run(harness, "bunch", job, bin_, os.path.join(tmp, "bunch_out"), cwd=tmp)
+    np.savez_compressed(os.path.join(dst, "bunch.npz"), particles=parts,
+                        moments=np.fromfile(os.path.join(tmp, "bunch_out", "bunch.bin")))
+
+
 def fixtures_for(harness, jobname, tag, with_kats=True):
     job = os.path.join(JOBS, jobname)
     dst = os.path.join(OUT, tag)
@@ -108,6 +118,7 @@ def fixtures_for(harness, jobname, tag, with_kats=True):
         run(harness, "deposit", job, din, os.path.join(tmp, "dep_out"), cwd=tmp)
         np.savez_compressed(os.path.join(dst, "deposit.npz"), particles=dep,
                             J=np.fromfile(os.path.join(tmp, "dep_out", "anp1.bin")))
+        bunch_fixture(harness, job, dst, tmp, ld(12, "particles").reshape(-1, 11))
     finally:
         shutil.rmtree(tmp)
 

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import mithra_gb300 as mg
+from oracle import pyoracle as po
 from tests._golden import BEAM_TAGS, TAGS, load, meta
 from tests.conftest import job, rel_l2
 
@@ -107,3 +108,16 @@ def test_fp32_beam_march(gpu_available, tag):
     print("%s: FP32 A relative L2 after 12 steps %.3e" % (tag, err))
     assert err <= BEAM_MARCH_RTOL
     assert ctx.download_particles().shape == run["particles12"].shape
+
+
+def test_fp32_bunch_diagnostics(gpu_available):
+    """Moments and bunching factor from the mixed form's cell + FP32 offset positions."""
+    tag = "kat-small-fd"
+    b, m = load(tag, "bunch"), meta(tag)
+    ctx = mg.Context.from_setup(mg.Setup.from_job(job(TAGS[tag][0])), mg.FP32)
+    ctx.upload_particles(b["particles"])
+    row = ctx.bunch_sample()
+    np.testing.assert_allclose(row[1:], b["moments"], rtol=1e-5, atol=1e-6 * np.abs(b["moments"]).max())
+    k = 2 * np.pi * m["gamma"] / m["und0_lu"]
+    ref = po.bunching_factor(m, b["particles"], k)
+    assert abs(ctx.bunching_factor(k) - ref) <= 1e-4 * ref

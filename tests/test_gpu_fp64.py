@@ -192,3 +192,18 @@ def test_beam_march_matches_reference(gpu_available, tag):
         assert_close_scaled(parts[:, col], ref[:, col], 1e-10, "particle column %d" % col)
     rows = ctx.power_rows().reshape(12, -1)
     assert_close_scaled(rows, run["power"], 1e-9, "power rows")
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_bunch_diagnostics(gpu_available, tag):
+    """Device bunch moments against the reference's Solver::bunchSample, and the bunching factor
+    against the oracle, on the reference's step-12 particles (compensated device sums agree with
+    the reference's ordered sums to rounding)."""
+    b, m = load(tag, "bunch"), meta(tag)
+    _, ctx = ctx_for(tag)
+    ctx.upload_particles(b["particles"])
+    row = ctx.bunch_sample()
+    np.testing.assert_allclose(row[1:], b["moments"], rtol=1e-12, atol=1e-12 * np.abs(b["moments"]).max())
+    k = 2 * np.pi * m["gamma"] / m["und0_lu"]
+    ref = po.bunching_factor(m, b["particles"], k)
+    assert abs(ctx.bunching_factor(k) - ref) <= 1e-11 * ref

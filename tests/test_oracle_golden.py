@@ -127,3 +127,22 @@ def test_oracle_seed_injection_is_active():
     for _ in range(12):
         r.step()
     assert not np.array_equal(r.an, run["an12"])
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_oracle_bunch_sample_matches_reference(tag):
+    """Solver::bunchSample moments of the step-12 particles, bit for bit."""
+    b = load(tag, "bunch")
+    assert np.array_equal(po.bunch_sample(meta(tag), b["particles"]), b["moments"])
+
+
+def test_oracle_bunching_factor_formula():
+    """The bunching factor restated with numpy (complex sum over the particles in the domain)."""
+    tag = "kat-small-fd"
+    m, p = meta(tag), load(tag, "bunch")["particles"]
+    k = 2 * np.pi * m["gamma"] / m["und0_lu"]
+    zr = np.fmod(p[:, 3] - m["zmin"], m["Lz"])
+    zr = np.where(zr < 0, zr + m["Lz"], zr) + m["zmin"]
+    sel = (zr >= m["zp0"]) & (zr < m["zp1"])
+    ref = abs(np.sum(p[sel, 0] * np.exp(1j * k * p[sel, 3]))) / p[sel, 0].sum()
+    assert abs(po.bunching_factor(m, p, k) - ref) <= 1e-12 * ref
