@@ -121,3 +121,32 @@ def test_fp32_bunch_diagnostics(gpu_available):
     k = 2 * np.pi * m["gamma"] / m["und0_lu"]
     ref = po.bunching_factor(m, b["particles"], k)
     assert abs(ctx.bunching_factor(k) - ref) <= 1e-4 * ref
+
+
+def test_fp32_error_statement_p_spectrum_bunching(gpu_available):
+    """The mixed form against the FP64 form over the full 48x48x384 march (20-point spectrum at
+    the power plane): saturated power, the P(z) curve at the resonant frequency, the final
+    spectrum and the final bunching factor at the ponderomotive bunch-frame wavenumber."""
+    s = mg.Setup.from_job(job("fel-ir-48x48x384-spectrum.job"))
+    m = s.meta()
+    nl = int(m["rp0_Nl"])
+    w = np.array([m["rp0_w%d" % i] for i in range(nl)])
+    # ponderomotive bunching in the moving frame: period lambda_u / (2 gamma)
+    k = 4 * np.pi * m["gamma"] / m["und0_lu"]
+    res = {}
+    for prec in (mg.FP64, mg.FP32):
+        fd = mg.FdTd(s, precision=prec)
+        rows = fd.solve().reshape(-1, 1 + nl)
+        res[prec] = (rows[:, 1:], fd.ctx.bunching_factor(k))
+        fd.ctx.close()
+    (p64, b64), (p32, b32) = res[mg.FP64], res[mg.FP32]
+    assert p64.shape == p32.shape and np.isfinite(p32).all()
+    ir = int(np.argmin(np.abs(w - w.mean())))   # centre of the 0.9 .. 1.1 sweep
+    psat = abs(p32[:, ir].max() - p64[:, ir].max()) / p64[:, ir].max()
+    curve = np.abs(p32[:, ir] - p64[:, ir]).max() / np.abs(p64[:, ir]).max()
+    spec = np.linalg.norm(p32[-1] - p64[-1]) / np.linalg.norm(p64[-1])
+    bunch = abs(b32 - b64) / b64
+    print("mixed vs FP64 form: P_sat %.2e, P(z) curve %.2e (max abs diff / max P), final spectrum %.2e "
+          "(relative L2), bunching factor %.2e (%.4g vs %.4g)" % (psat, curve, spec, bunch, b32, b64))
+    assert psat <= PSAT_RTOL
+    assert curve <= 0.05 and spec <= 0.05 and bunch <= 0.05
