@@ -181,6 +181,11 @@ int mithra_gpu_recycle(mithra_ctx* ctx);
  * timeBunch_, row[1..3] <r>, row[4..6] <gb>, row[7..9] rms r, row[10..12] rms gb (charge-weighted;
  * compensated FP64 sums). */
 int mithra_gpu_bunch_sample(mithra_ctx* ctx, double* row);
+/* FdTd::fieldSample (src/fdtd.cpp:851-950) at n points (x, y, z in the bunch frame): out[9 p ..]
+ * = E, B, A^n interpolated with the reference's trilinear weights (boosted-frame values; the
+ * reference's file adds the lab transform and unit factors).  Evaluates E/B on every interior
+ * node first; points outside the mesh give NaN. */
+int mithra_gpu_field_sample(mithra_ctx* ctx, const double* points, size_t n, double* out);
 /* Bunching factor |sum q exp(i k z)| / sum q at wavenumber k (bunch-frame z), the quantity read
  * from the reference's bunch dumps (Solver::bunchProfile, src/solver.cpp:1763-1792). */
 int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b);

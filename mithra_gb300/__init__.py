@@ -112,6 +112,7 @@ _SIGS = {
     "mithra_gpu_power_sample": [_vp],
     "mithra_gpu_power_sample_noalloc": [_vp],
     "mithra_gpu_bunch_sample": [_vp, _dp],
+    "mithra_gpu_field_sample": [_vp, _dp, C.c_size_t, _dp],
     "mithra_gpu_bunching_factor": [_vp, C.c_double, _dp],
     "mithra_gpu_field_shift": [_vp],
     "mithra_gpu_current_update": [_vp],
@@ -449,6 +450,13 @@ class Context:
         row = np.zeros(13)
         self.call("mithra_gpu_bunch_sample", dptr(row))
         return row
+
+    def field_sample(self, points) -> np.ndarray:
+        """FdTd::fieldSample: E, B, A^n at each point (n, 3) -> (n, 9)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((pts.shape[0], 9))
+        self.call("mithra_gpu_field_sample", dptr(pts), pts.shape[0], dptr(out))
+        return out
 
     def bunching_factor(self, k: float) -> float:
         """|sum q exp(i k z)| / sum q over the particles of the domain (bunch-frame z)."""

@@ -138,4 +138,38 @@ __global__ void k_diag_finish(const double2* partial, int nblocks, int nv, doubl
   out[q] = a.s + a.c;
 }
 
+// FdTd::fieldSample (src/fdtd.cpp:851-950): E, B and A^n at each point, trilinear with the
+// reference's weights (modf of the cell coordinate); out[9 p + 0..8] = E, B, A.
+template <typename TE, typename TA>
+__global__ void k_field_sample(GridDev g, const TE* __restrict__ E, const TE* __restrict__ B, const TA* __restrict__ A,
+                               const double* __restrict__ pts, int n, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const double* r = pts + 3 * p;
+  double c;
+  const double dxr = modf((r[0] - g.xmin) / g.dx, &c); const int i = (int)c;
+  const double dyr = modf((r[1] - g.ymin) / g.dy, &c); const int j = (int)c;
+  const double dzr = modf((r[2] - g.zmin) / g.dz, &c); const int k = (int)c;
+  double* o = out + 9 * (long long)p;
+  if (i < 0 || j < 0 || k < 0 || i > g.N0 - 2 || j > g.N1 - 2 || k > g.N2 - 2) {  // outside the mesh
+    for (int q = 0; q < 9; q++) o[q] = nan("");
+    return;
+  }
+  const long long m = node_index(g, k, i, j), sI = g.P1, sK = g.plane, cs = g.cstride;
+  const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+  const double w[8] = {(1.0 - dxr) * (1.0 - dyr) * (1.0 - dzr), dxr * (1.0 - dyr) * (1.0 - dzr),
+                       (1.0 - dxr) * dyr * (1.0 - dzr),         dxr * dyr * (1.0 - dzr),
+                       (1.0 - dxr) * (1.0 - dyr) * dzr,         dxr * (1.0 - dyr) * dzr,
+                       (1.0 - dxr) * dyr * dzr,                 dxr * dyr * dzr};
+  for (int comp = 0; comp < 3; comp++) {
+    double e = 0.0, b = 0.0, a = 0.0;
+    for (int q = 0; q < 8; q++) {
+      e += w[q] * (double)E[comp * cs + nd[q]];
+      b += w[q] * (double)B[comp * cs + nd[q]];
+      a += w[q] * (double)A[comp * cs + nd[q]];
+    }
+    o[comp] = e; o[3 + comp] = b; o[6 + comp] = a;
+  }
+}
+
 }  // namespace mithra

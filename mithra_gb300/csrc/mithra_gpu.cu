@@ -1123,6 +1123,30 @@ int mithra_gpu_bunch_sample(mithra_ctx* ctx, double* row) {
   return MITHRA_OK;
 }
 
+int mithra_gpu_field_sample(mithra_ctx* ctx, const double* points, size_t n, double* out) {
+  if (!ctx || (n && (!points || !out))) return MITHRA_ERR_ARG;
+  if (n == 0) return MITHRA_OK;
+  if (n > (1u << 24)) return fail(ctx, MITHRA_ERR_ARG, "too many sampling points (%zu)", n);
+  // E/B at every interior node from the current A^{n+1}, A^n: the nodes the reference's lazy
+  // evaluation reaches from a sampling point (src/fdtd.cpp:878-885).
+  int r = ctx->precision == MITHRA_PRECISION_FP32 ? fp32_eval_eb(ctx, true) : stage_eval_eb(ctx, true);
+  if (r) return r;
+  double* buf = nullptr;  // points, then results
+  if ((r = mithra::staging(ctx, n * 12 * sizeof(double), (void**)&buf))) return r;
+  CK(cudaMemcpyAsync(buf, points, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  const int blocks = (int)((n + 127) / 128);
+  if (ctx->precision == MITHRA_PRECISION_FP64)
+    k_field_sample<double, double><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E64, ctx->B64, ctx->A[ctx->idx[1]], buf,
+                                                                    (int)n, buf + 3 * n);
+  else
+    k_field_sample<float, float><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E, ctx->B, fp32_field(ctx, 1), buf,
+                                                                  (int)n, buf + 3 * n);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, buf + 3 * n, n * 9 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return MITHRA_OK;
+}
+
 int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b) {
   if (!ctx || !b) return MITHRA_ERR_ARG;
   double s[3];

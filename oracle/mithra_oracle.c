@@ -1001,3 +1001,33 @@ double mo_bunching_factor(double zmin, double Lz, double zp0, double zp1, const 
   }
   return q != 0.0 ? sqrt(cr * cr + ci * ci) / q : 0.0;
 }
+
+void mo_field_sample(const mo_field* f, const double* an, const float* en, const float* bn, const double* pts,
+                     long n, double* out) {
+  const long N1 = f->N1, N1N0 = (long)f->N1 * f->N0;
+  for (long p = 0; p < n; p++) {
+    const double* r = pts + 3 * p;
+    double c1;
+    double dxr = modf((r[0] - f->xmin) / f->dx, &c1); int i = (int)c1;
+    double dyr = modf((r[1] - f->ymin) / f->dy, &c1); int j = (int)c1;
+    double dzr = modf((r[2] - f->zmin) / f->dz, &c1); int k = (int)c1;
+    long m = (long)(k - f->k0) * N1N0 + (long)i * N1 + j;
+    const long nd[8] = {m, m + N1, m + 1, m + N1 + 1, m + N1N0, m + N1N0 + N1, m + N1N0 + 1, m + N1N0 + N1 + 1};
+    const double w[8] = {(1.0 - dxr) * (1.0 - dyr) * (1.0 - dzr), dxr * (1.0 - dyr) * (1.0 - dzr),
+                         (1.0 - dxr) * dyr * (1.0 - dzr),         dxr * dyr * (1.0 - dzr),
+                         (1.0 - dxr) * (1.0 - dyr) * dzr,         dxr * (1.0 - dyr) * dzr,
+                         (1.0 - dxr) * dyr * dzr,                 dxr * dyr * dzr};
+    double* o = out + 9 * p;
+    for (int c = 0; c < 3; c++) {
+      o[c] = w[0] * en[3 * nd[0] + c];
+      o[3 + c] = w[0] * bn[3 * nd[0] + c];
+      o[6 + c] = w[0] * an[3 * nd[0] + c];
+    }
+    for (int q = 1; q < 8; q++)
+      for (int c = 0; c < 3; c++) {
+        o[c] += w[q] * en[3 * nd[q] + c];
+        o[3 + c] += w[q] * bn[3 * nd[q] + c];
+        o[6 + c] += w[q] * an[3 * nd[q] + c];
+      }
+  }
+}

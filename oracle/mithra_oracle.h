@@ -149,6 +149,11 @@ long mo_erase_outside(double zmin, double Lz, double zp0, double zp1, double* re
  * slot.  Writes N*Nl powers into pG. */
 void mo_power_sample(const mo_power* p, unsigned nTime, const float* en, const float* bn, double* pG);
 
+/* FdTd::fieldSample (src/fdtd.cpp:851-950) at n points (x, y, z): out[9 p ..] = E (from en),
+ * B (from bn), A^n (from an), trilinear with the weights of the reference. */
+void mo_field_sample(const mo_field* f, const double* an, const float* en, const float* bn, const double* pts,
+                     long n, double* out);
+
 /* Solver::bunchSample (src/solver.cpp:1582-1635) for one domain: out[0..2] <r>, [3..5] <gb>,
  * [6..8] rms r, [9..11] rms gb, summed in particle order as the reference does. */
 void mo_bunch_sample(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double* out);

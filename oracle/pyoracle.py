@@ -137,6 +137,7 @@ def lib():
         _lib.mo_set_threads.argtypes = [C.c_int]
         dd = C.c_double
         _lib.mo_bunch_sample.argtypes = [dd, dd, dd, dd, d, l, d]
+        _lib.mo_field_sample.argtypes = [P(MoField), d, f, f, d, l, d]
         _lib.mo_bunching_factor.argtypes = [dd, dd, dd, dd, d, l, dd]
         _lib.mo_bunching_factor.restype = dd
     return _lib
@@ -389,3 +390,13 @@ def bunch_sample(m: dict, rec) -> np.ndarray:
 def bunching_factor(m: dict, rec, k: float) -> float:
     rec = np.ascontiguousarray(rec, dtype=np.float64)
     return lib().mo_bunching_factor(m["zmin"], m["Lz"], m["zp0"], m["zp1"], dptr(rec), rec.shape[0], float(k))
+
+
+def field_sample(m: dict, an, en, bn, pts, solver: int = 0) -> np.ndarray:
+    """FdTd::fieldSample interpolation (E, B, A^n) at points, as (n, 9)."""
+    fp = field_params(m, solver, 2)
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    out = np.zeros((pts.shape[0], 9))
+    lib().mo_field_sample(C.byref(fp), dptr(np.ascontiguousarray(an, dtype=np.float64)), fptr(en), fptr(bn),
+                          dptr(pts), pts.shape[0], dptr(out))
+    return out

@@ -17,6 +17,7 @@
  *   deposit JOB IN OUT              load particles, currentReset + currentUpdate (+ currentCommunicate)
  *   power   JOB IN OUT K            K calls of Solver::powerSample on loaded field pairs
  *   bunch   JOB IN OUT              Solver::bunchSample moments of loaded particles
+ *   fieldsample JOB IN OUT          FdTd::fieldSample at loaded points on loaded A^n, A^{n+1}
  */
 #include <cmath>
 #include <cstdio>
@@ -362,6 +363,32 @@ int main(int argc, char** argv) {
     if (mesh.spaceCharge_) dump_scalar_field(jp(out, "fnp1.bin"), s->fnp1_);
     s->currentCommunicate();
     dump_particles(jp(out, "particles.bin"), s->chargeVectorn_);
+  } else if (mode == "fieldsample") {
+    // FdTd::fieldSample at each loaded point (one point per call), on loaded A^n / A^{n+1}; the
+    // interpolated et, bt, at it leaves in sf_ are dumped at full precision.
+    std::string in = argv[3], out = argv[4];
+    mkdir(out.c_str(), 0755);
+    load_vec3(jp(in, "an.bin"), s->an_);
+    load_vec3(jp(in, "anp1.bin"), s->anp1_);
+    std::vector<char> raw = read_raw(jp(in, "points.bin"));
+    const double* pts = (const double*)raw.data();
+    const size_t np = raw.size() / 24;
+    std::fill(s->pic_.begin(), s->pic_.end(), false);
+    bind_field_pointers(s);
+    eval_boundary_planes(s);
+    std::ofstream sink("/dev/null");
+    s->sf_.file = &sink;
+    s->sf_.N = 1;
+    s->seed_.samplingPosition_.assign(1, FieldVector<Double>(0.0));
+    std::vector<double> v;
+    for (size_t n = 0; n < np; n++) {
+      for (int c = 0; c < 3; c++) s->seed_.samplingPosition_[0][c] = pts[3 * n + c];
+      s->fieldSample();
+      for (int c = 0; c < 3; c++) v.push_back(s->sf_.et[c]);
+      for (int c = 0; c < 3; c++) v.push_back(s->sf_.bt[c]);
+      for (int c = 0; c < 3; c++) v.push_back(s->sf_.at[c]);
+    }
+    write_raw(jp(out, "sample.bin"), v.data(), v.size() * 8);
   } else if (mode == "bunch") {
     // Solver::bunchSample on loaded particles; the moments it writes (4 digits) are dumped here
     // at full precision from its own sb_ members: <r>, <gb>, rms r, rms gb.

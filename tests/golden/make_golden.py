@@ -46,6 +46,21 @@ def bunch_fixture(harness, job, dst, tmp, parts):
                         moments=np.fromfile(os.path.join(tmp, "bunch_out", "bunch.bin")))
 
 
+def field_sample_fixture(harness, job, dst, tmp, an, anp1, meta, rng):
+    """FdTd::fieldSample at 24 random points inside the interior cells, on random potentials."""
+    fin = os.path.join(tmp, "fs_in")
+    os.makedirs(fin, exist_ok=True)
+    lo = np.array([meta["xmin"] + meta["dx"], meta["ymin"] + meta["dy"], meta["zmin"] + meta["dz"]])
+    hi = np.array([meta["xmax"] - meta["dx"], meta["ymax"] - meta["dy"], meta["zmax"] - meta["dz"]])
+    pts = lo + (hi - lo) * rng.uniform(0, 1, size=(24, 3))
+    an.tofile(os.path.join(fin, "an.bin"))
+    anp1.tofile(os.path.join(fin, "anp1.bin"))
+    pts.tofile(os.path.join(fin, "points.bin"))
+    run(harness, "fieldsample", job, fin, os.path.join(tmp, "fs_out"), cwd=tmp)
+    np.savez_compressed(os.path.join(dst, "fieldsample.npz"), an=an, anp1=anp1, points=pts,
+                        sample=np.fromfile(os.path.join(tmp, "fs_out", "sample.bin")).reshape(-1, 9))
+
+
 def fixtures_for(harness, jobname, tag, with_kats=True):
     job = os.path.join(JOBS, jobname)
     dst = os.path.join(OUT, tag)
@@ -119,6 +134,7 @@ def fixtures_for(harness, jobname, tag, with_kats=True):
         np.savez_compressed(os.path.join(dst, "deposit.npz"), particles=dep,
                             J=np.fromfile(os.path.join(tmp, "dep_out", "anp1.bin")))
         bunch_fixture(harness, job, dst, tmp, ld(12, "particles").reshape(-1, 11))
+        field_sample_fixture(harness, job, dst, tmp, a_n, a_np1, meta, rng)
     finally:
         shutil.rmtree(tmp)
 

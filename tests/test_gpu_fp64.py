@@ -207,3 +207,14 @@ def test_bunch_diagnostics(gpu_available, tag):
     k = 2 * np.pi * m["gamma"] / m["und0_lu"]
     ref = po.bunching_factor(m, b["particles"], k)
     assert abs(ctx.bunching_factor(k) - ref) <= 1e-11 * ref
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_field_sample_matches_reference(gpu_available, tag):
+    """Device field sampling (E, B, A^n at 24 points) against the reference's FdTd::fieldSample."""
+    fs = load(tag, "fieldsample")
+    _, ctx = ctx_for(tag)
+    ctx.upload_fields(fs["anp1"], fs["an"], None)
+    out = ctx.field_sample(fs["points"])
+    for c in range(9):
+        assert_close_scaled(out[:, c], fs["sample"][:, c], EB_RTOL, "sample column %d" % c)

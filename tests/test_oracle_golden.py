@@ -146,3 +146,16 @@ def test_oracle_bunching_factor_formula():
     sel = (zr >= m["zp0"]) & (zr < m["zp1"])
     ref = abs(np.sum(p[sel, 0] * np.exp(1j * k * p[sel, 3]))) / p[sel, 0].sum()
     assert abs(po.bunching_factor(m, p, k) - ref) <= 1e-12 * ref
+
+
+@pytest.mark.parametrize("tag", sorted(TAGS))
+def test_oracle_field_sample_matches_reference(tag):
+    """FdTd::fieldSample at 24 points on random potentials, bit for bit."""
+    m, fs = meta(tag), load(tag, "fieldsample")
+    nodes = fs["an"].size // 3
+    en = np.zeros(nodes * 3, dtype=np.float32)
+    bn = np.zeros(nodes * 3, dtype=np.float32)
+    fp = po.field_params(m, TAGS[tag][1], 2)
+    po.lib().mo_eval_eb(po.C.byref(fp), po.dptr(fs["anp1"].copy()), po.dptr(fs["an"].copy()), None, po.fptr(en),
+                        po.fptr(bn))
+    assert np.array_equal(po.field_sample(m, fs["an"], en, bn, fs["points"], TAGS[tag][1]), fs["sample"])
