@@ -27,6 +27,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
@@ -55,7 +57,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS) + ["sweep-192"])
+    ap.add_argument("--autotune-steps", type=int, default=0,
+                    help="sweep-192: autotune every instance on this many steps per candidate shape")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -384,12 +388,65 @@ def run_gpu(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def run_sweep(args, dist):
+    """192 seeded FEL designs (mixed form) stepped as one batch: one graph launch per field step."""
+    import tempfile
+
+    import mithra_gb300 as mg
+    from mithra_gb300 import sweep
+    params = sweep.sweep_parameters(192)
+    setups = sweep.make_setups(params, tempfile.mkdtemp(prefix="mithra-sweep-"))
+    batch, ctxs, tuned = sweep.make_batch(setups, mg.FP32, dist.local, args.autotune_steps)
+    units, steps_to_end, total_nodes, total_particles = 0, [], 0, 0
+    for s, c in zip(setups, ctxs):
+        npart = c.particle_count()
+        nodes, pushes, _ = units_per_step(s.meta(), npart)
+        units += nodes + pushes
+        total_nodes += nodes
+        total_particles += npart
+        steps_to_end.append(sweep.steps_to_exit(s, c))
+    batch.run(args.warmup)
+    dist.barrier()
+    with ClockSampler(dist.local) as clk:
+        ms = batch.run_timed(args.steps)
+    dist.barrier()
+    ms_max = dist.max(ms)
+    step_s = ms_max / 1e3 / args.steps
+    value = dist.world * units / step_s
+    # FEL runs per hour: every design marched to its undulator exit.  Lock-step: the batch runs
+    # until its longest design ends; refilled: finished slots take new designs at once.
+    runs_lockstep = dist.world * len(ctxs) * 3600.0 / (max(steps_to_end) * step_s)
+    runs_refill = dist.world * len(ctxs) * 3600.0 / (float(np.mean(steps_to_end)) * step_s)
+    batch.close()
+    for c in ctxs:
+        c.close()
+    if dist.rank != 0:
+        return
+    out = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (192 seeded designs, Halton bunches)",
+        "config": {"workload": "sweep-192", "instances": len(ctxs), "precision": "fp32",
+                   "nodes": total_nodes, "particles": total_particles,
+                   "autotune_steps": args.autotune_steps, "parallelism": "one graph launch per step for all instances",
+                   "l2": "inputs larger than L2"},
+        "fel_runs_per_hour": {"lockstep": runs_lockstep, "refilled": runs_refill,
+                              "steps_to_exit": {"min": min(steps_to_end), "mean": float(np.mean(steps_to_end)),
+                                                "max": max(steps_to_end)}},
+        "tuning": [[t.blocks_per_sm, t.slab_planes, ms] for t, ms in tuned][:8],
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload == "sweep-192":
+            run_sweep(args, dist)
         else:
             run_gpu(args, dist)
     finally:

@@ -241,6 +241,35 @@ int mithra_host_free(void* p);
 /* Parses a MITHRA job file (src/readdata.cpp:10-53, src/datainput.cpp:18-751) and runs the
  * reference's FP64 initialisation (Solver::initialize, src/solver.cpp:547-595) on the host.
  * The setup object holds the descriptors above, the initial fields and the particles. */
+/* ---- launch shapes ------------------------------------------------------------------------ */
+
+/* Launch shapes of a context (no counterpart in the reference).  blocks_per_sm caps the grid of
+ * the particle and boundary kernels (grid-stride loops); slab_planes is the z extent of the tiles
+ * of the mixed form's bulk-tensor stencil.  Results do not depend on them beyond the order of
+ * atomic additions. */
+typedef struct {
+  int32_t blocks_per_sm;       /* 2 .. 64, default 16 */
+  int32_t slab_planes;         /* 16 .. 256, default 64 */
+} mithra_tuning;
+int mithra_gpu_set_tuning(mithra_ctx* ctx, const mithra_tuning* t);
+int mithra_gpu_get_tuning(const mithra_ctx* ctx, mithra_tuning* t);
+/* Times every candidate shape on `steps_per_trial` real field steps of the march (the steps are
+ * part of the simulation) and keeps the fastest; writes the chosen shape and its ms per step. */
+int mithra_gpu_autotune(mithra_ctx* ctx, int steps_per_trial, mithra_tuning* chosen, double* ms_per_step);
+
+/* ---- batched instances ---------------------------------------------------------------------- */
+
+/* Several independent contexts on one device (a parameter sweep: each with its own mesh, bunch
+ * and undulator) stepped together: every field step of all instances is one CUDA graph launch,
+ * the per-instance step graphs being child graphs of it, so the instances' kernels run
+ * concurrently.  No counterpart in the reference (one job per run).  The contexts must be in the
+ * same step phase (buffer rotation and sort parity: contexts created and stepped together are). */
+typedef struct mithra_batch mithra_batch;
+int mithra_batch_create(mithra_ctx* const* ctxs, int n, mithra_batch** out);
+int mithra_batch_run(mithra_batch* b, int64_t nsteps);
+int mithra_batch_run_timed(mithra_batch* b, int64_t nsteps, double* device_ms);
+int mithra_batch_destroy(mithra_batch* b);
+
 typedef struct mithra_setup mithra_setup;
 int mithra_setup_from_job(const char* job_path, mithra_setup** out, char* err, size_t err_len);
 int mithra_setup_destroy(mithra_setup* s);

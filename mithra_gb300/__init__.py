@@ -20,7 +20,7 @@ import numpy as np
 
 from . import build as _build
 
-__all__ = ["Setup", "Context", "FdTd", "FdTdSC", "MithraError", "PinnedArray", "lib", "FP64", "FP32"]
+__all__ = ["Setup", "Context", "Batch", "FdTd", "FdTdSC", "MithraError", "PinnedArray", "lib", "FP64", "FP32"]
 
 FP64 = 0
 FP32 = 1
@@ -70,6 +70,10 @@ class UndulatorDesc(C.Structure):
                 ("length", C.c_double), ("dist", C.c_double), ("theta", C.c_double), ("beam", BeamDesc)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("blocks_per_sm", C.c_int32), ("slab_planes", C.c_int32)]
+
+
 class PowerDesc(C.Structure):
     _fields_ = [("N", C.c_int32), ("Nl", C.c_int32), ("Nf", C.c_int32), ("pc", C.c_double),
                 ("z", C.POINTER(C.c_double)), ("twiddle_re", C.POINTER(C.c_double)),
@@ -112,6 +116,13 @@ _SIGS = {
     "mithra_gpu_power_sample": [_vp],
     "mithra_gpu_power_sample_noalloc": [_vp],
     "mithra_gpu_bunch_sample": [_vp, _dp],
+    "mithra_gpu_set_tuning": [_vp, _P(Tuning)],
+    "mithra_gpu_get_tuning": [_vp, _P(Tuning)],
+    "mithra_gpu_autotune": [_vp, C.c_int, _P(Tuning), _dp],
+    "mithra_batch_create": [_P(_vp), C.c_int, _P(_vp)],
+    "mithra_batch_run": [_vp, C.c_int64],
+    "mithra_batch_run_timed": [_vp, C.c_int64, _dp],
+    "mithra_batch_destroy": [_vp],
     "mithra_gpu_field_sample": [_vp, _dp, C.c_size_t, _dp],
     "mithra_gpu_bunching_factor": [_vp, C.c_double, _dp],
     "mithra_gpu_field_shift": [_vp],
@@ -445,6 +456,22 @@ class Context:
     def power_sample(self):
         self.call("mithra_gpu_power_sample")
 
+    def set_tuning(self, blocks_per_sm: int = 16, slab_planes: int = 64):
+        self.call("mithra_gpu_set_tuning", C.byref(Tuning(blocks_per_sm, slab_planes)))
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self.call("mithra_gpu_get_tuning", C.byref(t))
+        return t
+
+    def autotune(self, steps_per_trial: int = 2):
+        """Times the candidate launch shapes on real steps of the march; keeps the fastest.
+        Returns (Tuning, ms per step)."""
+        t = Tuning()
+        ms = np.zeros(1)
+        self.call("mithra_gpu_autotune", int(steps_per_trial), C.byref(t), dptr(ms))
+        return t, float(ms[0])
+
     def bunch_sample(self) -> np.ndarray:
         """Solver::bunchSample row: timeBunch, <r>(3), <gb>(3), rms r(3), rms gb(3)."""
         row = np.zeros(13)
@@ -496,6 +523,47 @@ class Context:
 
     def synchronize(self):
         self.call("mithra_gpu_synchronize")
+
+
+class Batch:
+    """Independent contexts on one device stepped together: one graph launch per field step
+    advances every instance (a parameter sweep)."""
+
+    def __init__(self, contexts):
+        self.contexts = list(contexts)
+        arr = (_vp * len(self.contexts))(*[c._h for c in self.contexts])
+        self._h = _vp()
+        r = lib().mithra_batch_create(arr, len(self.contexts), C.byref(self._h))
+        if r != 0:
+            raise MithraError("mithra_batch_create failed with status %d" % r)
+
+    def _ck(self, r, what):
+        if r != 0:
+            for c in self.contexts:   # a failing instance reports through its own context
+                buf = C.create_string_buffer(1024)
+                lib().mithra_gpu_last_error(c._h, buf, len(buf))
+                if buf.value:
+                    raise MithraError("%s: %s (status %d)" % (what, buf.value.decode(errors="replace"), r))
+            raise MithraError("%s failed with status %d" % (what, r))
+
+    def run(self, nsteps: int):
+        self._ck(lib().mithra_batch_run(self._h, int(nsteps)), "mithra_batch_run")
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = np.zeros(1)
+        self._ck(lib().mithra_batch_run_timed(self._h, int(nsteps), dptr(ms)), "mithra_batch_run_timed")
+        return float(ms[0])
+
+    def close(self):
+        if self._h:
+            lib().mithra_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class FdTd:

@@ -92,6 +92,8 @@ struct mithra_ctx {
   bool particles_loaded = false;
   std::string err;
   int sm_count = 152;
+  unsigned graph_generation = 0;  // incremented whenever the captured step graphs are dropped
+  mithra_tuning tune{16, 64};     // launch shapes (mithra_gpu_set_tuning / mithra_gpu_autotune)
   int launches_per_step = 0;
   int launch_counter = 0;
   void* diag_partial = nullptr;  // bunch diagnostics: per-block compensated sums (allocated on first use)
@@ -145,6 +147,16 @@ int timed(mithra_ctx* ctx, const char* name, Fn fn) {
 
 // TF/SF injection of the seed into the new vector potential (float or double storage).
 int stage_seed(mithra_ctx* ctx, void* anp1);
+
+// One field step as a graph, for composing several contexts into one launch (batch.cu):
+// step_key names the rotation / sort-parity state a captured step belongs to, capture_step
+// records one step without applying it, after_step applies the host-side state change of a
+// launched step, prepare_run / finish_run bracket a run of steps (row log, state checks).
+int step_key(const mithra_ctx* ctx);
+int capture_step(mithra_ctx* ctx, cudaGraph_t* out);
+void after_step(mithra_ctx* ctx);
+int prepare_run(mithra_ctx* ctx, int64_t nsteps);
+int finish_run(mithra_ctx* ctx);
 
 // Mixed-precision form (fp32_form.cu).
 int fp32_alloc(mithra_ctx* ctx);

@@ -78,7 +78,8 @@ int run_interior_tma(mithra_ctx* ctx, const PotentialArgs<float>& p) {
   a.np1 = p.np1; a.N0 = g.N0; a.N1 = g.N1; a.N2 = g.N2; a.P1 = g.P1; a.plane = g.plane; a.cstride = g.cstride;
   a.a0 = p.k.a0; a.a1 = p.k.a1; a.a2 = p.k.a2; a.a3 = p.k.a3; a.asrc = p.asrc; a.al = p.k.al; a.be = p.k.be;
   a.error = f.tma_error;
-  const int nslab = (g.N2 - 2 + TMA_KS - 1) / TMA_KS;
+  a.ks = ctx->tune.slab_planes;
+  const int nslab = (g.N2 - 2 + a.ks - 1) / a.ks;
   dim3 grd((g.N1 - 2 + TMA_TJ - 1) / TMA_TJ, (g.N0 - 2 + TMA_TI - 1) / TMA_TI, 3 * nslab);
   const CUtensorMap* an = (const CUtensorMap*)f.map_an[ctx->idx[1]];
   const CUtensorMap* am = (const CUtensorMap*)f.map_c[ctx->idx[2]];

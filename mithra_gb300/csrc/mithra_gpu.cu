@@ -38,7 +38,7 @@ int fail(mithra_ctx* c, int code, const char* fmt, ...) {
 
 int grid_stride_blocks(const mithra_ctx* ctx, long long work, int block) {
   long long b = (work + block - 1) / block;
-  long long cap = (long long)ctx->sm_count * 16;
+  long long cap = (long long)ctx->sm_count * ctx->tune.blocks_per_sm;
   return (int)std::max<long long>(1, std::min(b, cap));
 }
 
@@ -99,6 +99,7 @@ int staging(mithra_ctx* ctx, size_t bytes, void** p) {
 void invalidate_graphs(mithra_ctx* ctx) {
   for (auto& gr : ctx->graph)
     if (gr) { cudaGraphExecDestroy(gr); gr = nullptr; }
+  ctx->graph_generation++;
 }
 
 }  // namespace mithra
@@ -342,6 +343,40 @@ int check_state(mithra_ctx* ctx) {
 }  // namespace
 
 namespace mithra {
+
+int step_key(const mithra_ctx* ctx) { return ctx->idx[0] + 3 * ctx->f32.parity; }
+
+int capture_step(mithra_ctx* ctx, cudaGraph_t* out) {
+  const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
+  const Fp32State saved_f32 = ctx->f32;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  ctx->launch_counter = 0;
+  const int r = enqueue_step(ctx);
+  ctx->launches_per_step = ctx->launch_counter;
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, out);
+  // enqueue_step rotated the indices (and swapped the particle buffer sets) while recording;
+  // restore them so that a launch of the graph followed by after_step applies them once.
+  ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
+  ctx->f32 = saved_f32;
+  if (r) return r;
+  if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+  return MITHRA_OK;
+}
+
+void after_step(mithra_ctx* ctx) {
+  rotate(ctx);
+  if (ctx->precision == MITHRA_PRECISION_FP32) fp32_after_step(ctx);
+}
+
+int prepare_run(mithra_ctx* ctx, int64_t nsteps) {
+  if (!ctx->particles_loaded) return fail(ctx, MITHRA_ERR_STATE, "no particles uploaded");
+  int r = ensure_rows(ctx, nsteps);
+  if (r) return r;
+  if (!ctx->power.empty()) ctx->rows_pending += nsteps;
+  return MITHRA_OK;
+}
+
+int finish_run(mithra_ctx* ctx) { return check_state(ctx); }
 
 int stage_seed(mithra_ctx* ctx, void* anp1) {
   const GridDev& g = ctx->g;
@@ -928,30 +963,15 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
     return check_state(ctx);
   }
   for (int64_t s = 0; s < nsteps; s++) {
-    const int key = ctx->idx[0] + 3 * ctx->f32.parity;
+    const int key = step_key(ctx);
     if (!ctx->graph[key]) {
       cudaGraph_t graph;
-      const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
-      const int saved_parity = ctx->f32.parity;
-      const Fp32State saved_f32 = ctx->f32;
-      CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      ctx->launch_counter = 0;
-      r = enqueue_step(ctx);
-      ctx->launches_per_step = ctx->launch_counter;
-      cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
-      if (r) return r;
-      if (ce != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      if ((r = capture_step(ctx, &graph))) return r;
       CK(cudaGraphInstantiate(&ctx->graph[key], graph, 0));
       CK(cudaGraphDestroy(graph));
-      // enqueue_step rotated the indices (and swapped the particle buffer sets) while recording;
-      // restore them so that the launch below applies those changes exactly once.
-      ctx->idx[0] = saved[0]; ctx->idx[1] = saved[1]; ctx->idx[2] = saved[2];
-      ctx->f32 = saved_f32;
-      ctx->f32.parity = saved_parity;
     }
     CK(cudaGraphLaunch(ctx->graph[key], ctx->stream));
-    rotate(ctx);
-    if (ctx->precision == MITHRA_PRECISION_FP32) fp32_after_step(ctx);
+    after_step(ctx);
   }
   return check_state(ctx);
 }

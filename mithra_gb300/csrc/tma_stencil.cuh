@@ -21,7 +21,7 @@ constexpr int TMA_TJ = 32;               // tile width along j (threads along x)
 constexpr int TMA_TI = 16;               // tile height along i
 constexpr int TMA_BW = TMA_TJ + 4;       // box width: j0-1 .. j0+TJ, rounded up to 16 bytes
 constexpr int TMA_BH = TMA_TI + 2;       // A^n box height incl. halo rows
-constexpr int TMA_KS = 64;               // planes per slab
+constexpr int TMA_KS = 64;               // default planes per slab (TmaStencilArgs::ks)
 constexpr unsigned TMA_SPIN_LIMIT = 20000000u;
 
 struct TmaStencilArgs {
@@ -29,6 +29,7 @@ struct TmaStencilArgs {
   int N0, N1, N2, P1;
   long long plane, cstride;
   float a0, a1, a2, a3, asrc, al, be;
+  int ks;            // planes per slab (the z extent of a CTA's tile)
   int* error;        // set to 1 when a barrier wait gives up
 };
 
@@ -93,12 +94,12 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
   __shared__ int s_abort;
 
   const int tx = threadIdx.x % TMA_TJ, ty = threadIdx.x / TMA_TJ;
-  const int nslab = (a.N2 - 2 + TMA_KS - 1) / TMA_KS;
+  const int nslab = (a.N2 - 2 + a.ks - 1) / a.ks;
   const int comp = blockIdx.z / nslab, slab = blockIdx.z % nslab;
   const int jb = blockIdx.x * TMA_TJ;   // box origin along j (= j0 - 1, 16-byte aligned)
   const int ib = blockIdx.y * TMA_TI;   // A^n box origin along i (= i0 - 1)
-  const int k_first = 1 + slab * TMA_KS;
-  const int k_last = min(a.N2 - 2, k_first + TMA_KS - 1);
+  const int k_first = 1 + slab * a.ks;
+  const int k_last = min(a.N2 - 2, k_first + a.ks - 1);
   const int j = jb + 1 + tx, i = ib + 1 + ty;
   const unsigned bytes_an = TMA_BW * TMA_BH * 4, bytes_c = TMA_BW * TMA_TI * 4;
 

@@ -1,0 +1,146 @@
+"""Parameter sweeps of FEL designs run as one batch of independent instances.
+
+Each instance is a job of the 48x48x384 FEL family with its own undulator, bunch and mesh,
+drawn from fixed ranges with a seeded generator:
+
+    gamma 80 .. 400, undulator parameter K 0.8 .. 2.0, period 1.5 .. 3 cm (30 periods),
+    charge 50 .. 500 pC, relative energy spread 1e-5 .. 1e-3,
+    transverse cells 32 .. 96, longitudinal cells 128 .. 768, macro-particles 5e4 .. 1e6.
+
+The jobs are ordinary job files (written to a work directory), set up on the host in parallel
+and stepped together on one device by `mithra_gb300.Batch`.
+"""
+from __future__ import annotations
+
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from . import FP32, Batch, Context, Setup
+
+ELECTRONS_PER_PC = 1.0 / 1.602e-7
+PERIODS = 30
+
+
+def sweep_parameters(n: int = 192, seed: int = 20261204) -> list[dict]:
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(dict(
+            index=i,
+            gamma=float(rng.uniform(80.0, 400.0)),
+            K=float(rng.uniform(0.8, 2.0)),
+            lambda_u=float(rng.uniform(1.5e4, 3.0e4)),           # um
+            charge_pc=float(rng.uniform(50.0, 500.0)),
+            energy_spread=float(10.0 ** rng.uniform(-5.0, -3.0)),
+            n_transverse=int(rng.integers(32, 97)),
+            n_longitudinal=int(rng.integers(128, 769)),
+            particles=int(rng.integers(50_000, 1_000_001)),
+        ))
+    return out
+
+
+def job_text(p: dict) -> str:
+    """Job file of one sweep instance (the 48x48x384 FEL job with the instance's parameters)."""
+    lx, lz = 2400.0, 180.0
+    dx, dz = lx / p["n_transverse"], lz / p["n_longitudinal"]
+    # march from the bunch's start to the undulator exit (plus the 2-period default gap)
+    total_time = (PERIODS + 2) * p["lambda_u"] / 299.792458 * 1.05
+    return f"""# sweep instance {p['index']}
+MESH
+{{
+  length-scale              = MICROMETER
+  time-scale                = PICOSECOND
+  mesh-lengths              = ( {lx}, {lx}, {lz} )
+  mesh-resolution           = ( {dx!r}, {dx!r}, {dz!r} )
+  mesh-center               = ( 0.0, 0.0, 0.0 )
+  total-time                = {total_time!r}
+  bunch-time-step           = 1.6
+  mesh-truncation-order     = 2
+  space-charge              = false
+  solver                    = FD
+}}
+
+BUNCH
+{{
+  bunch-initialization
+  {{
+    type                    = ellipsoid
+    distribution            = uniform
+    charge                  = {p['charge_pc'] * ELECTRONS_PER_PC!r}
+    number-of-particles     = {p['particles']}
+    gamma                   = {p['gamma']!r}
+    direction               = ( 0.0, 0.0, 1.0 )
+    position                = ( 0.0, 0.0, 0.0 )
+    sigma-position          = ( 200.0, 200.0, 30.0 )
+    sigma-momentum          = ( 0.005, 0.005, {p['energy_spread'] * p['gamma']!r} )
+    transverse-truncation   = 800.0
+    longitudinal-truncation = 60.0
+    shot-noise              = true
+  }}
+}}
+
+UNDULATOR
+{{
+  static-undulator
+  {{
+    undulator-parameter     = {p['K']!r}
+    period                  = {p['lambda_u']!r}
+    length                  = {PERIODS}
+    polarization-angle      = 0.0
+  }}
+}}
+
+FEL-OUTPUT
+{{
+  radiation-power
+  {{
+    sample                  = true
+    type                    = at-point
+    directory               = ./
+    base-name               = power-sampling/power
+    plane-position          = 60.0
+    normalized-frequency    = 1.0
+  }}
+}}
+"""
+
+
+def make_setups(params: list[dict], workdir: str, threads: int | None = None) -> list[Setup]:
+    """Writes the job files and runs the host initialisation of every instance in parallel."""
+    os.makedirs(workdir, exist_ok=True)
+    paths = []
+    for p in params:
+        path = os.path.join(workdir, "sweep-%03d.job" % p["index"])
+        with open(path, "w") as f:
+            f.write(job_text(p))
+        paths.append(path)
+    with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 4) as ex:
+        return list(ex.map(Setup.from_job, paths))
+
+
+def make_batch(setups: list[Setup], precision: int = FP32, device: int = 0, autotune_steps: int = 0):
+    """Contexts for every instance (prelude marched), optionally autotuned, and their batch."""
+    contexts = []
+    for s in setups:
+        c = Context.from_setup(s, precision, device)
+        c.run_prelude()
+        contexts.append(c)
+    tuned = []
+    if autotune_steps > 0:
+        for c in contexts:
+            tuned.append(c.autotune(autotune_steps))
+    # tuning marches each instance by the same number of steps, so they stay in one step phase
+    return Batch(contexts), contexts, tuned
+
+
+def steps_to_exit(setup: Setup, ctx: Context) -> int:
+    """Field steps left until the job's total time (the reference's `while (time_ < totalTime)`)."""
+    t = ctx.get_time()
+    total, dt = setup.total_time(), setup.meta()["dt"]
+    time, n = t.time, 0
+    while time < total:
+        time += dt
+        n += 1
+    return n
