@@ -620,6 +620,13 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
   for (int o = 0; o < n; o++) {
     const mithra_power_desc& d = outs[o];
     if (d.N <= 0 || d.Nl < 0 || d.Nf <= 0 || !d.z || (d.Nl && (!d.twiddle_re || !d.twiddle_im))) return MITHRA_ERR_ARG;
+    // The sample kernel reduces the Nl powers of a block in shared memory (kPowerBlock x Nl doubles).
+    const size_t shm = (size_t)kPowerBlock * d.Nl * sizeof(double);
+    if (shm > 220 * 1024) return fail(ctx, MITHRA_ERR_ARG, "%d frequencies exceed the power sampler's limit of 220", d.Nl);
+    if (shm > 48 * 1024) {
+      CK(cudaFuncSetAttribute(k_power_sample<kPowerBlock, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+      CK(cudaFuncSetAttribute(k_power_sample<kPowerBlock, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    }
     PowerOut po;
     std::vector<int> pk(d.N), ps(d.N);
     std::vector<double> pz(d.N);

@@ -41,12 +41,25 @@ def sweep_parameters(n: int = 192, seed: int = 20261204) -> list[dict]:
     return out
 
 
-def job_text(p: dict) -> str:
-    """Job file of one sweep instance (the 48x48x384 FEL job with the instance's parameters)."""
-    lx, lz = 2400.0, 180.0
+def job_text(p: dict, spectrum_points: int = 0) -> str:
+    """Job file of one sweep instance (the 48x48x384 FEL job with the instance's parameters).
+    p may set "periods" (default 30), "sigma_r" (transverse rms size in um, default 200),
+    "lz" (mesh length along z in um, default 180; the bunch's rms length is lz / 6, truncated at
+    lz / 3, and the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD);
+    spectrum_points > 0 samples the power at that many normalized frequencies in 0.9 .. 1.1
+    instead of at 1.0 only."""
+    lx, lz = 2400.0, float(p.get("lz", 180.0))
     dx, dz = lx / p["n_transverse"], lz / p["n_longitudinal"]
+    periods = int(p.get("periods", PERIODS))
+    sr = float(p.get("sigma_r", 200.0))
+    solver = p.get("solver", "FD")
     # march from the bunch's start to the undulator exit (plus the 2-period default gap)
-    total_time = (PERIODS + 2) * p["lambda_u"] / 299.792458 * 1.05
+    total_time = (periods + 2) * p["lambda_u"] / 299.792458 * 1.05
+    if spectrum_points > 0:
+        freq = ("minimum-normalized-frequency = 0.9\n    maximum-normalized-frequency = 1.1\n"
+                "    number-of-frequency-points   = %d" % spectrum_points)
+    else:
+        freq = "normalized-frequency    = 1.0"
     return f"""# sweep instance {p['index']}
 MESH
 {{
@@ -59,7 +72,7 @@ MESH
   bunch-time-step           = 1.6
   mesh-truncation-order     = 2
   space-charge              = false
-  solver                    = FD
+  solver                    = {solver}
 }}
 
 BUNCH
@@ -73,10 +86,10 @@ BUNCH
     gamma                   = {p['gamma']!r}
     direction               = ( 0.0, 0.0, 1.0 )
     position                = ( 0.0, 0.0, 0.0 )
-    sigma-position          = ( 200.0, 200.0, 30.0 )
+    sigma-position          = ( {sr!r}, {sr!r}, {lz / 6.0!r} )
     sigma-momentum          = ( 0.005, 0.005, {p['energy_spread'] * p['gamma']!r} )
-    transverse-truncation   = 800.0
-    longitudinal-truncation = 60.0
+    transverse-truncation   = {4.0 * sr!r}
+    longitudinal-truncation = {lz / 3.0!r}
     shot-noise              = true
   }}
 }}
@@ -87,7 +100,7 @@ UNDULATOR
   {{
     undulator-parameter     = {p['K']!r}
     period                  = {p['lambda_u']!r}
-    length                  = {PERIODS}
+    length                  = {periods}
     polarization-angle      = 0.0
   }}
 }}
@@ -100,21 +113,21 @@ FEL-OUTPUT
     type                    = at-point
     directory               = ./
     base-name               = power-sampling/power
-    plane-position          = 60.0
-    normalized-frequency    = 1.0
+    plane-position          = {lz / 3.0!r}
+    {freq}
   }}
 }}
 """
 
 
-def make_setups(params: list[dict], workdir: str, threads: int | None = None) -> list[Setup]:
+def make_setups(params: list[dict], workdir: str, threads: int | None = None, spectrum_points: int = 0) -> list[Setup]:
     """Writes the job files and runs the host initialisation of every instance in parallel."""
     os.makedirs(workdir, exist_ok=True)
     paths = []
     for p in params:
         path = os.path.join(workdir, "sweep-%03d.job" % p["index"])
         with open(path, "w") as f:
-            f.write(job_text(p))
+            f.write(job_text(p, spectrum_points))
         paths.append(path)
     with ThreadPoolExecutor(max_workers=threads or os.cpu_count() or 4) as ex:
         return list(ex.map(Setup.from_job, paths))
