@@ -26,6 +26,7 @@ PushF32 push_constants(const mithra_ctx* ctx) {
   C.und0_dist = P.und0_dist;
   C.gamma_f = (float)P.gamma; C.bc_f = (float)(P.beta * P.c0); C.gdz = (float)(P.gamma * g.dz);
   C.zmin_f = (float)g.zmin; C.dz_f = (float)g.dz; C.und0_dist_f = (float)P.und0_dist;
+  C.rb0_f = ctx->und_host.empty() ? 0.0f : (float)ctx->und_host[0].rb;
   C.P64 = P;
   C.xmin_d = g.xmin; C.ymin_d = g.ymin; C.dxd = g.dx; C.dyd = g.dy;
   return C;

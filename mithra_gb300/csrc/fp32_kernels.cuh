@@ -70,6 +70,7 @@ struct PushF32 {
   double und0_dist;
   float gamma_f, bc_f, gdz;      // gamma, beta*c0 and gamma*dz in FP32
   float zmin_f, dz_f, und0_dist_f;
+  float rb0_f;                   // rb of the first undulator module
   PushDev P64;                   // FP64 parameters for the laser beams (optical undulators, external fields)
   double xmin_d, ymin_d, dxd, dyd;
 };
@@ -99,10 +100,23 @@ __global__ void k_undulator_table(const UndDev* __restrict__ und, int n_und, int
   }
 }
 
+// Lab-frame z, gamma (z + beta c0 (timeBunch + dt_)), of a particle outside the mesh's z range,
+// in FP64.  Out of line, so that the FP64 instructions run only for the (rare) particles that
+// need them instead of being predicated into every thread's path.
+__device__ __noinline__ double lab_z_outside(double zmin, double dzd, double gamma, double tshift, int k, float fz) {
+  return gamma * (zmin + ((double)k + (double)fz) * dzd + tshift);
+}
+
+// Undulator lz and phase ku*lz reduced modulo 2 pi, from the FP64 lab z (particles outside the mesh).
+__device__ __noinline__ float2 undulator_phase_outside(double labz, double rb, double ku) {
+  const double lzd = labz - rb;
+  const double ph = ku * lzd;
+  return make_float2((float)lzd, (float)fma(-rint(ph * (1.0 / (2.0 * kPI))), 2.0 * kPI, ph));
+}
+
 __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, const UndTableEntry* __restrict__ table,
-                                              int n_und, int N2, float gdz, int k, float fz, double zd_slow,
-                                              double tshift, double gamma, float x, float y, float* bt, float* et,
-                                              float gamma_f, float bc_f) {
+                                              int n_und, int N2, float gdz, int k, float fz, double labz_outside,
+                                              float x, float y, float* bt, float* et, float gamma_f, float bc_f) {
   for (int u = 0; u < n_und; u++) {
     const UndDev& U = und[u];
     if (U.type != 0) continue;
@@ -112,10 +126,9 @@ __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, co
       lz = fmaf(gdz, fz, te.lz);
       phase = fmaf(U.ku_f * gdz, fz, te.phase);
     } else {  // outside the mesh along z (rare): form the phase in FP64
-      const double lzd = gamma * (zd_slow + tshift) - U.rb;
-      const double ph = U.ku * lzd;
-      lz = (float)lzd;
-      phase = (float)fma(-rint(ph * (1.0 / (2.0 * kPI))), 2.0 * kPI, ph);
+      const float2 lp = undulator_phase_outside(labz_outside, U.rb, U.ku);
+      lz = lp.x;
+      phase = lp.y;
     }
     const float ct = U.ct_f, st = U.st_f, ku = U.ku_f, b0 = U.b0_f;
     const float ly = x * ct + y * st;
@@ -196,8 +209,9 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
       const bool b1z = (k >= 0 && k <= C.N2 - 2);
       float bt[3] = {0.f, 0.f, 0.f}, et[3] = {0.f, 0.f, 0.f};
       const bool k_in = (k >= 0 && k <= C.N2);
-      const double zd_slow = k_in ? 0.0 : C.zmin + ((double)k + (double)fz) * C.dzd;
-      undulator_f32(und, table, C.n_und, C.N2, C.gdz, k, fz, zd_slow, tshift, C.gamma, x, y, bt, et, C.gamma_f, C.bc_f);
+      double labz_outside = 0.0;
+      if (!k_in) labz_outside = lab_z_outside(C.zmin, C.dzd, C.gamma, tshift, k, fz);
+      undulator_f32(und, table, C.n_und, C.N2, C.gdz, k, fz, labz_outside, x, y, bt, et, C.gamma_f, C.bc_f);
       if (BEAMS) {
         // Laser beams in FP64: their phase, like the undulator's, is a large lab-frame coordinate.
         const double xd = C.xmin_d + ((double)i + (double)fx) * C.dxd;
@@ -233,8 +247,8 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
         // lz without the module offset rb: rb of the first module is zero after the shift of
         // src/solver.cpp:184-185, so it is the first table entry's lz.
         float lz;
-        if (k_in) lz = fmaf(C.gdz, fz, table[k].lz + (float)und[0].rb);
-        else lz = (float)(C.gamma * (zd_slow + tshift));
+        if (k_in) lz = fmaf(C.gdz, fz, table[k].lz + C.rb0_f);
+        else lz = (float)labz_outside;
         e = (lz > -C.und0_dist_f) ? 1 : 0;
         pt.e[p] = e;
       } else {
