@@ -189,6 +189,20 @@ int mithra_gpu_field_sample(mithra_ctx* ctx, const double* points, size_t n, dou
 /* Bunching factor |sum q exp(i k z)| / sum q at wavenumber k (bunch-frame z), the quantity read
  * from the reference's bunch dumps (Solver::bunchProfile, src/solver.cpp:1763-1792). */
 int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b);
+/* Lab-frame screens, Solver::screenProfile (src/solver.cpp:2205-2257), screens from
+ * initializeScreenProfile (src/solver.cpp:2145-2199): from now on every step (and every step of
+ * mithra_gpu_run_prelude) records the particles whose lab z passes one of the n screens lz[]
+ * (um from the undulator start, in the order given).  capacity = records kept per screen (0:
+ * the particle capacity of the context); further crossings are counted and reported by
+ * mithra_gpu_screen_records as MITHRA_ERR_CAPACITY.  n = 0 removes the screens.  Replaces the
+ * files the reference opens per screen: their rows come from mithra_gpu_screen_records. */
+int mithra_gpu_set_screens(mithra_ctx* ctx, const double* lz, int n, long long capacity);
+/* Drops the records collected so far (the screens stay). */
+int mithra_gpu_screen_clear(mithra_ctx* ctx);
+/* Records of screen `screen` in the reference's file order (steps in order, particles in list
+ * order): out[7 r ..] = x, y, t (lab, interpolated to the screen), gbx, gby, gbz (lab), nTime_
+ * of the step.  out = NULL returns the count in *n_rows. */
+int mithra_gpu_screen_records(mithra_ctx* ctx, int screen, double* out, long long cap_rows, long long* n_rows);
 /* Solver::powerSample (src/radiation.cpp:127-232); the row is appended to the device row log. */
 int mithra_gpu_power_sample(mithra_ctx* ctx);
 /* mithra_gpu_power_sample without any device allocation.  No counterpart in the reference: it

@@ -125,6 +125,9 @@ _SIGS = {
     "mithra_batch_destroy": [_vp],
     "mithra_gpu_field_sample": [_vp, _dp, C.c_size_t, _dp],
     "mithra_gpu_bunching_factor": [_vp, C.c_double, _dp],
+    "mithra_gpu_set_screens": [_vp, _dp, C.c_int, C.c_longlong],
+    "mithra_gpu_screen_clear": [_vp],
+    "mithra_gpu_screen_records": [_vp, C.c_int, _dp, C.c_longlong, C.POINTER(C.c_longlong)],
     "mithra_gpu_field_shift": [_vp],
     "mithra_gpu_current_update": [_vp],
     "mithra_gpu_advance_time": [_vp],
@@ -278,6 +281,12 @@ class Setup:
         lib().mithra_setup_fields(self._h, dptr(anp1), dptr(an), dptr(anm1))
         return anp1, an, anm1
 
+    def screens(self) -> np.ndarray:
+        """Lab z of the job's screens (bunch-profile-lab-frame groups), in the reference's
+        order: FEL-OUTPUT entries in order, each entry's positions sorted."""
+        m = self.meta()
+        return np.array([m["scr%d_z" % i] for i in range(int(m.get("n_screens", 0)))])
+
     def meta(self) -> dict:
         need = C.c_size_t()
         lib().mithra_setup_meta(self._h, None, 0, C.byref(need))
@@ -288,6 +297,19 @@ class Setup:
             k, v = line.split()
             out[k] = float(v)
         return out
+
+
+def format_screen_text(rows, first_in_file: bool = True) -> str:
+    """Screen rows (x, y, t, gbx, gby, gbz) as the reference writes them
+    (src/solver.cpp:2186-2191, :2230-2252): scientific with 15 decimals, tab-separated, one
+    crossing per line; the stream's width of 40 applies once, to the first value of the file."""
+    out = []
+    for r, row in enumerate(np.asarray(rows, dtype=np.float64).reshape(-1, 6)):
+        vals = ["%.15e" % v for v in row]
+        if r == 0 and first_in_file:
+            vals[0] = vals[0].rjust(40)
+        out.append("\t".join(vals) + "\n")
+    return "".join(out)
 
 
 class Context:
@@ -491,6 +513,43 @@ class Context:
         self.call("mithra_gpu_bunching_factor", float(k), dptr(b))
         return float(b[0])
 
+    def set_screens(self, lz, capacity: int = 0):
+        """Lab-frame screens (Solver::screenProfile): every following step, and every step of
+        run_prelude, records the particles whose lab z passes a screen.  lz in um from the
+        undulator start; capacity = records kept per screen (0: the particle capacity)."""
+        z = np.ascontiguousarray(lz, dtype=np.float64)
+        self.n_screens = len(z)
+        self.call("mithra_gpu_set_screens", dptr(z) if len(z) else None, len(z), int(capacity))
+
+    def screen_clear(self):
+        self.call("mithra_gpu_screen_clear")
+
+    def screen_records(self, screen: int) -> np.ndarray:
+        """Records of one screen in the reference's file order: (n, 7) rows of x, y, t, gbx,
+        gby, gbz (lab) and the step's nTime_."""
+        n = C.c_longlong(0)
+        self.call("mithra_gpu_screen_records", int(screen), None, 0, C.byref(n))
+        out = np.zeros((n.value, 7))
+        if n.value:
+            self.call("mithra_gpu_screen_records", int(screen), dptr(out), n.value, C.byref(n))
+        return out
+
+    def write_screen_files(self, base: str) -> list:
+        """The reference's screen files, base + "-p0-screen<i>.txt" (src/solver.cpp:2186-2191,
+        :2230-2252): per crossing x, y, t, gbx, gby, gbz tab-separated in %.15e, the first value
+        of a file right-aligned in 40 characters (the stream's one-shot width).  Returns the
+        file names."""
+        names = []
+        d = os.path.dirname(base)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        for i in range(getattr(self, "n_screens", 0)):
+            name = "%s-p0-screen%d.txt" % (base, i)
+            with open(name, "w") as f:
+                f.write(format_screen_text(self.screen_records(i)[:, :6]))
+            names.append(name)
+        return names
+
     def power_sample_noalloc(self):
         """power_sample with no device allocation: partial sums in a fixed per-device array."""
         self.call("mithra_gpu_power_sample_noalloc")
@@ -579,6 +638,9 @@ class FdTd:
         self.setup = setup
         self.meta = setup.meta()
         self.ctx = Context.from_setup(setup, self.precision if precision is None else precision, device, capacity_factor)
+        screens = setup.screens()
+        if len(screens):  # Solver::initializeScreenProfile: record crossings from the start
+            self.ctx.set_screens(screens)
 
     def currentReset(self):  # noqa: N802 - reference name
         pass  # folded into currentUpdate, as the reference calls them back to back

@@ -100,6 +100,13 @@ struct mithra_ctx {
   double* diag_out = nullptr;
   void* staging = nullptr;  // device staging buffer for host-layout transfers
   size_t staging_bytes = 0;
+  // lab-frame screens (mithra_gpu_set_screens): records appended by k_screen every step
+  int n_screens = 0;
+  long long screen_cap = 0;              // records per screen
+  double* screen_lz = nullptr;           // [n_screens]
+  double* screen_rec = nullptr;          // [n_screens][screen_cap][6]
+  long long* screen_key = nullptr;       // [n_screens][screen_cap]
+  unsigned long long* screen_count = nullptr;  // [n_screens]
 };
 
 namespace mithra {

@@ -64,7 +64,25 @@ struct DiagParticles {
   const long long* cell;
   const float *fx, *fy, *fz, *gxf, *gyf, *gzf, *qf;
   const uint8_t* status;
+  // previous position (rnm) and list order, for the screen crossing
+  const double *mx, *my, *mz;
+  const long long* mcell;
+  const float *mfx, *mfy, *mfz;
+  const int* id;
   double xmin, ymin, zmin, dx, dy, dz;
+  __device__ __forceinline__ void get_rnm(long long p, double* r) const {
+    if (x) {
+      r[0] = mx[p]; r[1] = my[p]; r[2] = mz[p];
+    } else {
+      int i, j, k;
+      unpack_cell(mcell[p], i, j, k);
+      r[0] = xmin + ((double)i + (double)mfx[p]) * dx;
+      r[1] = ymin + ((double)j + (double)mfy[p]) * dy;
+      r[2] = zmin + ((double)k + (double)mfz[p]) * dz;
+    }
+  }
+  // position in the reference's particle list (erased particles never reach here)
+  __device__ __forceinline__ long long order(long long p) const { return x ? p : (long long)id[p]; }
   __device__ __forceinline__ void get(long long p, double* r, double* g, double& qq) const {
     if (x) {
       r[0] = x[p]; r[1] = y[p]; r[2] = z[p];
@@ -127,6 +145,66 @@ __global__ void __launch_bounds__(kDiagBlock) k_bunching(GridDev g, DiagParticle
     csum_add(v[2], q * sn);
   }
   csum_block_store<3>(v, partial);
+}
+
+// Lab-frame screens of Solver::screenProfile (src/solver.cpp:2205-2257).  rec holds 6 doubles
+// per record (x, y, t, gbx, gby, gbz_lab), key the sort key (n_time << 40 | list order) that
+// restores the reference's file order (steps in order, particles in list order).
+struct ScreenDev {
+  double gamma, beta, c0, dt_shift, dt;
+  int n;
+  const double* lz;
+  double* rec;
+  long long* key;
+  unsigned long long* count;
+  long long cap;  // records per screen
+};
+
+// Solver::interp (src/solver.cpp:2283-2286) without contraction.
+__device__ __forceinline__ double screen_interp(double x0, double x1, double y0, double y1, double x) {
+  return __dadd_rn(y0, __dmul_rn(__ddiv_rn(__dsub_rn(x, x0), __dsub_rn(x1, x0)), __dsub_rn(y1, y0)));
+}
+
+// Every particle in the domain whose lab z (gamma (z + beta c0 t)) passes a screen between the
+// start (rnm, timeBunch - dt) and the end (rnp, timeBunch) of the step is recorded: x, y and the
+// lab time interpolated linearly in lab z to the screen, the momentum after the step and its lab
+// longitudinal component.  The reference's operation order is kept, without contraction, so the
+// FP64 form reproduces its values from the same positions.
+__global__ void __launch_bounds__(256) k_screen(GridDev g, DiagParticles P, ScreenDev S, const StateDev* st) {
+  const long long n = st->n_particles;
+  const double tb = st->time_bunch;
+  const long long step = st->n_time;
+  const double bc = __dmul_rn(S.beta, S.c0), boc = __ddiv_rn(S.beta, S.c0);
+  const double tm0 = __dadd_rn(__dsub_rn(tb, S.dt), S.dt_shift);        // timeBunch_ - dt + dt_
+  const double tp0 = __dadd_rn(tb, S.dt_shift);                           // timeBunch_ + dt_
+  const double tt_m = __dsub_rn(__dadd_rn(tb, S.dt_shift), S.dt);         // timeBunch_ + dt_ - dt
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    if (P.status[p] & 1) continue;
+    double r[3], gb[3], q;
+    P.get(p, r, gb, q);
+    if (!in_processor(g, r[2])) continue;
+    double rm[3];
+    P.get_rnm(p, rm);
+    const double lzm = __dmul_rn(S.gamma, __dadd_rn(rm[2], __dmul_rn(bc, tm0)));
+    const double lzp = __dmul_rn(S.gamma, __dadd_rn(r[2], __dmul_rn(bc, tp0)));
+    for (int i = 0; i < S.n; i++) {
+      const double lzs = S.lz[i];
+      if (lzm >= lzs || lzp < lzs) continue;
+      const unsigned long long slot = atomicAdd(&S.count[i], 1ull);
+      if ((long long)slot >= S.cap) continue;  // counted; the host reports the overflow
+      double* o = S.rec + ((long long)i * S.cap + (long long)slot) * 6;
+      o[0] = screen_interp(lzm, lzp, rm[0], r[0], lzs);
+      o[1] = screen_interp(lzm, lzp, rm[1], r[1], lzs);
+      const double tm = __dmul_rn(S.gamma, __dadd_rn(tt_m, __dmul_rn(boc, rm[2])));
+      const double tp = __dmul_rn(S.gamma, __dadd_rn(tp0, __dmul_rn(boc, r[2])));
+      o[2] = screen_interp(lzm, lzp, tm, tp, lzs);
+      o[3] = gb[0];
+      o[4] = gb[1];
+      const double n2 = __dadd_rn(__dadd_rn(__dmul_rn(gb[0], gb[0]), __dmul_rn(gb[1], gb[1])), __dmul_rn(gb[2], gb[2]));
+      o[5] = __dmul_rn(S.gamma, __dadd_rn(gb[2], __dmul_rn(S.beta, __dsqrt_rn(__dadd_rn(1.0, n2)))));
+      S.key[(long long)i * S.cap + (long long)slot] = (step << 40) | P.order(p);
+    }
+  }
 }
 
 // Adds the block results in block order; out[q] = compensated total of quantity q.

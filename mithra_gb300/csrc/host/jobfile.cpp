@@ -503,11 +503,28 @@ void read_fel(Cursor& c, Job& J) {
       } while (c.cur() != "}");
       J.fel.push_back(f);
     }
-    // Power visualisation, radiation energy and lab-frame screens are diagnostics outside the
-    // time-marching path.  Their groups are accepted; the radiation-energy group, which the
-    // reference parses into the radiation-power fields (src/datainput.cpp:706-717), adds an
-    // output entry the same way.
-    static const char* other[] = {"power-visualization", "radiation-energy", "bunch-profile-lab-frame"};
+    // Lab-frame screens, src/datainput.cpp:726-745.
+    if (c.cur() == "bunch-profile-lab-frame") {
+      c.open("bunch-profile-lab-frame");
+      FEL f;
+      ScreenProfile& sp = f.screenProfile;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "sample") sp.sampling = bool_of(l);
+        else if (n == "directory") sp.directory = string_of(l);
+        else if (n == "base-name") sp.basename = string_of(l);
+        else if (n == "position") sp.pos.push_back(double_of(l));
+        else if (n == "rhythm") sp.rhythm = double_of(l);
+        else die(n + " is not defined in the bunch-profile-lab-frame group.");
+        c.next();
+      } while (c.cur() != "}");
+      J.fel.push_back(f);
+    }
+    // Power visualisation and radiation energy are diagnostics outside the time-marching path.
+    // Their groups are accepted; the radiation-energy group, which the reference parses into the
+    // radiation-power fields (src/datainput.cpp:706-717), adds an output entry the same way.
+    static const char* other[] = {"power-visualization", "radiation-energy"};
     for (const char* grp : other) {
       if (c.cur() != grp) continue;
       c.open(grp);

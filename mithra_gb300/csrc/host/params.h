@@ -109,8 +109,16 @@ struct RadiationPower {  // FreeElectronLaser::RadiationSampling, src/classes.cp
   unsigned lambdaRes = 0;
 };
 
+struct ScreenProfile {  // FreeElectronLaser::ScreenProfile, src/classes.h:554-572, src/classes.cpp:1324-1331
+  bool sampling = false;
+  std::string directory = "./", basename;
+  std::vector<double> pos;  // lab z of the screens, from the undulator start
+  double rhythm = 0.0;
+};
+
 struct FEL {
   RadiationPower radiationPower;
+  ScreenProfile screenProfile;
 };
 
 struct Job {

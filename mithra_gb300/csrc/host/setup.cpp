@@ -641,6 +641,26 @@ void Setup::initialize() {
     power_fel_index.push_back((int)jf);
   }
 
+  // Lab-frame screens, Solver::initializeScreenProfile (src/solver.cpp:2145-2199): the given
+  // positions plus, with a rhythm, 0, rhythm, 2 rhythm, ... up to the undulator end, sorted.  The
+  // reference bounds the rhythm by undulator_.end(), one past the last module (undefined); the
+  // last module is used here.
+  for (size_t jf = 0; jf < job.fel.size(); jf++) {
+    const ScreenProfile& sp = job.fel[jf].screenProfile;
+    if (!sp.sampling) continue;
+    std::vector<double> pos = sp.pos;
+    if (sp.rhythm > 0.0 && !job.undulators.empty()) {
+      const Undulator& U = job.undulators.back();
+      for (double z = 0.0; z < U.rb + U.length * U.lu; z += sp.rhythm) pos.push_back(z);
+    }
+    std::sort(pos.begin(), pos.end());
+    if (pos.empty()) die("No position is set for the screen although the screen sampling is activated !!!");
+    for (double z : pos) {
+      screen_z.push_back(z);
+      screen_fel.push_back((int)jf);
+    }
+  }
+
   // Solver::shiftBackInTime, src/solver.cpp:1184-1206.
   if (mesh.timeShift != 0.0) {
     timem1 -= mesh.timeShift;
@@ -759,6 +779,12 @@ std::string Setup::meta() const {
     for (int i = 0; i < pc.Nl; i++) kv(p + "w" + std::to_string(i), pc.w[i]);
     for (int i = 0; i < pc.N; i++) kv(p + "z" + std::to_string(i), pc.z[i]);
   }
+  for (size_t i = 0; i < screen_z.size(); i++) {
+    const std::string p = "scr" + std::to_string(i) + "_";
+    kv(p + "z", screen_z[i]);
+    kv(p + "fel", (double)screen_fel[i]);
+  }
+  kv("n_screens", (double)screen_z.size());
   return o.str();
 }
 

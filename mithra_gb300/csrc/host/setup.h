@@ -39,6 +39,8 @@ struct Setup {
   double uc_dv = 0, uc_rc = 0, ub_dtb = 0, ub_r1 = 0, ub_r2 = 0;
   std::vector<double> an, anm1;  // initial potentials (seed fill), reference AoS layout; empty = zero
   std::vector<PowerCfg> power;   // one per FEL entry with radiation-power sampling
+  std::vector<double> screen_z;  // lab z of the screens (FEL entries in order, positions sorted)
+  std::vector<int> screen_fel;   // FEL entry of each screen
   std::vector<int> power_fel_index;
 
   void initialize();

@@ -217,6 +217,21 @@ int stage_power(mithra_ctx* ctx) {
   return MITHRA_OK;
 }
 
+DiagParticles diag_particles(const mithra_ctx* ctx);
+
+// Solver::screenProfile (src/solver.cpp:2205-2257), when screens are set.
+int stage_screen(mithra_ctx* ctx) {
+  if (ctx->n_screens == 0) return MITHRA_OK;
+  ScreenDev S;
+  S.gamma = ctx->P.gamma; S.beta = ctx->P.beta; S.c0 = ctx->P.c0; S.dt_shift = ctx->P.dt_shift; S.dt = ctx->g.dt;
+  S.n = ctx->n_screens; S.lz = ctx->screen_lz; S.rec = ctx->screen_rec; S.key = ctx->screen_key;
+  S.count = ctx->screen_count; S.cap = ctx->screen_cap;
+  const DiagParticles P = diag_particles(ctx);
+  return timed(ctx, "screen", [&] {
+    k_screen<<<grid_stride_blocks(ctx, (long long)ctx->capacity, 256), 256, 0, ctx->stream>>>(ctx->g, P, S, ctx->st);
+  });
+}
+
 void rotate(mithra_ctx* ctx) {
   const int np1 = ctx->idx[0], n = ctx->idx[1], nm1 = ctx->idx[2];
   ctx->idx[0] = nm1;
@@ -251,7 +266,8 @@ int n_substeps(const mithra_ctx* ctx) {
 }
 
 // The body of the main loop of Solver::solve (src/solver.cpp:1300-1399), diagnostics other
-// than the power sample omitted.  Ends with the buffer rotation of FdTd::fieldShift.
+// than the screens and the power sample omitted.  Ends with the buffer rotation of
+// FdTd::fieldShift.
 int enqueue_step(mithra_ctx* ctx) {
   int r;
   if ((r = stage_field_update(ctx))) return r;
@@ -260,6 +276,7 @@ int enqueue_step(mithra_ctx* ctx) {
     if ((r = stage_push(ctx, s == 0))) return r;
   if (ns == 0 && (r = stage_save_positions(ctx))) return r;
   if ((r = stage_erase(ctx))) return r;
+  if ((r = stage_screen(ctx))) return r;
   if ((r = stage_power(ctx))) return r;
   rotate(ctx);
   if ((r = stage_current(ctx))) return r;
@@ -522,6 +539,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
   cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev); cudaFree(ctx->Jedge);
   cudaFree(ctx->diag_partial); cudaFree(ctx->diag_out);
+  cudaFree(ctx->screen_lz); cudaFree(ctx->screen_rec); cudaFree(ctx->screen_key); cudaFree(ctx->screen_count);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
     void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
@@ -1052,6 +1070,7 @@ int mithra_gpu_run_prelude(mithra_ctx* ctx) {
     for (int s = 0; s < ns; s++)
       if ((r = stage_push(ctx, s == 0))) return r;
     if (ns == 0 && (r = stage_save_positions(ctx))) return r;
+    if ((r = stage_screen(ctx))) return r;  // before the recycling here (src/solver.cpp:1248)
     if ((r = stage_erase(ctx))) return r;
     if ((r = stage_advance_time(ctx))) return r;
     if ((r = harvest_timers(ctx))) return r;
@@ -1098,10 +1117,12 @@ DiagParticles diag_particles(const mithra_ctx* ctx) {
   if (ctx->precision == MITHRA_PRECISION_FP64) {
     const ParticlesDev<double>& t = ctx->pt;
     P.x = t.x; P.y = t.y; P.z = t.z; P.gx = t.gx; P.gy = t.gy; P.gz = t.gz; P.q = t.q; P.status = t.status;
+    P.mx = t.mx; P.my = t.my; P.mz = t.mz;
   } else {
     const ParticlesF32& t = ctx->f32.pt;
     P.cell = t.cell; P.fx = t.fx; P.fy = t.fy; P.fz = t.fz; P.gxf = t.gx; P.gyf = t.gy; P.gzf = t.gz; P.qf = t.q;
     P.status = t.status;
+    P.mcell = t.mcell; P.mfx = t.mfx; P.mfy = t.mfy; P.mfz = t.mfz; P.id = t.id;
   }
   return P;
 }
@@ -1183,6 +1204,65 @@ int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b) {
   }, s, nullptr);
   if (r) return r;
   *b = (s[0] != 0.0) ? sqrt(s[1] * s[1] + s[2] * s[2]) / s[0] : 0.0;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_set_screens(mithra_ctx* ctx, const double* lz, int n, long long capacity) {
+  if (!ctx || n < 0 || (n > 0 && !lz) || capacity < 0) return MITHRA_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->screen_lz); cudaFree(ctx->screen_rec); cudaFree(ctx->screen_key); cudaFree(ctx->screen_count);
+  ctx->screen_lz = nullptr; ctx->screen_rec = nullptr; ctx->screen_key = nullptr; ctx->screen_count = nullptr;
+  ctx->n_screens = 0;
+  ctx->screen_cap = 0;
+  invalidate_graphs(ctx);  // the step graphs gain or lose the screen kernel
+  if (n == 0) return MITHRA_OK;
+  const long long cap = capacity > 0 ? capacity : std::max(1024LL, (long long)ctx->capacity);
+  CK(cudaMalloc(&ctx->screen_lz, (size_t)n * sizeof(double)));
+  CK(cudaMalloc(&ctx->screen_rec, (size_t)n * cap * 6 * sizeof(double)));
+  CK(cudaMalloc(&ctx->screen_key, (size_t)n * cap * sizeof(long long)));
+  CK(cudaMalloc(&ctx->screen_count, (size_t)n * sizeof(unsigned long long)));
+  CK(cudaMemcpyAsync(ctx->screen_lz, lz, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemsetAsync(ctx->screen_count, 0, (size_t)n * sizeof(unsigned long long), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->n_screens = n;
+  ctx->screen_cap = cap;
+  return MITHRA_OK;
+}
+
+int mithra_gpu_screen_clear(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  if (ctx->n_screens == 0) return MITHRA_OK;
+  CK(cudaMemsetAsync(ctx->screen_count, 0, (size_t)ctx->n_screens * sizeof(unsigned long long), ctx->stream));
+  return MITHRA_OK;
+}
+
+int mithra_gpu_screen_records(mithra_ctx* ctx, int screen, double* out, long long cap_rows, long long* n_rows) {
+  if (!ctx || !n_rows || screen < 0 || screen >= ctx->n_screens || cap_rows < 0) return MITHRA_ERR_ARG;
+  unsigned long long count = 0;
+  CK(cudaMemcpyAsync(&count, ctx->screen_count + screen, sizeof(count), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if ((long long)count > ctx->screen_cap)
+    return fail(ctx, MITHRA_ERR_CAPACITY, "screen %d: %llu records for a capacity of %lld", screen, count,
+                ctx->screen_cap);
+  *n_rows = (long long)count;
+  if (!out || count == 0) return MITHRA_OK;
+  if (cap_rows < (long long)count) return fail(ctx, MITHRA_ERR_ARG, "screen rows buffer too small (%lld < %llu)", cap_rows, count);
+  std::vector<double> rec((size_t)count * 6);
+  std::vector<long long> key((size_t)count);
+  const size_t base = (size_t)screen * (size_t)ctx->screen_cap;
+  CK(cudaMemcpyAsync(rec.data(), ctx->screen_rec + base * 6, rec.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(key.data(), ctx->screen_key + base, key.size() * sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  // the reference's file order: steps in order, particles in list order within a step
+  std::vector<long long> order((size_t)count);
+  for (size_t i = 0; i < order.size(); i++) order[i] = (long long)i;
+  std::sort(order.begin(), order.end(), [&](long long a, long long b) { return key[a] < key[b]; });
+  for (size_t i = 0; i < order.size(); i++) {
+    const double* src = rec.data() + (size_t)order[i] * 6;
+    double* dst = out + i * 7;
+    for (int c = 0; c < 6; c++) dst[c] = src[c];
+    dst[6] = (double)(key[order[i]] >> 40);  // nTime_ of the step
+  }
   return MITHRA_OK;
 }
 

@@ -1002,6 +1002,44 @@ double mo_bunching_factor(double zmin, double Lz, double zp0, double zp1, const 
   return q != 0.0 ? sqrt(cr * cr + ci * ci) / q : 0.0;
 }
 
+/* Solver::interp, src/solver.cpp:2283-2286. */
+static double screen_interp(double x0, double x1, double y0, double y1, double x) {
+  return y0 + (x - x0) / (x1 - x0) * (y1 - y0);
+}
+
+/* Solver::screenProfile, src/solver.cpp:2205-2257: the step runs from timeBunch - dt to timeBunch
+ * with the particle at rnm and rnp; x, y and the lab time are interpolated linearly in the lab z
+ * to the screen, the momentum is the one after the step (stair-case). */
+long mo_screen_profile(const mo_screen* s, const double* lz_screen, int n_screens, double time_bunch,
+                       const double* rec, long n, double* out, long cap) {
+  long w = 0;
+  for (int i = 0; i < n_screens; i++) {
+    const double lzs = lz_screen[i];
+    for (long p = 0; p < n; p++) {
+      const double* c = rec + MO_REC * p;
+      if (!in_processor(s->zmin, s->Lz, s->zp0, s->zp1, c[3])) continue;
+      const double lzm = s->gamma * (c[6] + s->beta * s->c0 * (time_bunch - s->dt + s->dt_shift));
+      if (lzm >= lzs) continue;
+      const double lzp = s->gamma * (c[3] + s->beta * s->c0 * (time_bunch + s->dt_shift));
+      if (lzp < lzs) continue;
+      if (w < cap) {
+        double* o = out + 7 * w;
+        o[0] = screen_interp(lzm, lzp, c[4], c[1], lzs);
+        o[1] = screen_interp(lzm, lzp, c[5], c[2], lzs);
+        const double tm = s->gamma * (time_bunch + s->dt_shift - s->dt + s->beta / s->c0 * c[6]);
+        const double tp = s->gamma * (time_bunch + s->dt_shift + s->beta / s->c0 * c[3]);
+        o[2] = screen_interp(lzm, lzp, tm, tp, lzs);
+        o[3] = c[7];
+        o[4] = c[8];
+        o[5] = s->gamma * (c[9] + s->beta * sqrt(1.0 + (c[7] * c[7] + c[8] * c[8] + c[9] * c[9])));
+        o[6] = (double)p;
+      }
+      w++;
+    }
+  }
+  return w;
+}
+
 void mo_field_sample(const mo_field* f, const double* an, const float* en, const float* bn, const double* pts,
                      long n, double* out) {
   const long N1 = f->N1, N1N0 = (long)f->N1 * f->N0;

@@ -161,6 +161,21 @@ void mo_bunch_sample(double zmin, double Lz, double zp0, double zp1, const doubl
 /* |sum q exp(i k z)| / sum q over the particles of the domain, in particle order. */
 double mo_bunching_factor(double zmin, double Lz, double zp0, double zp1, const double* rec, long n, double k);
 
+/* Lab-frame screen crossing of Solver::screenProfile (src/solver.cpp:2205-2257). */
+typedef struct {
+  double gamma, beta, c0;   /* moving frame */
+  double dt_shift;          /* dt_ */
+  double dt;                /* mesh_.timeStep_ */
+  double zmin, Lz, zp0, zp1;
+} mo_screen;
+
+/* Solver::screenProfile for one domain, after the substeps of a step that ends at time_bunch:
+ * for each screen (lab z, in the given order) and each particle of the list (in order) whose lab
+ * z passes the screen during the step, one row (x, y, t, gbx, gby, gbz_lab, list index) in out.
+ * Returns the number of rows (at most cap are written). */
+long mo_screen_profile(const mo_screen* s, const double* lz_screen, int n_screens, double time_bunch,
+                       const double* rec, long n, double* out, long cap);
+
 /* Thread count used by the parallel loops (1 = serial, bitwise reproduction of the reference). */
 void mo_set_threads(int n);
 int mo_get_threads(void);

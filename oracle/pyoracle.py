@@ -114,6 +114,28 @@ class MoPower(C.Structure):
                 ("ep_im", C.POINTER(C.c_double)), ("fdt", C.POINTER(C.c_double))]
 
 
+class MoScreen(C.Structure):
+    _fields_ = [("gamma", C.c_double), ("beta", C.c_double), ("c0", C.c_double), ("dt_shift", C.c_double),
+                ("dt", C.c_double), ("zmin", C.c_double), ("Lz", C.c_double), ("zp0", C.c_double),
+                ("zp1", C.c_double)]
+
+
+def screen_params(m: dict) -> MoScreen:
+    return MoScreen(m["gamma"], m["beta"], m["c0"], m["dt_shift"], m["dt"], m["zmin"], m["Lz"], m["zp0"], m["zp1"])
+
+
+def screen_profile(m: dict, lz_screens, time_bunch: float, rec) -> np.ndarray:
+    """Solver::screenProfile rows (x, y, t, gbx, gby, gbz_lab, list index) of one step, screens
+    in the given order, particles in list order."""
+    rec = np.ascontiguousarray(rec, dtype=np.float64)
+    lz = np.ascontiguousarray(lz_screens, dtype=np.float64)
+    sp = screen_params(m)
+    n = lib().mo_screen_profile(C.byref(sp), dptr(lz), len(lz), float(time_bunch), dptr(rec), rec.shape[0], None, 0)
+    out = np.zeros((max(n, 1), 7))
+    lib().mo_screen_profile(C.byref(sp), dptr(lz), len(lz), float(time_bunch), dptr(rec), rec.shape[0], dptr(out), n)
+    return out[:n]
+
+
 _lib = None
 
 
@@ -140,6 +162,8 @@ def lib():
         _lib.mo_field_sample.argtypes = [P(MoField), d, f, f, d, l, d]
         _lib.mo_bunching_factor.argtypes = [dd, dd, dd, dd, d, l, dd]
         _lib.mo_bunching_factor.restype = dd
+        _lib.mo_screen_profile.argtypes = [P(MoScreen), d, C.c_int, dd, d, l, d, l]
+        _lib.mo_screen_profile.restype = l
     return _lib
 
 
@@ -316,6 +340,8 @@ class OracleRun:
         self.dtb_time = meta["dtb"]
         self.power = PowerSampler(meta) if int(meta.get("n_fel", 0)) > 0 and "rp0_N" in meta else None
         self.power_rows = []
+        self.screens = None        # lab z of the screens (set_screens)
+        self.screen_rows = []      # per step: rows of screen_profile with the screen index in column 7
 
     @property
     def particles(self):
@@ -353,6 +379,17 @@ class OracleRun:
         lib().mo_deposit_current(C.byref(self.d), dptr(self.rec), self.n, dptr(self.anp1),
                                  dptr(self.fnp1) if self.sc else None)
 
+    def set_screens(self, lz_screens):
+        """Record Solver::screenProfile rows every step (screens in the given order)."""
+        self.screens = np.ascontiguousarray(lz_screens, dtype=np.float64)
+
+    def _screen(self):
+        rows = []
+        for i, lz in enumerate(self.screens):
+            r = screen_profile(self.m, [lz], self.time_bunch, self.particles)
+            rows.append(np.column_stack([r, np.full(len(r), float(i))]))
+        self.screen_rows.append(np.concatenate(rows) if rows else np.zeros((0, 8)))
+
     def step(self):
         """One field step, src/solver.cpp:1300-1399 (diagnostic file writers omitted)."""
         self.field_update()
@@ -365,6 +402,8 @@ class OracleRun:
             self.n_time_bunch += 1
             t += 1.0
         self.erase()
+        if self.screens is not None:
+            self._screen()
         if self.power is not None:
             pg = self.power.sample(self.n_time, self.en, self.bn)
             m = self.m

@@ -14,6 +14,10 @@
  *   run     JOB NSTEPS OUT EVERY    initialise, march NSTEPS field steps, dump every EVERY steps
  *   field   JOB IN OUT              load an/anm1/anp1(=J), FdTd::fieldUpdate, evaluate E/B eagerly
  *   push    JOB IN OUT              load an/anp1/particles/timeBunch, one Solver::bunchUpdate
+ *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile where solve()
+ *                                   calls it; the reference writes its own screen files into the
+ *                                   job's directory, OUT/offsets.bin holds each screen file's size
+ *                                   after the prelude and after every step
  *   deposit JOB IN OUT              load particles, currentReset + currentUpdate (+ currentCommunicate)
  *   power   JOB IN OUT K            K calls of Solver::powerSample on loaded field pairs
  *   bunch   JOB IN OUT              Solver::bunchSample moments of loaded particles
@@ -235,6 +239,17 @@ static void pre_loop(Solver* s) {
   }
 }
 
+/* Byte size of every open screen file (flushed), in FEL and screen order. */
+static void screen_offsets(Solver* s, std::vector<double>& out) {
+  for (size_t jf = 0; jf < s->FEL_.size(); jf++) {
+    if (!s->FEL_[jf].screenProfile_.sampling_) continue;
+    for (size_t i = 0; i < s->scrp_[jf].files.size(); i++) {
+      s->scrp_[jf].files[i]->flush();
+      out.push_back((double)s->scrp_[jf].files[i]->tellp());
+    }
+  }
+}
+
 /* FdTd::fieldEvaluate reads the potentials through the uf_ pointers that fieldUpdate sets
  * (src/fdtd.cpp:240-245); modes that evaluate fields without a field update set them here. */
 static void bind_field_pointers(Solver* s) {
@@ -320,6 +335,51 @@ int main(int argc, char** argv) {
       if (n % every == 0 || n == nsteps) dump_state(s, jp(out, "step" + std::to_string(n)));
     }
     fclose(pw);
+  } else if (mode == "screen") {
+    // The negative-time loop and the field steps with screenProfile at its places in
+    // Solver::solve: after the substeps in the prelude (src/solver.cpp:1248), after
+    // recycleParticles in the main loop (src/solver.cpp:1374).
+    int nsteps = atoi(argv[3]);
+    std::string out = argv[4];
+    mkdir(out.c_str(), 0755);
+    std::vector<double> offs;
+    while (s->time_ < 0.0) {
+      for (auto it = s->chargeVectorn_.begin(); it != s->chargeVectorn_.end(); it++) it->rnm = it->rnp;
+      for (double t = 0.0; t < s->nUpdateBunch_; t += 1.0) {
+        s->bunchUpdate();
+        s->timeBunch_ += s->bunch_.timeStep_;
+        ++s->nTimeBunch_;
+      }
+      s->screenProfile();
+      s->recycleParticles();
+      s->timem1_ += s->mesh_.timeStep_;
+      s->time_ += s->mesh_.timeStep_;
+      s->timep1_ += s->mesh_.timeStep_;
+      ++s->nTime_;
+    }
+    screen_offsets(s, offs);
+    for (int n = 1; n <= nsteps; n++) {
+      s->fieldUpdate();
+      for (auto it = s->chargeVectorn_.begin(); it != s->chargeVectorn_.end(); it++) it->rnm = it->rnp;
+      for (double t = 0.0; t < s->nUpdateBunch_; t += 1.0) {
+        s->bunchUpdate();
+        s->timeBunch_ += s->bunch_.timeStep_;
+        ++s->nTimeBunch_;
+      }
+      s->recycleParticles();
+      s->screenProfile();
+      s->powerSample();
+      s->fieldShift();
+      s->currentReset();
+      s->currentUpdate();
+      s->currentCommunicate();
+      s->timem1_ += s->mesh_.timeStep_;
+      s->time_ += s->mesh_.timeStep_;
+      s->timep1_ += s->mesh_.timeStep_;
+      ++s->nTime_;
+      screen_offsets(s, offs);
+    }
+    write_raw(jp(out, "offsets.bin"), offs.data(), offs.size() * 8);
   } else if (mode == "field") {
     std::string in = argv[3], out = argv[4];
     mkdir(out.c_str(), 0755);

@@ -5,7 +5,7 @@ against the single-rank MPI stand-in) on the small known-answer jobs and stores 
 outputs as compressed .npz files.  Run from the repository root in a checkout that has the
 reference tree:
 
-    python tests/golden/make_golden.py [REF_SRC]
+    python tests/golden/make_golden.py [REF_SRC] [--only=screen]
 
 Seeded random inputs (numpy default_rng) make every fixture reproducible.
 """
@@ -59,6 +59,37 @@ def field_sample_fixture(harness, job, dst, tmp, an, anp1, meta, rng):
     run(harness, "fieldsample", job, fin, os.path.join(tmp, "fs_out"), cwd=tmp)
     np.savez_compressed(os.path.join(dst, "fieldsample.npz"), an=an, anp1=anp1, points=pts,
                         sample=np.fromfile(os.path.join(tmp, "fs_out", "sample.bin")).reshape(-1, 9))
+
+
+def screen_fixture(harness, jobname, tag, nsteps=12):
+    """Solver::screenProfile through the prelude and nsteps field steps: the screen files the
+    reference writes (text as written) and each file's size after the prelude and every step."""
+    job = os.path.join(JOBS, jobname)
+    dst = os.path.join(OUT, tag)
+    os.makedirs(dst, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        run(harness, "screen", job, nsteps, os.path.join(tmp, "screen_out"), cwd=tmp)
+        offsets = np.fromfile(os.path.join(tmp, "screen_out", "offsets.bin"))
+        files = sorted(f for f in os.listdir(os.path.join(tmp, "screen")) if f.endswith(".txt"))
+        offsets = offsets.reshape(nsteps + 1, len(files))
+        texts = [open(os.path.join(tmp, "screen", f), "rb").read() for f in files]
+        rows, screen, step = [], [], []
+        for i, t in enumerate(texts):
+            start = 0
+            for n in range(nsteps + 1):
+                end = int(offsets[n, i])
+                for line in t[start:end].decode().splitlines():
+                    rows.append([float(x) for x in line.split()])
+                    screen.append(i)
+                    step.append(n)
+                start = end
+        np.savez_compressed(os.path.join(dst, "screen.npz"), names=np.array(files), offsets=offsets,
+                            text=np.frombuffer(b"".join(texts), dtype=np.uint8),
+                            text_sizes=np.array([len(t) for t in texts]),
+                            rows=np.array(rows).reshape(-1, 6), screen=np.array(screen), step=np.array(step))
+    finally:
+        shutil.rmtree(tmp)
 
 
 def fixtures_for(harness, jobname, tag, with_kats=True):
@@ -140,17 +171,26 @@ def fixtures_for(harness, jobname, tag, with_kats=True):
 
 
 def main():
-    ref_src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src"
+    args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
+    only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
+    ref_src = args[0] if args else "/root/reference/src"
     harness = pyoracle.build_reference(ref_src)
     if harness is None:
         sys.exit("reference sources not found at %s" % ref_src)
     harness = os.path.abspath(harness)
+    if only == ["screen"]:  # the lab-frame screen fixtures alone
+        fixtures_for(harness, "kat-small-screen.job", "kat-small-screen", with_kats=False)
+        screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
+        print("golden vectors written to", OUT)
+        return
     fixtures_for(harness, "kat-small.job", "kat-small-fd")
     fixtures_for(harness, "kat-small-nsfd.job", "kat-small-nsfd")
     fixtures_for(harness, "kat-small-sc.job", "kat-small-sc", with_kats=False)
     fixtures_for(harness, "kat-small-seed.job", "kat-small-seed", with_kats=False)
     fixtures_for(harness, "kat-small-ext.job", "kat-small-ext", with_kats=False)
     fixtures_for(harness, "kat-small-optical.job", "kat-small-optical", with_kats=False)
+    fixtures_for(harness, "kat-small-screen.job", "kat-small-screen", with_kats=False)
+    screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
     print("golden vectors written to", OUT)
 
 

@@ -66,3 +66,26 @@ def test_seed_fill_matches_reference():
     anp1, an, anm1 = mg.Setup.from_job(job("kat-small-seed.job")).fields()
     assert np.abs(z["an"]).max() > 0
     assert np.array_equal(an, z["an"]) and np.array_equal(anm1, z["anm1"])
+
+
+def test_screen_positions_parsed_and_sorted(tmp_path):
+    """bunch-profile-lab-frame (src/datainput.cpp:726-745) and initializeScreenProfile
+    (src/solver.cpp:2145-2199): positions sorted, a rhythm adds 0, r, 2r, ... to the undulator end,
+    unknown keys and screens without positions are errors with the reference's messages."""
+    s = mg.Setup.from_job(job("kat-small-screen.job"))
+    assert list(s.screens()) == [-65000.0, -50000.0, -35000.0]
+    text = open(job("kat-small-screen.job")).read()
+    m = s.meta()
+    end = m["und0_rb"] + m["und0_length"] * m["und0_lu"]
+    rhythm = text.replace("    position                = -50000.0\n", "    rhythm                  = 400000.0\n")
+    p = tmp_path / "r.job"
+    p.write_text(rhythm)
+    z = list(mg.Setup.from_job(str(p)).screens())
+    assert z == sorted([-65000.0, -35000.0] + list(np.arange(0.0, end, 400000.0)))
+    p.write_text(text.replace("    position                = -50000.0\n", "    no-such-key             = 1\n"))
+    with pytest.raises(mg.MithraError, match="not defined in the bunch-profile-lab-frame group"):
+        mg.Setup.from_job(str(p))
+    nopos = "\n".join(l for l in text.splitlines() if "position                = -" not in l)
+    p.write_text(nopos)
+    with pytest.raises(mg.MithraError, match="No position is set for the screen"):
+        mg.Setup.from_job(str(p))

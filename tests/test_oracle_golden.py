@@ -159,3 +159,52 @@ def test_oracle_field_sample_matches_reference(tag):
     po.lib().mo_eval_eb(po.C.byref(fp), po.dptr(fs["anp1"].copy()), po.dptr(fs["an"].copy()), None, po.fptr(en),
                         po.fptr(bn))
     assert np.array_equal(po.field_sample(m, fs["an"], en, bn, fs["points"], TAGS[tag][1]), fs["sample"])
+
+
+def _screen_golden():
+    z = load("kat-small-screen", "screen")
+    texts, start = [], 0
+    for size in z["text_sizes"]:
+        texts.append(bytes(z["text"][start:start + size]).decode())
+        start += size
+    return z, texts
+
+
+def test_oracle_screen_profile_matches_reference():
+    """Solver::screenProfile rows of the 12 field steps against the reference's own screen files
+    (16 significant digits in the files)."""
+    m = meta("kat-small-screen")
+    init = load("kat-small-screen", "init")
+    z, _ = _screen_golden()
+    lz = np.sort([-35000.0, -65000.0, -50000.0])
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    r.set_screens(lz)
+    for _ in range(12):
+        r.step()
+    for step in range(1, 13):
+        got = r.screen_rows[step - 1]
+        for i in range(3):
+            g = got[got[:, 7] == i][:, :6]
+            ref = z["rows"][(z["step"] == step) & (z["screen"] == i)]
+            assert g.shape == ref.shape, (step, i)
+            assert np.all(np.abs(g - ref) <= 1e-15 * np.abs(ref) + 1e-300)
+    assert sum(len(x) for x in r.screen_rows) == int(np.sum(z["step"] > 0))
+
+
+def test_screen_file_format_matches_reference():
+    """The writer of mithra_gb300 reproduces the reference's screen files byte for byte from the
+    oracle's rows (screens without prelude crossings: the whole file; the first screen: the part
+    written by the field steps)."""
+    import mithra_gb300 as mg
+    m = meta("kat-small-screen")
+    init = load("kat-small-screen", "init")
+    z, texts = _screen_golden()
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    r.set_screens(np.sort([-35000.0, -65000.0, -50000.0]))
+    for _ in range(12):
+        r.step()
+    rows = np.concatenate(r.screen_rows)
+    for i in range(3):
+        mine = rows[rows[:, 7] == i][:, :6]
+        prelude = int(z["offsets"][0, i])
+        assert mg.format_screen_text(mine, first_in_file=prelude == 0) == texts[i][prelude:]
