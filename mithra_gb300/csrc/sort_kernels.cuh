@@ -195,7 +195,7 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
 
 constexpr int kDepositBlock = 128;
 
-__global__ void __launch_bounds__(kDepositBlock, 8) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
+__global__ void __launch_bounds__(kDepositBlock, 7) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
                                                        StateDev* st, float* J, float* rho, long long cs,
                                                        long long plane, int P1) {
   extern __shared__ float sJ[];  // 3 * TILE_NODES
@@ -213,57 +213,78 @@ __global__ void __launch_bounds__(kDepositBlock, 8) k_deposit_tiled(DepositF32 D
   }
   int kmin = 0x7fffffff, kmax = -0x7fffffff;
   const long long sI = P1, sK = plane;
-  for (int p = beg + threadIdx.x; p < end; p += blockDim.x) {
+  // The particle data of the next iteration is loaded before the current particle's atomics, so
+  // each thread keeps two particles' loads in flight (the loop is bound by global-load latency).
+  struct Loaded {
+    long long cell, mcell;
+    float fx, fy, fz, mfx, mfy, mfz, q;
+  };
+  auto load = [&](int p) {
+    Loaded L;
+    L.cell = pt.cell[p]; L.mcell = pt.mcell[p];
+    L.fx = pt.fx[p]; L.fy = pt.fy[p]; L.fz = pt.fz[p];
+    L.mfx = pt.mfx[p]; L.mfy = pt.mfy[p]; L.mfz = pt.mfz[p];
+    L.q = pt.q[p];
+    return L;
+  };
+  int p = beg + threadIdx.x;
+  Loaded cur{};
+  if (p < end) cur = load(p);
+  for (; p < end; p += kDepositBlock) {
+    Loaded nxt{};
+    if (p + kDepositBlock < end) nxt = load(p + kDepositBlock);
     int ip, jp, kp, im, jm, km;
-    unpack_cell(pt.cell[p], ip, jp, kp);
-    unpack_cell(pt.mcell[p], im, jm, km);
+    unpack_cell(cur.cell, ip, jp, kp);
+    unpack_cell(cur.mcell, im, jm, km);
     kmin = min(kmin, kp);
     kmax = max(kmax, kp);
-    const float fxp = pt.fx[p], fyp = pt.fy[p], fzp = pt.fz[p];
-    const float fxm = pt.mfx[p], fym = pt.mfy[p], fzm = pt.mfz[p];
+    const float fxp = cur.fx, fyp = cur.fy, fzp = cur.fz;
+    const float fxm = cur.mfx, fym = cur.mfy, fzm = cur.mfz;
     const bool bp = inside_f32(D, ip, jp, kp, fxp, fyp);
     const bool bm = inside_f32(D, im, jm, km, fxm, fym);
-    if (!(bp || bm)) continue;
-    int bx, by, bz;
-    float rxm, rxp, rym, ryp, rzm, rzp;
-    const float rx = relay_axis(im, ip, fxm, fxp, &bx, &rxm, &rxp);
-    const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
-    const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
-    const float qh = 0.5f * pt.q[p];
-    float* sj = tiled ? sJ : nullptr;
-    if (bp) {
-      const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
-                  az = 0.5f * (rzp + rz) - (float)(kp - bz);
-      if (sj)
-        tile_half(sj, J, cs, plane, P1, i0, j0, k0, ip, jp, kp, qh, ax, ay, az, (rxp - rx) * D.dx, (ryp - ry) * D.dy,
-                  (rzp - rz) * D.dz);
-      else
-        deposit_half_f32(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, ax, ay, az,
-                         (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
-      if (rho) {
-        const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
-        const float q = pt.q[p];
-        const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
-        atomicAdd(rho + m, q * x1 * y1 * z1);
-        atomicAdd(rho + m + sI, q * fxp * y1 * z1);
-        atomicAdd(rho + m + 1, q * x1 * fyp * z1);
-        atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
-        atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
-        atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
-        atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
-        atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
+    if (bp || bm) {
+      int bx, by, bz;
+      float rxm, rxp, rym, ryp, rzm, rzp;
+      const float rx = relay_axis(im, ip, fxm, fxp, &bx, &rxm, &rxp);
+      const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
+      const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
+      const float qh = 0.5f * cur.q;
+      float* sj = tiled ? sJ : nullptr;
+      if (bp) {
+        const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
+                    az = 0.5f * (rzp + rz) - (float)(kp - bz);
+        if (sj)
+          tile_half(sj, J, cs, plane, P1, i0, j0, k0, ip, jp, kp, qh, ax, ay, az, (rxp - rx) * D.dx,
+                    (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+        else
+          deposit_half_f32(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, ax, ay, az,
+                           (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+        if (rho) {
+          const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
+          const float q = cur.q;
+          const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
+          atomicAdd(rho + m, q * x1 * y1 * z1);
+          atomicAdd(rho + m + sI, q * fxp * y1 * z1);
+          atomicAdd(rho + m + 1, q * x1 * fyp * z1);
+          atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
+          atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
+          atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
+          atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
+          atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
+        }
+      }
+      if (bm) {
+        const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
+                    az = 0.5f * (rzm + rz) - (float)(km - bz);
+        if (sj)
+          tile_half(sj, J, cs, plane, P1, i0, j0, k0, im, jm, km, qh, ax, ay, az, (rx - rxm) * D.dx,
+                    (ry - rym) * D.dy, (rz - rzm) * D.dz);
+        else
+          deposit_half_f32(J, cs, (long long)km * plane + (long long)im * P1 + jm, sI, sK, qh, ax, ay, az,
+                           (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
       }
     }
-    if (bm) {
-      const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
-                  az = 0.5f * (rzm + rz) - (float)(km - bz);
-      if (sj)
-        tile_half(sj, J, cs, plane, P1, i0, j0, k0, im, jm, km, qh, ax, ay, az, (rx - rxm) * D.dx, (ry - rym) * D.dy,
-                  (rz - rzm) * D.dz);
-      else
-        deposit_half_f32(J, cs, (long long)km * plane + (long long)im * P1 + jm, sI, sK, qh, ax, ay, az,
-                         (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
-    }
+    cur = nxt;
   }
   for (int o = 16; o > 0; o >>= 1) {
     kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
