@@ -197,6 +197,9 @@ int mithra_gpu_bunching_factor(mithra_ctx* ctx, double k, double* b);
  * mithra_gpu_screen_records as MITHRA_ERR_CAPACITY.  n = 0 removes the screens.  Replaces the
  * files the reference opens per screen: their rows come from mithra_gpu_screen_records. */
 int mithra_gpu_set_screens(mithra_ctx* ctx, const double* lz, int n, long long capacity);
+/* Solver::screenProfile for the current step alone (the stage-wise form of what every step of
+ * mithra_gpu_run does when screens are set). */
+int mithra_gpu_screen_profile(mithra_ctx* ctx);
 /* Drops the records collected so far (the screens stay). */
 int mithra_gpu_screen_clear(mithra_ctx* ctx);
 /* Records of screen `screen` in the reference's file order (steps in order, particles in list
@@ -298,6 +301,32 @@ int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double*
 int mithra_setup_total_time(const mithra_setup* s, double* total_time);
 /* Writes `key value` lines (the derived scalars of the initialisation) into buf. */
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed);
+/* Base name (directory prefixed, as Solver::initializeSeedVTK, src/solver.cpp:961-964) of the
+ * i-th field-visualization output; the other parameters of the outputs are in the meta text
+ * (vtk<i>_type, _plane, _rhythm (bunch frame), _pos0..2 (bunch frame), _nfield, _f<l>). */
+int mithra_setup_vtk_basename(const mithra_setup* s, int i, char* buf, size_t len, size_t* needed);
+
+/* ---- field visualization files ----------------------------------------------------------- */
+
+#define MITHRA_VTK_MAX_FIELDS 16
+typedef struct {
+  int N0, N1, N2;   /* nodes of the mesh */
+  int np, k0;       /* planes of this domain and its first plane (one domain: N2, 0) */
+  double xmin, ymin, zmin, dx, dy, dz;  /* bunch frame */
+  int type;         /* 0 all-domain, 1 in-plane */
+  int plane;        /* in-plane: 0 yz (x normal), 1 xz (y normal), 2 xy (z normal) */
+  double position[3];                   /* plane position, bunch frame */
+  int nfield;
+  int field[MITHRA_VTK_MAX_FIELDS];     /* 0..9 = Ex Ey Ez Bx By Bz Ax Ay Az F */
+} mithra_vtk_desc;
+
+/* FdTd::fieldVisualizeAllDomain / fieldVisualizeInPlane (src/fdtd.cpp:956-1540; FdTdSC with F,
+ * src/fdtdSC.cpp:1263-1920): writes <basename>-p0-<n_time>.vts and, except for the z-normal
+ * plane, <basename>-<n_time>.pvts in the reference's text layout, from host copies of E and B
+ * (float, 3 per node), A^n (double, 3 per node) and phi^n (NULL without space charge).  The
+ * caller evaluates E/B on every node first (mithra_gpu_field_evaluate + mithra_gpu_download_eb). */
+int mithra_vtk_write_field(const mithra_vtk_desc* d, const char* basename, long long n_time, const float* en,
+                           const float* bn, const double* an, const double* fn);
 /* Creates a context from a setup and uploads its state; the power outputs are configured. */
 int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int device,
                                  double capacity_factor, mithra_ctx** out);

@@ -80,6 +80,13 @@ class PowerDesc(C.Structure):
                 ("twiddle_im", C.POINTER(C.c_double))]
 
 
+class VtkDesc(C.Structure):
+    _fields_ = [("N0", C.c_int), ("N1", C.c_int), ("N2", C.c_int), ("np", C.c_int), ("k0", C.c_int),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double), ("dx", C.c_double),
+                ("dy", C.c_double), ("dz", C.c_double), ("type", C.c_int), ("plane", C.c_int),
+                ("position", C.c_double * 3), ("nfield", C.c_int), ("field", C.c_int * 16)]
+
+
 class TimeState(C.Structure):
     _fields_ = [("time", C.c_double), ("time_bunch", C.c_double), ("n_time", C.c_int64),
                 ("n_time_bunch", C.c_int64)]
@@ -152,6 +159,9 @@ _SIGS = {
     "mithra_setup_fields": [_vp, _dp, _dp, _dp],
     "mithra_setup_total_time": [_vp, _dp],
     "mithra_setup_meta": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_vtk_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
+    "mithra_gpu_screen_profile": [_vp],
     "mithra_gpu_create_from_setup": [_vp, C.c_int, C.c_int, C.c_double, _P(_vp)],
 }
 
@@ -281,6 +291,15 @@ class Setup:
         lib().mithra_setup_fields(self._h, dptr(anp1), dptr(an), dptr(anm1))
         return anp1, an, anm1
 
+    def vtk_basename(self, i: int) -> str:
+        """Base name of field-visualization output i (directory prefixed)."""
+        need = C.c_size_t()
+        if lib().mithra_setup_vtk_basename(self._h, int(i), None, 0, C.byref(need)) != 0:
+            raise MithraError("no field-visualization output %d" % i)
+        buf = C.create_string_buffer(need.value)
+        lib().mithra_setup_vtk_basename(self._h, int(i), buf, need.value, C.byref(need))
+        return buf.value.decode()
+
     def screens(self) -> np.ndarray:
         """Lab z of the job's screens (bunch-profile-lab-frame groups), in the reference's
         order: FEL-OUTPUT entries in order, each entry's positions sorted."""
@@ -297,6 +316,46 @@ class Setup:
             k, v = line.split()
             out[k] = float(v)
         return out
+
+
+def vtk_desc(meta: dict, i: int) -> VtkDesc:
+    """The i-th field-visualization output of a job (meta of Setup.meta) as the writer's
+    descriptor: one domain, bunch-frame geometry, field codes Ex..Az = 0..8, F = 9."""
+    p = "vtk%d_" % i
+    d = VtkDesc()
+    d.N0, d.N1, d.N2 = int(meta["N0"]), int(meta["N1"]), int(meta["N2"])
+    d.np, d.k0 = int(meta["np"]), int(meta["k0"])
+    d.xmin, d.ymin, d.zmin = meta["xmin"], meta["ymin"], meta["zmin"]
+    d.dx, d.dy, d.dz = meta["dx"], meta["dy"], meta["dz"]
+    d.type, d.plane = int(meta[p + "type"]), int(meta[p + "plane"])
+    for q in range(3):
+        d.position[q] = meta[p + "pos%d" % q]
+    d.nfield = int(meta[p + "nfield"])
+    for l in range(d.nfield):
+        d.field[l] = int(meta[p + "f%d" % l])
+    return d
+
+
+def vtk_due(meta: dict, i: int, time: float) -> bool:
+    """Solver::solve's condition for writing output i at field time `time` (src/solver.cpp:1328-1340)."""
+    p = "vtk%d_" % i
+    return bool(meta[p + "sample"]) and float(np.fmod(time, meta[p + "rhythm"])) < meta["dt"] and time > 0.0
+
+
+def write_field_vtk(meta: dict, i: int, basename: str, n_time: int, en, bn, an, fn=None):
+    """Writes output i (FdTd::fieldVisualize*, the reference's file layout) from host arrays: E, B
+    float32 and A^n float64 with 3 values per node, phi^n float64 or None."""
+    d = os.path.dirname(basename)
+    if d:
+        os.makedirs(d, exist_ok=True)
+    en = np.ascontiguousarray(en, dtype=np.float32)
+    bn = np.ascontiguousarray(bn, dtype=np.float32)
+    an = np.ascontiguousarray(an, dtype=np.float64)
+    fn = None if fn is None else np.ascontiguousarray(fn, dtype=np.float64)
+    r = lib().mithra_vtk_write_field(C.byref(vtk_desc(meta, i)), basename.encode(), int(n_time), fptr(en), fptr(bn),
+                                     dptr(an), dptr(fn))
+    if r != 0:
+        raise MithraError("mithra_vtk_write_field failed with status %d (output %d)" % (r, i))
 
 
 def format_screen_text(rows, first_in_file: bool = True) -> str:
@@ -673,12 +732,54 @@ class FdTd:
         return n
 
     def solve(self, max_steps: int | None = None):
+        """Solver::solve: the prelude, then field steps to the total time.  Steps at which a
+        field-visualization output is due (src/solver.cpp:1328-1340) run stage by stage and
+        write their files where the reference does (after the recycling); all others replay the
+        captured step graph."""
         self.ctx.run_prelude()
         n = self.steps_to_total_time()
         if max_steps is not None:
             n = min(n, max_steps)
-        self.ctx.run(n)
+        m = self.meta
+        nv = int(m.get("n_vtk", 0))
+        due = []
+        if nv:
+            t, dt = self.ctx.get_time().time, m["dt"]
+            for s in range(n):
+                outs = [i for i in range(nv) if vtk_due(m, i, t)]
+                if outs:
+                    due.append((s, outs))
+                t += dt
+        done = 0
+        for s, outs in due:
+            self.ctx.run(s - done)
+            self._step_with_vtk(outs)
+            done = s + 1
+        self.ctx.run(n - done)
         return self.ctx.power_rows()
+
+    def _step_with_vtk(self, outs):
+        c = self.ctx
+        n_time = c.get_time().n_time
+        c.field_update()
+        c.save_positions()
+        t = 0.0
+        while t < self.meta["nUpdateBunch"]:
+            c.bunch_update()
+            t += 1.0
+        c.recycle()
+        c.field_evaluate()
+        en, bn = c.download_eb()
+        _, an, _ = c.download_fields()
+        fn = c.download_scalar()[1] if isinstance(self, FdTdSC) else None
+        for i in outs:
+            write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
+        if getattr(c, "n_screens", 0):
+            c.call("mithra_gpu_screen_profile")
+        c.power_sample()
+        c.field_shift()
+        c.current_update()
+        c.advance_time()
 
 
 class FdTdSC(FdTd):

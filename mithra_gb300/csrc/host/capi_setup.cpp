@@ -160,6 +160,16 @@ int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double*
   return MITHRA_OK;
 }
 
+int mithra_setup_vtk_basename(const mithra_setup* s, int i, char* buf, size_t len, size_t* needed) {
+  if (!s || i < 0 || i >= (int)s->s.job.seed.vtk.size()) return MITHRA_ERR_ARG;
+  const std::string& b = s->s.job.seed.vtk[(size_t)i].basename;
+  if (needed) *needed = b.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < b.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, b.c_str(), b.size() + 1);
+  return MITHRA_OK;
+}
+
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
   if (!s) return MITHRA_ERR_ARG;
   const std::string m = s->s.meta();

@@ -347,7 +347,44 @@ void read_field(Cursor& c, Job& J) {
       } while (c.cur() != "}");
       Signal s = k.signal();
       init_beam(J.seed, k.type, k.position, k.direction, k.polarization, k.a0, k.radius, k.order, s, false);
-    } else if (g == "field-sampling" || g == "field-visualization" || g == "field-profile") {
+    } else if (g == "field-visualization") {
+      // src/datainput.cpp:370-398 with Seed::vtkType / planeType / fieldType (src/classes.cpp:879-909)
+      c.open("field-visualization");
+      FieldVtk v;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        if (n == "sample") v.sample = bool_of(l);
+        else if (n == "directory") v.directory = string_of(l);
+        else if (n == "type") {
+          const std::string t = string_of(l);
+          if (t == "in-plane") v.type = VTK_INPLANE;
+          else if (t == "all-domain") v.type = VTK_ALLDOMAIN;
+          else die(t + " is an unknown vtk type.");
+        } else if (n == "plane") {
+          const std::string t = string_of(l);
+          if (t == "yz") v.plane = VTK_XNORMAL;
+          else if (t == "xz") v.plane = VTK_YNORMAL;
+          else if (t == "xy") v.plane = VTK_ZNORMAL;
+          else die(t + " is an unknown vtk plane type.");
+        } else if (n == "base-name") v.basename = string_of(l);
+        else if (n == "field") {
+          static const char* names[] = {"Ex", "Ey", "Ez", "Bx", "By", "Bz", "Ax", "Ay", "Az", "F"};
+          const std::string t = string_of(l);
+          int code = -1;
+          for (int q = 0; q < 10; q++)
+            if (t == names[q]) code = q;
+          if (code < 0) die(t + " is an unknown sampling field.");
+          v.field.push_back(code);
+        } else if (n == "rhythm") v.rhythm = double_of(l);
+        else if (n == "position") {
+          const std::vector<double> p = vector_of(l);
+          for (size_t q = 0; q < 3 && q < p.size(); q++) v.position[q] = p[q];
+        } else die(n + " is not defined in seed-visualization group.");
+        c.next();
+      } while (c.cur() != "}");
+      J.seed.vtk.push_back(v);
+    } else if (g == "field-sampling" || g == "field-profile") {
       // Diagnostics outside the time-marching path: accepted and validated, not produced.
       const std::string grp = g;
       c.open(grp.c_str());

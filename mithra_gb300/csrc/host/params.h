@@ -81,9 +81,24 @@ struct Beam {
   std::vector<double> zR = {0.0, 0.0};
 };
 
+// Seed::vtk (src/classes.h:216-229, defaults src/classes.cpp:858-868): one field-visualization
+// output.  field codes: 0..9 = Ex Ey Ez Bx By Bz Ax Ay Az F (Seed::fieldType, src/classes.cpp:896-909).
+enum VtkType { VTK_ALLDOMAIN = 0, VTK_INPLANE = 1 };
+enum VtkPlane { VTK_XNORMAL = 0, VTK_YNORMAL = 1, VTK_ZNORMAL = 2 };
+struct FieldVtk {
+  bool sample = false;
+  std::vector<int> field;
+  std::string directory, basename;
+  VtkType type = VTK_ALLDOMAIN;
+  VtkPlane plane = VTK_ZNORMAL;
+  double rhythm = 0.0;
+  Vec3 position{0, 0, 0};
+};
+
 struct Seed : Beam {  // src/classes.h Seed
   double beta = 0.0, gamma = 1.0, dt = 0.0;
   bool sampling = false, profile = false;
+  std::vector<FieldVtk> vtk;
   // Seed::fields (src/classes.cpp:740-855): the vector potential of the seed at a bunch-frame
   // point and time.  `a` is accumulated into for super-Gaussian beams, as in the reference.
   void fields(const Vec3& r, double time, Vec3& a) const;

@@ -597,6 +597,30 @@ void Setup::initialize() {
   ub_r1 = -EC / (EM * c0) * bunch.timeStep / 2.0;
   ub_r2 = -EC / EM * bunch.timeStep / 2.0;
 
+  // Solver::initializeSeedVTK, src/solver.cpp:938-1016: the rhythm and the plane position go to
+  // the bunch frame, the directory is prefixed to a relative base name, and an in-plane output
+  // whose plane lies outside the mesh is dropped.  The reference drops it from the vector it is
+  // iterating over and then advances the index, so the output after a dropped one is skipped
+  // (left unboosted); that is reproduced.  Its range check reads ub_.dx, ub_.dy, ub_.dz before
+  // initializeBunchUpdate sets them; the mesh resolution is used here.
+  for (size_t i = 0; i < job.seed.vtk.size(); i++) {
+    FieldVtk& v = job.seed.vtk[i];
+    if (!v.sample) continue;
+    if (v.rhythm == 0) die("The visualization rhythm of the field is zero although visualization is activated !!!");
+    v.rhythm /= gamma;
+    v.position[2] *= gamma;
+    if (v.basename.empty() || v.basename[0] != '/') v.basename = v.directory + v.basename;
+    if (v.type != VTK_INPLANE) continue;
+    bool outside = false;
+    if (v.plane == VTK_XNORMAL)
+      outside = v.position[0] > xmax - mesh.meshResolution[0] || v.position[0] < xmin + mesh.meshResolution[0];
+    else if (v.plane == VTK_YNORMAL)
+      outside = v.position[1] > ymax - mesh.meshResolution[1] || v.position[1] < ymin + mesh.meshResolution[1];
+    else
+      outside = v.position[2] > zmax - mesh.meshResolution[2] || v.position[2] < zmin + mesh.meshResolution[2];
+    if (outside) job.seed.vtk.erase(job.seed.vtk.begin() + (long)i);
+  }
+
   // Solver::initializePowerSample, src/radiation.cpp:18-121.
   for (size_t jf = 0; jf < job.fel.size(); jf++) {
     RadiationPower& rp = job.fel[jf].radiationPower;
@@ -778,6 +802,18 @@ std::string Setup::meta() const {
     kv(p + "N", pc.N); kv(p + "Nl", pc.Nl); kv(p + "Nf", pc.Nf); kv(p + "pc", pc.pc);
     for (int i = 0; i < pc.Nl; i++) kv(p + "w" + std::to_string(i), pc.w[i]);
     for (int i = 0; i < pc.N; i++) kv(p + "z" + std::to_string(i), pc.z[i]);
+  }
+  kv("n_vtk", (double)job.seed.vtk.size());
+  for (size_t i = 0; i < job.seed.vtk.size(); i++) {
+    const FieldVtk& v = job.seed.vtk[i];
+    const std::string p = "vtk" + std::to_string(i) + "_";
+    kv(p + "sample", v.sample ? 1.0 : 0.0);
+    kv(p + "type", (double)v.type);
+    kv(p + "plane", (double)v.plane);
+    kv(p + "rhythm", v.rhythm);
+    for (int d = 0; d < 3; d++) kv(p + "pos" + std::to_string(d), v.position[d]);
+    kv(p + "nfield", (double)v.field.size());
+    for (size_t l = 0; l < v.field.size(); l++) kv(p + "f" + std::to_string(l), (double)v.field[l]);
   }
   for (size_t i = 0; i < screen_z.size(); i++) {
     const std::string p = "scr" + std::to_string(i) + "_";

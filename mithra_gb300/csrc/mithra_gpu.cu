@@ -949,6 +949,11 @@ int mithra_gpu_recycle(mithra_ctx* ctx) {
   return stage_erase(ctx);
 }
 
+int mithra_gpu_screen_profile(mithra_ctx* ctx) {
+  if (!ctx) return MITHRA_ERR_ARG;
+  return stage_screen(ctx);
+}
+
 int mithra_gpu_power_sample(mithra_ctx* ctx) {
   if (!ctx) return MITHRA_ERR_ARG;
   int r = ensure_rows(ctx, 1);

@@ -342,6 +342,7 @@ class OracleRun:
         self.power_rows = []
         self.screens = None        # lab z of the screens (set_screens)
         self.screen_rows = []      # per step: rows of screen_profile with the screen index in column 7
+        self.after_recycle = None  # called as f(run) where Solver::solve writes its field diagnostics
 
     @property
     def particles(self):
@@ -402,6 +403,8 @@ class OracleRun:
             self.n_time_bunch += 1
             t += 1.0
         self.erase()
+        if self.after_recycle is not None:
+            self.after_recycle(self)
         if self.screens is not None:
             self._screen()
         if self.power is not None:

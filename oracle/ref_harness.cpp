@@ -14,6 +14,9 @@
  *   run     JOB NSTEPS OUT EVERY    initialise, march NSTEPS field steps, dump every EVERY steps
  *   field   JOB IN OUT              load an/anm1/anp1(=J), FdTd::fieldUpdate, evaluate E/B eagerly
  *   push    JOB IN OUT              load an/anp1/particles/timeBunch, one Solver::bunchUpdate
+ *   vtk     JOB N OUT               prelude and N steps with the field visualization where solve()
+ *                                   calls it (the reference writes its .vts/.pvts files into the
+ *                                   job's directory); OUT/steps.bin lists the nTime_ of each step
  *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile where solve()
  *                                   calls it; the reference writes its own screen files into the
  *                                   job's directory, OUT/offsets.bin holds each screen file's size
@@ -335,6 +338,40 @@ int main(int argc, char** argv) {
       if (n % every == 0 || n == nsteps) dump_state(s, jp(out, "step" + std::to_string(n)));
     }
     fclose(pw);
+  } else if (mode == "vtk") {
+    // Solver::solve's field visualization (src/solver.cpp:1328-1340) after recycleParticles.
+    int nsteps = atoi(argv[3]);
+    std::string out = argv[4];
+    mkdir(out.c_str(), 0755);
+    pre_loop(s);
+    std::vector<double> steps;
+    for (int n = 1; n <= nsteps; n++) {
+      steps.push_back((double)s->nTime_);
+      s->fieldUpdate();
+      for (auto it = s->chargeVectorn_.begin(); it != s->chargeVectorn_.end(); it++) it->rnm = it->rnp;
+      for (double t = 0.0; t < s->nUpdateBunch_; t += 1.0) {
+        s->bunchUpdate();
+        s->timeBunch_ += s->bunch_.timeStep_;
+        ++s->nTimeBunch_;
+      }
+      s->recycleParticles();
+      for (unsigned int i = 0; i < s->seed_.vtk_.size(); i++) {
+        if (s->seed_.vtk_[i].sample_ && fmod(s->time_, s->seed_.vtk_[i].rhythm_) < s->mesh_.timeStep_ && s->time_ > 0.0) {
+          if (s->seed_.vtk_[i].type_ == ALLDOMAIN) s->fieldVisualizeAllDomain(i);
+          else if (s->seed_.vtk_[i].type_ == INPLANE) s->fieldVisualizeInPlane(i);
+        }
+      }
+      s->powerSample();
+      s->fieldShift();
+      s->currentReset();
+      s->currentUpdate();
+      s->currentCommunicate();
+      s->timem1_ += s->mesh_.timeStep_;
+      s->time_ += s->mesh_.timeStep_;
+      s->timep1_ += s->mesh_.timeStep_;
+      ++s->nTime_;
+    }
+    write_raw(jp(out, "steps.bin"), steps.data(), steps.size() * 8);
   } else if (mode == "screen") {
     // The negative-time loop and the field steps with screenProfile at its places in
     // Solver::solve: after the substeps in the prelude (src/solver.cpp:1248), after

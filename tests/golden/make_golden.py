@@ -5,7 +5,7 @@ against the single-rank MPI stand-in) on the small known-answer jobs and stores 
 outputs as compressed .npz files.  Run from the repository root in a checkout that has the
 reference tree:
 
-    python tests/golden/make_golden.py [REF_SRC] [--only=screen]
+    python tests/golden/make_golden.py [REF_SRC] [--only=screen|--only=vtk]
 
 Seeded random inputs (numpy default_rng) make every fixture reproducible.
 """
@@ -88,6 +88,25 @@ def screen_fixture(harness, jobname, tag, nsteps=12):
                             text=np.frombuffer(b"".join(texts), dtype=np.uint8),
                             text_sizes=np.array([len(t) for t in texts]),
                             rows=np.array(rows).reshape(-1, 6), screen=np.array(screen), step=np.array(step))
+    finally:
+        shutil.rmtree(tmp)
+
+
+def vtk_fixture(harness, jobname, tag, nsteps=12):
+    """FdTd::fieldVisualize* through nsteps field steps: every .vts/.pvts file the reference
+    writes (text as written) and the nTime_ of each step."""
+    job = os.path.join(JOBS, jobname)
+    dst = os.path.join(OUT, tag)
+    os.makedirs(dst, exist_ok=True)
+    tmp = tempfile.mkdtemp()
+    try:
+        run(harness, "vtk", job, nsteps, os.path.join(tmp, "vtk_out"), cwd=tmp)
+        files = sorted(os.listdir(os.path.join(tmp, "vtk")))
+        texts = [open(os.path.join(tmp, "vtk", f), "rb").read() for f in files]
+        np.savez_compressed(os.path.join(dst, "vtk.npz"), names=np.array(files),
+                            text=np.frombuffer(b"".join(texts), dtype=np.uint8),
+                            text_sizes=np.array([len(t) for t in texts]),
+                            steps=np.fromfile(os.path.join(tmp, "vtk_out", "steps.bin")))
     finally:
         shutil.rmtree(tmp)
 
@@ -183,6 +202,11 @@ def main():
         screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
         print("golden vectors written to", OUT)
         return
+    if only == ["vtk"]:  # the field visualization fixtures alone
+        fixtures_for(harness, "kat-small-vtk.job", "kat-small-vtk", with_kats=False)
+        vtk_fixture(harness, "kat-small-vtk.job", "kat-small-vtk")
+        print("golden vectors written to", OUT)
+        return
     fixtures_for(harness, "kat-small.job", "kat-small-fd")
     fixtures_for(harness, "kat-small-nsfd.job", "kat-small-nsfd")
     fixtures_for(harness, "kat-small-sc.job", "kat-small-sc", with_kats=False)
@@ -191,6 +215,8 @@ def main():
     fixtures_for(harness, "kat-small-optical.job", "kat-small-optical", with_kats=False)
     fixtures_for(harness, "kat-small-screen.job", "kat-small-screen", with_kats=False)
     screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
+    fixtures_for(harness, "kat-small-vtk.job", "kat-small-vtk", with_kats=False)
+    vtk_fixture(harness, "kat-small-vtk.job", "kat-small-vtk")
     print("golden vectors written to", OUT)
 
 

@@ -208,3 +208,34 @@ def test_screen_file_format_matches_reference():
         mine = rows[rows[:, 7] == i][:, :6]
         prelude = int(z["offsets"][0, i])
         assert mg.format_screen_text(mine, first_in_file=prelude == 0) == texts[i][prelude:]
+
+
+def test_field_vtk_files_match_reference(tmp_path):
+    """The field-visualization writer (all-domain and the three in-plane orientations) reproduces
+    the reference's .vts and .pvts files byte for byte from the oracle's E, B and A^n at the
+    steps where Solver::solve writes them."""
+    import mithra_gb300 as mg
+    m = meta("kat-small-vtk")
+    init = load("kat-small-vtk", "init")
+    z = load("kat-small-vtk", "vtk")
+    setup = mg.Setup.from_job(__import__("tests.conftest", fromlist=["job"]).job("kat-small-vtk.job"))
+    sm = setup.meta()
+    names = [setup.vtk_basename(i).split("/")[-1] for i in range(int(sm["n_vtk"]))]
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+
+    def write(run):
+        for i, name in enumerate(names):
+            if mg.vtk_due(sm, i, run.time):
+                mg.write_field_vtk(sm, i, str(tmp_path / name), run.n_time, run.en, run.bn, run.an)
+
+    r.after_recycle = write
+    for _ in range(12):
+        r.step()
+    ref, start = {}, 0
+    for name, size in zip(z["names"], z["text_sizes"]):
+        ref[str(name)] = bytes(z["text"][start:start + size])
+        start += size
+    mine = {p.name: p.read_bytes() for p in tmp_path.iterdir()}
+    assert sorted(mine) == sorted(ref)
+    for name in ref:
+        assert mine[name] == ref[name], name
