@@ -157,6 +157,8 @@ int mithra_gpu_download_scalar(mithra_ctx* ctx, double* fnp1, double* fn, double
 int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn);
 /* chargeVectorn_ (src/solver.h:271) as 11-double records. */
 int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n);
+/* The same from records already in device memory (on the context's device). */
+int mithra_gpu_upload_particles_device(mithra_ctx* ctx, const double* dev_rec, size_t n);
 int mithra_gpu_download_particles(mithra_ctx* ctx, double* rec, size_t cap, size_t* n);
 int mithra_gpu_particle_count(mithra_ctx* ctx, size_t* n);
 int mithra_gpu_set_time(mithra_ctx* ctx, const mithra_time_state* t);
@@ -301,6 +303,14 @@ int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double*
 int mithra_setup_total_time(const mithra_setup* s, double* total_time);
 /* Writes `key value` lines (the derived scalars of the initialisation) into buf. */
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed);
+/* mithra_setup_from_job with the particle phase of Solver::initialize on GPU `device`:
+ * Bunch::initializeEllipsoid (src/classes.cpp:104-298), Solver::lorentzBoostBunch
+ * (src/solver.cpp:263-423), distributeParticles and shiftBackInTime run as kernels and the
+ * particles stay in device memory (mithra_gpu_create_from_setup takes them without a host copy;
+ * mithra_setup_particles downloads them).  Ellipsoid bunches with the Halton generator only;
+ * other bunch types are refused with MITHRA_ERR_ARG.  Records agree with the host
+ * initialisation to the last place of the device's log/sin/cos. */
+int mithra_setup_from_job_device(const char* job_path, int device, mithra_setup** out, char* err, size_t err_len);
 /* Base name (directory prefixed, as Solver::initializeSeedVTK, src/solver.cpp:961-964) of the
  * i-th field-visualization output; the other parameters of the outputs are in the meta text
  * (vtk<i>_type, _plane, _rhythm (bunch frame), _pos0..2 (bunch frame), _nfield, _f<l>). */

@@ -160,6 +160,8 @@ _SIGS = {
     "mithra_setup_total_time": [_vp, _dp],
     "mithra_setup_meta": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_vtk_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_from_job_device": [C.c_char_p, C.c_int, _P(_vp), C.c_char_p, C.c_size_t],
+    "mithra_gpu_upload_particles_device": [_vp, _vp, C.c_size_t],
     "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
     "mithra_gpu_screen_profile": [_vp],
     "mithra_gpu_create_from_setup": [_vp, C.c_int, C.c_int, C.c_double, _P(_vp)],
@@ -227,10 +229,16 @@ class Setup:
         self._h = handle
 
     @classmethod
-    def from_job(cls, path: str) -> "Setup":
+    def from_job(cls, path: str, device_init: bool = False, device: int = 0) -> "Setup":
+        """Parses the job and runs Solver::initialize.  device_init=True runs the particle phase
+        (ellipsoid bunch generation, boost, distribution, time shift) as kernels on `device`,
+        and the particles stay there for Context.from_setup."""
         h = _vp()
         err = C.create_string_buffer(1024)
-        r = lib().mithra_setup_from_job(os.fsencode(path), C.byref(h), err, len(err))
+        if device_init:
+            r = lib().mithra_setup_from_job_device(os.fsencode(path), int(device), C.byref(h), err, len(err))
+        else:
+            r = lib().mithra_setup_from_job(os.fsencode(path), C.byref(h), err, len(err))
         if r != 0:
             raise MithraError("job %s: %s (status %d)" % (path, err.value.decode(errors="replace"), r))
         return cls(h)

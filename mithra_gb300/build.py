@@ -21,6 +21,8 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(REPO, "include")] + ARCH
+# Translation units whose arithmetic must round like the host initialisation (no FMA contraction).
+NO_FMA = {"init_kernels.cu"}
 HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
               "-I", os.path.join(REPO, "include")]
 
@@ -53,7 +55,8 @@ def build(verbose: bool = False) -> str:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         objs.append(obj)
         if _stale(obj, src, headers):
-            jobs.append(([NVCC] + CUDA_FLAGS + ["-c", src, "-o", obj], obj))
+            extra = ["--fmad=false"] if os.path.basename(src) in NO_FMA else []
+            jobs.append(([NVCC] + CUDA_FLAGS + extra + ["-c", src, "-o", obj], obj))
     for src in sorted(glob.glob(os.path.join(CSRC, "host", "*.cpp"))):
         obj = os.path.join(BUILD, "host_" + os.path.basename(src) + ".o")
         objs.append(obj)

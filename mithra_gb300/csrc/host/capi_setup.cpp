@@ -37,8 +37,34 @@ int mithra_setup_from_job(const char* job_path, mithra_setup** out, char* err, s
   return MITHRA_OK;
 }
 
+int mithra_setup_from_job_device(const char* job_path, int device, mithra_setup** out, char* err, size_t err_len) {
+  if (!job_path || !out) return MITHRA_ERR_ARG;
+  *out = nullptr;
+  mithra_setup* h = new mithra_setup();
+  try {
+    h->s.job = mithra::host::parse_job_file(job_path);
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    delete h;
+    return MITHRA_ERR_PARSE;
+  }
+  h->s.device_init = true;
+  h->s.dstore.device = device;
+  try {
+    h->s.initialize();
+  } catch (const std::exception& e) {
+    if (err && err_len) snprintf(err, err_len, "%s", e.what());
+    mithra::devinit::release(h->s.dstore);
+    delete h;
+    return MITHRA_ERR_ARG;
+  }
+  *out = h;
+  return MITHRA_OK;
+}
+
 int mithra_setup_destroy(mithra_setup* s) {
   if (!s) return MITHRA_ERR_ARG;
+  mithra::devinit::release(s->s.dstore);
   delete s;
   return MITHRA_OK;
 }
@@ -133,6 +159,12 @@ int mithra_setup_total_time(const mithra_setup* s, double* total_time) {
 
 int mithra_setup_particles(const mithra_setup* s, double* rec, size_t cap, size_t* n) {
   if (!s || !n) return MITHRA_ERR_ARG;
+  if (s->s.device_init) {  // copy of the device records
+    *n = s->s.dstore.n;
+    if (!rec || !*n) return MITHRA_OK;
+    char err[256];
+    return mithra::devinit::download(s->s.dstore, rec, std::min(cap, *n), err, sizeof err) ? MITHRA_ERR_CUDA : MITHRA_OK;
+  }
   const auto& C = s->s.charges;
   *n = C.size();
   if (!rec) return MITHRA_OK;
@@ -189,7 +221,7 @@ int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int devic
   S.fill_grid(&g);
   S.fill_push(&p);
   if (capacity_factor < 1.0) capacity_factor = 1.0;
-  const size_t cap = (size_t)std::ceil(S.charges.size() * capacity_factor) + 1024;
+  const size_t cap = (size_t)std::ceil(S.particle_count() * capacity_factor) + 1024;
   int r = mithra_gpu_create(&g, &p, precision, device, cap, out);
   if (r) return r;
   mithra_ctx* ctx = *out;
@@ -219,10 +251,15 @@ int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int devic
   const double* an = S.an.empty() ? a1.data() : S.an.data();
   const double* anm1 = S.anm1.empty() ? a1.data() : S.anm1.data();
   if ((r = mithra_gpu_upload_fields(ctx, a1.data(), an, anm1))) return bail(r);
-  std::vector<double> rec(S.charges.size() * 11);
-  size_t n = 0;
-  if ((r = mithra_setup_particles(s, rec.data(), S.charges.size(), &n))) return bail(r);
-  if ((r = mithra_gpu_upload_particles(ctx, rec.data(), n))) return bail(r);
+  if (S.device_init) {
+    if (S.dstore.device != device) return bail(MITHRA_ERR_ARG);  // records live on another device
+    if ((r = mithra_gpu_upload_particles_device(ctx, S.dstore.rec, S.dstore.n))) return bail(r);
+  } else {
+    std::vector<double> rec(S.charges.size() * 11);
+    size_t n = 0;
+    if ((r = mithra_setup_particles(s, rec.data(), S.charges.size(), &n))) return bail(r);
+    if ((r = mithra_gpu_upload_particles(ctx, rec.data(), n))) return bail(r);
+  }
   mithra_time_state t;
   mithra_setup_time(s, &t);
   if ((r = mithra_gpu_set_time(ctx, &t))) return bail(r);

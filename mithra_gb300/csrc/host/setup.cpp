@@ -324,6 +324,61 @@ void scale_beam(Beam& b, double c0) {  // src/solver.cpp:77-125
 
 }  // namespace
 
+void Setup::dev_check(int r) {
+  if (r) die(dev_err);
+}
+
+// Solver::initializeBunch for device initialisation: every bunch-initialization group must be
+// an ellipsoid with the Halton generator; each position of a group is one call of
+// Bunch::initializeEllipsoid (src/classes.cpp:104-298) with the scalar prologue computed here
+// exactly as init_ellipsoid does and the particle loops on the device.
+void Setup::init_bunch_on_device() {
+  for (auto& bi : job.bunch.inits) {
+    if (bi.type != "ellipsoid")
+      die("device initialisation supports ellipsoid bunches only (bunch type " + bi.type + ")");
+    if (bi.generator == "random") die("device initialisation supports the Halton generator only");
+    if (bi.distribution != "uniform" && bi.distribution != "gaussian")
+      die("The longitudinal type is not correctly given to the code !!!");
+  }
+  for (auto& bi : job.bunch.inits) {
+    if (bi.position.empty()) bi.position.push_back({0.0, 0.0, 0.0});
+    const size_t group_start = dstore.n;
+    for (size_t ia = 0; ia < bi.position.size(); ia++) {
+      BunchInit b = bi;
+      if (b.numberOfParticles % 4 != 0) b.numberOfParticles += 4 - b.numberOfParticles % 4;
+      if (b.bF > 2.0 || b.bF < 0.0) die("The bunching factor can not be larger than one or a negative value !!!");
+      devinit::Ellipsoid e;
+      e.Np = b.numberOfParticles;
+      e.Np0 = (unsigned)(dstore.n - group_start);
+      e.ng = (b.lambda == 0.0) ? 1 : 4;
+      e.n_main = e.Np / e.ng;
+      e.n_taper = unsigned(e.Np / e.ng * (1.0 + 2.0 * b.lambda * std::sqrt(2.0 * PI) / (2.0 * b.sigmaPosition[2])));
+      e.gaussian = (b.distribution == "gaussian") ? 1 : 0;
+      e.shot_noise = b.shotNoise ? 1 : 0;
+      e.q = b.cloudCharge / e.Np;
+      for (int d = 0; d < 3; d++) {
+        e.gb[d] = b.initialGamma * b.betaVector[d];
+        e.sig_r[d] = b.sigmaPosition[d];
+        e.sig_gb[d] = b.sigmaGammaBeta[d];
+        e.pos[d] = b.position[ia][d];
+      }
+      e.tran_trun = b.tranTrun;
+      e.long_trun = b.longTrun;
+      e.lambda = b.lambda;
+      e.bF_user = b.bF;
+      e.bFP = b.bFP;
+      double zmin = 1e100, bF = 0.0;
+      if (b.shotNoise) {
+        dev_check(devinit::candidate_zmin(dstore.device, e, &zmin, dev_err, sizeof dev_err));
+        zmin = zmin + b.position[ia][2];
+        const double Ne = b.cloudCharge * b.lambda / (2.0 * b.sigmaPosition[2]);
+        bF = (b.bF == 0.0) ? 1.0 / std::sqrt(Ne) : b.bF;
+      }
+      dev_check(devinit::generate(dstore, e, zmin, bF, dev_err, sizeof dev_err));
+    }
+  }
+}
+
 void Setup::initialize() {
   Mesh& mesh = job.mesh;
   Bunch& bunch = job.bunch;
@@ -380,7 +435,9 @@ void Setup::initialize() {
   seed.gamma = gamma;
 
   // Solver::initializeBunch, src/solver.cpp:1130-1178.
+  if (device_init) init_bunch_on_device();
   for (auto& b : bunch.inits) {
+    if (device_init) break;
     std::vector<Charge> qv;
     if (b.position.empty()) b.position.push_back({0.0, 0.0, 0.0});
     if (b.type == "manual")
@@ -442,6 +499,10 @@ void Setup::initialize() {
     return (zr >= zp[0]) && (zr < zp[1]);
   };
   auto distribute = [&]() {  // Solver::distributeParticles with one rank, src/solver.cpp:429-487
+    if (device_init) {
+      dev_check(devinit::distribute(dstore, zmin, mesh.meshLength[2], zp[0], zp[1], dev_err, sizeof dev_err));
+      return;
+    }
     std::vector<Charge> kept;
     kept.reserve(charges.size());
     for (auto& c : charges)
@@ -455,6 +516,7 @@ void Setup::initialize() {
   else bunch.timeStep = mesh.timeStep / std::ceil(mesh.timeStep / bunch.timeStep);
   nUpdateBunch = mesh.timeStep / bunch.timeStep;
   double zmaxL = -1.0e100;
+  if (device_init) dev_check(devinit::boost(dstore, gamma, beta, &zmaxL, dev_err, sizeof dev_err));
   for (auto& q : charges) {
     double gq = std::sqrt(1.0 + norm2(q.gb));
     double bz = q.gb[2] / gq;
@@ -471,6 +533,7 @@ void Setup::initialize() {
   seed.dt = dt_shift;
   bunch.zu = zmaxG;
   bunch.beta = beta;
+  if (device_init) dev_check(devinit::back_propagate(dstore, bunch.zu, beta, dev_err, sizeof dev_err));
   for (auto& q : charges) {
     double gq = std::sqrt(1.0 + norm2(q.gb));
     q.rnp[0] += q.gb[0] / gq * (q.rnp[2] - bunch.zu) * beta;
@@ -479,12 +542,13 @@ void Setup::initialize() {
   }
   if (mesh.optimizePosition && und.size() > 0) {
     double zL = 0.0, bzL = 0.0;
+    if (device_init) dev_check(devinit::sums_z_bz(dstore, &zL, &bzL, dev_err, sizeof dev_err));
     for (auto& q : charges) {
       zL += q.rnp[2];
       bzL += q.gb[2] / std::sqrt(1 + norm2(q.gb));
     }
     double zG = zL, bzG = bzL;
-    unsigned NqG = (unsigned)charges.size();
+    unsigned NqG = (unsigned)particle_count();
     zG /= NqG;
     bzG /= NqG;
     double shift = bzG * (zmaxG + und[0].dist / gamma - zG) / (bzG + beta) + zG;
@@ -492,6 +556,7 @@ void Setup::initialize() {
     bunch.zu = zmaxG;
     dt_shift = -1.0 / (beta * und[0].c0) * (zmaxG + und[0].dist / gamma);
     seed.dt = dt_shift;
+    if (device_init) dev_check(devinit::shift_z(dstore, shift, dev_err, sizeof dev_err));
     for (auto& q : charges) q.rnp[2] -= shift;
   }
   distribute();
@@ -500,11 +565,15 @@ void Setup::initialize() {
     for (auto& u : und) Lu += u.lu * u.length / gamma;
     double zEnd = mesh.totalDist / gamma;
     double zMin = 1e100, bz = 0;
+    if (device_init) {
+      dev_check(devinit::min_z(dstore, &zMin, dev_err, sizeof dev_err));
+      dev_check(devinit::sums_z_bz(dstore, nullptr, &bz, dev_err, sizeof dev_err));
+    }
     for (auto& q : charges) {
       zMin = std::min(zMin, q.rnp[2]);
       bz += q.gb[2] / std::sqrt(1 + norm2(q.gb));
     }
-    unsigned Nq = (unsigned)charges.size();
+    unsigned Nq = (unsigned)particle_count();
     bz /= Nq;
     mesh.totalTime = 1 / (c0 * (bz + beta)) * (zEnd - beta * c0 * dt_shift - zMin + bz / beta * Lu);
   }
@@ -691,6 +760,7 @@ void Setup::initialize() {
     time -= mesh.timeShift;
     timep1 -= mesh.timeShift;
     timeBunch -= mesh.timeShift;
+    if (device_init) dev_check(devinit::time_shift(dstore, c0, mesh.timeShift, dev_err, sizeof dev_err));
     for (auto& q : charges) {
       double t = c0 * mesh.timeShift / std::sqrt(1.0 + norm2(q.gb));
       for (int d = 0; d < 3; d++) q.rnp[d] -= t * q.gb[d];
@@ -794,7 +864,7 @@ std::string Setup::meta() const {
   kv("seed_c0", job.seed.c0); kv("seed_dt", job.seed.dt);
   kv("n_ext", (double)job.extFields.size());
   for (size_t x = 0; x < job.extFields.size(); x++) beam_meta(kv, "ext" + std::to_string(x) + "_", job.extFields[x]);
-  kv("n_particles", (double)charges.size());
+  kv("n_particles", (double)particle_count());
   kv("n_fel", (double)job.fel.size());
   for (size_t o2 = 0; o2 < power.size(); o2++) {
     const PowerCfg& pc = power[o2];

@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "mithra_gpu.h"
+#include "devinit.h"
 #include "params.h"
 
 namespace mithra {
@@ -33,6 +34,13 @@ struct Setup {
   long long nTime = 0, nTimeBunch = 0;
   double nUpdateBunch = 0;
   std::vector<Charge> charges;
+  // Particles generated and transformed on the device (Setup::device_init); `charges` stays empty.
+  bool device_init = false;
+  devinit::Store dstore;
+  size_t particle_count() const { return device_init ? dstore.n : charges.size(); }
+  char dev_err[256] = {0};
+  void dev_check(int r);
+  void init_bunch_on_device();
   // Field-update coefficients (uf_), current and bunch-update constants (uc_, ub_).
   double a[6] = {0}, nsfd_alpha = 0, nsfd_beta = 0;
   double bB[5] = {0}, cB[5] = {0}, dB[5] = {0}, eE[5] = {0}, fE[5] = {0}, gE[5] = {0}, hC[17] = {0};

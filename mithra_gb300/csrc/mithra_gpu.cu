@@ -828,12 +828,30 @@ int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
   return MITHRA_OK;
 }
 
+namespace {
+// Records already in device memory (host upload or device initialisation) -> particle arrays.
+int particles_from_device_records(mithra_ctx* ctx, const double* staging, size_t n);
+}  // namespace
+
 int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
   if (!ctx || (n && !rec)) return MITHRA_ERR_ARG;
   if (n > ctx->capacity) return fail(ctx, MITHRA_ERR_CAPACITY, "%zu particles exceed capacity %zu", n, ctx->capacity);
   double* staging = nullptr;
   { int r = mithra::staging(ctx, std::max<size_t>(n, 1) * 11 * sizeof(double), (void**)&staging); if (r) return r; }
   if (n) CK(cudaMemcpyAsync(staging, rec, n * 11 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  return particles_from_device_records(ctx, staging, n);
+}
+
+int mithra_gpu_upload_particles_device(mithra_ctx* ctx, const double* dev_rec, size_t n) {
+  if (!ctx || (n && !dev_rec)) return MITHRA_ERR_ARG;
+  if (n > ctx->capacity) return fail(ctx, MITHRA_ERR_CAPACITY, "%zu particles exceed capacity %zu", n, ctx->capacity);
+  return particles_from_device_records(ctx, dev_rec, n);
+}
+
+}  // extern "C"
+
+namespace {
+int particles_from_device_records(mithra_ctx* ctx, const double* staging, size_t n) {
   if (ctx->precision == MITHRA_PRECISION_FP64) {
     k_records_to_soa<<<grid_stride_blocks(ctx, (long long)n, 256), 256, 0, ctx->stream>>>(staging, (long long)n, ctx->pt);
     CK(cudaGetLastError());
@@ -856,6 +874,9 @@ int mithra_gpu_upload_particles(mithra_ctx* ctx, const double* rec, size_t n) {
   ctx->particles_loaded = true;
   return MITHRA_OK;
 }
+}  // namespace
+
+extern "C" {
 
 int mithra_gpu_particle_count(mithra_ctx* ctx, size_t* n) {
   if (!ctx || !n) return MITHRA_ERR_ARG;
