@@ -133,7 +133,7 @@ def resonant_wavelength(p: dict) -> float:
     return p["lambda_u"] * (1.0 + 0.5 * p["K"] ** 2) / (2.0 * p["gamma"] ** 2)
 
 
-def design_parameters(n: int, seed: int, small: bool = False) -> list[dict]:
+def design_parameters(n: int, seed: int, small: bool = False, seeded: bool = False) -> list[dict]:
     """Seeded FEL designs for the surrogate: the sweep family's undulator and bunch ranges
     (gamma 100 .. 250) with the undulator length (periods) and the bunch radius varied as well.
     The mesh follows the radiation as the 48x48x384 FEL job does: 80 resonant wavelengths along
@@ -142,7 +142,9 @@ def design_parameters(n: int, seed: int, small: bool = False) -> list[dict]:
     the power varies by several percent, irregularly, with the number of macro-particles (their
     sampling noise seeds the radiation), which is a numerical parameter and not a design input.
     small=True: 40 wavelengths on 192 cells, a 32x32 transverse mesh, 32768 particles and short
-    undulators (fast runs for tests)."""
+    undulators (fast runs for tests).  seeded=True adds a resonant continuous seed with strength
+    parameter a0 drawn log-uniformly in 1e-6 .. 3e-5 (seed_power = a0^2); otherwise the
+    radiation starts from the bunch's noise (seed_power = 0)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
@@ -157,6 +159,9 @@ def design_parameters(n: int, seed: int, small: bool = False) -> list[dict]:
             seed_power=0.0,
             solver="NSFD",
         )
+        if seeded:
+            p["seed_a0"] = float(10.0 ** rng.uniform(-6.0, np.log10(3e-5)))
+            p["seed_power"] = p["seed_a0"] ** 2
         lam = resonant_wavelength(p)
         if small:
             p.update(periods=int(rng.integers(6, 13)), n_transverse=32, n_longitudinal=192, lz=40.0 * lam,
@@ -170,7 +175,8 @@ def design_parameters(n: int, seed: int, small: bool = False) -> list[dict]:
 
 def features(ps: list[dict]) -> np.ndarray:
     return np.array([[p["gamma"] / 100.0, p["K"], p["lambda_u"] / 1e4, p["periods"] / 10.0, np.log10(p["charge_pc"]),
-                      p["sigma_r"] / 100.0, np.log10(p["energy_spread"]), p["seed_power"]] for p in ps])
+                      p["sigma_r"] / 100.0, np.log10(p["energy_spread"]),
+                      np.log10(p["seed_power"]) if p["seed_power"] > 0 else -20.0] for p in ps])
 
 
 def solve_designs(ps: list[dict], spectrum_points: int, workdir: str, device: int = 0, chunk: int = 256):
@@ -296,6 +302,7 @@ def main(argv=None):
     ap.add_argument("--designs", type=int, default=2304, help="solved designs (training + held-out)")
     ap.add_argument("--held-out", type=int, default=256)
     ap.add_argument("--small", action="store_true", help="32x32x192 meshes, short undulators")
+    ap.add_argument("--seeded", action="store_true", help="designs with a resonant seed of varied power")
     ap.add_argument("--spectrum", type=int, default=128, help="frequency points of the spectrum")
     ap.add_argument("--steps", type=int, default=3000, help="Adam steps")
     ap.add_argument("--batch", type=int, default=128, help="mini-batch size")
@@ -312,7 +319,7 @@ def main(argv=None):
         host_s, dev_s = float(d["host_s"]), float(d["dev_s"])
         a.designs, a.spectrum = X.shape[0], spectra.shape[1]
     else:
-        ps = design_parameters(a.designs, a.seed, small=a.small)
+        ps = design_parameters(a.designs, a.seed, small=a.small, seeded=a.seeded)
         work = tempfile.mkdtemp(prefix="mithra-surrogate-")
         curves, spectra, psat, host_s, dev_s = solve_designs(ps, a.spectrum, work)
         X = features(ps)
@@ -343,7 +350,7 @@ def main(argv=None):
                          accepted_p90_err=float(np.quantile(err[acc], 0.9)) if acc.any() else None,
                          speedup=solve_s / (infer_s + f * solve_s)))
     print(json.dumps(dict(
-        designs=a.designs, held_out=a.held_out, small=a.small, spectrum=a.spectrum,
+        designs=a.designs, held_out=a.held_out, small=a.small, seeded=a.seeded, spectrum=a.spectrum,
         solve_s_per_design=solve_s, host_s_per_design=host_s / a.designs, device_s_per_design=dev_s / a.designs,
         train_s=train_s, train_steps=a.steps, final_loss=[float(x) for x in loss[-100:].mean(0)],
         infer_s_per_design=infer_s, median_err=float(np.median(err)), p90_err=float(np.quantile(err, 0.9)),

@@ -47,7 +47,9 @@ def job_text(p: dict, spectrum_points: int = 0) -> str:
     "lz" (mesh length along z in um, default 180; the bunch's rms length is lz / 6, truncated at
     lz / 3, and the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD);
     spectrum_points > 0 samples the power at that many normalized frequencies in 0.9 .. 1.1
-    instead of at 1.0 only."""
+    instead of at 1.0 only.  p["seed_a0"] > 0 adds a continuous gaussian-beam seed at the
+    resonant wavelength lambda_u (1 + K^2/2) / (2 gamma^2), polarised along y, focused at the
+    undulator start with a waist of 2 sigma_r and that strength parameter."""
     lx, lz = 2400.0, float(p.get("lz", 180.0))
     dx, dz = lx / p["n_transverse"], lz / p["n_longitudinal"]
     periods = int(p.get("periods", PERIODS))
@@ -60,6 +62,30 @@ def job_text(p: dict, spectrum_points: int = 0) -> str:
                 "    number-of-frequency-points   = %d" % spectrum_points)
     else:
         freq = "normalized-frequency    = 1.0"
+    a0 = float(p.get("seed_a0", 0.0))
+    field = ""
+    if a0 > 0.0:
+        lam = p["lambda_u"] * (1.0 + 0.5 * p["K"] ** 2) / (2.0 * p["gamma"] ** 2)
+        field = f"""
+FIELD
+{{
+  field-initialization
+  {{
+    type                    = gaussian-beam
+    position                = ( 0.0, 0.0, 0.0 )
+    direction               = ( 0.0, 0.0, 1.0 )
+    polarization            = ( 0.0, 1.0, 0.0 )
+    radius-parallel         = {2.0 * sr!r}
+    radius-perpendicular    = {2.0 * sr!r}
+    strength-parameter      = {a0!r}
+    signal-type             = gaussian
+    offset                  = 0.0
+    pulse-length            = 1.0e12
+    wavelength              = {lam!r}
+    CEP                     = 0.0
+  }}
+}}
+"""
     return f"""# sweep instance {p['index']}
 MESH
 {{
@@ -94,6 +120,7 @@ BUNCH
   }}
 }}
 
+{field}
 UNDULATOR
 {{
   static-undulator
