@@ -130,19 +130,53 @@ __global__ void __launch_bounds__(1024) k_scan_add(int* counts, int* offsets, co
 }
 
 // Pass 3: scatter every particle to its sorted slot in the other buffer set.
+// Each thread moves two particles per iteration: all their loads are issued before any store,
+// so a thread keeps the destination lookups and 2 x 15 loads in flight (the kernel is bound by
+// the latency of the offsets[key] lookup, not by bandwidth).
+struct Moved {
+  long long cell, mcell;
+  float fx, fy, fz, gx, gy, gz, mfx, mfy, mfz, q;
+  uint8_t e, status;
+  int id;
+  long long d;
+};
+
+__device__ __forceinline__ Moved move_load(const ParticlesF32& src, const int* __restrict__ key,
+                                           const int* __restrict__ rank, const int* __restrict__ offsets,
+                                           long long p) {
+  Moved m;
+  m.d = (long long)offsets[key[p]] + rank[p];
+  m.cell = src.cell[p];
+  m.fx = src.fx[p]; m.fy = src.fy[p]; m.fz = src.fz[p];
+  m.gx = src.gx[p]; m.gy = src.gy[p]; m.gz = src.gz[p];
+  m.mcell = src.mcell[p];
+  m.mfx = src.mfx[p]; m.mfy = src.mfy[p]; m.mfz = src.mfz[p];
+  m.q = src.q[p]; m.e = src.e[p]; m.status = src.status[p]; m.id = src.id[p];
+  return m;
+}
+
+__device__ __forceinline__ void move_store(const ParticlesF32& dst, const Moved& m) {
+  const long long d = m.d;
+  dst.cell[d] = m.cell;
+  dst.fx[d] = m.fx; dst.fy[d] = m.fy; dst.fz[d] = m.fz;
+  dst.gx[d] = m.gx; dst.gy[d] = m.gy; dst.gz[d] = m.gz;
+  dst.mcell[d] = m.mcell;
+  dst.mfx[d] = m.mfx; dst.mfy[d] = m.mfy; dst.mfz[d] = m.mfz;
+  dst.q[d] = m.q; dst.e[d] = m.e; dst.status[d] = m.status; dst.cross[d] = 0;
+  dst.id[d] = m.id;
+}
+
 __global__ void __launch_bounds__(256) k_tile_scatter(ParticlesF32 src, ParticlesF32 dst, const int* key,
                                                       const int* rank, const int* offsets, int n_bins) {
   const long long n_in = offsets[n_bins];  // every particle of the unsorted set, erased ones included
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n_in;
-       p += (long long)gridDim.x * blockDim.x) {
-    const long long d = (long long)offsets[key[p]] + rank[p];
-    dst.cell[d] = src.cell[p];
-    dst.fx[d] = src.fx[p]; dst.fy[d] = src.fy[p]; dst.fz[d] = src.fz[p];
-    dst.gx[d] = src.gx[p]; dst.gy[d] = src.gy[p]; dst.gz[d] = src.gz[p];
-    dst.mcell[d] = src.mcell[p];
-    dst.mfx[d] = src.mfx[p]; dst.mfy[d] = src.mfy[p]; dst.mfz[d] = src.mfz[p];
-    dst.q[d] = src.q[p]; dst.e[d] = src.e[p]; dst.status[d] = src.status[p]; dst.cross[d] = 0;
-    dst.id[d] = src.id[p];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n_in; p += 2 * stride) {
+    const Moved a = move_load(src, key, rank, offsets, p);
+    const bool two = p + stride < n_in;
+    Moved b;
+    if (two) b = move_load(src, key, rank, offsets, p + stride);
+    move_store(dst, a);
+    if (two) move_store(dst, b);
   }
 }
 
