@@ -183,7 +183,7 @@ __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, co
 // BEAMS: the job defines optical undulators or external fields (a separate instantiation keeps
 // the FP64 laser-beam code, and its registers, out of the common kernel).
 template <bool BEAMS>
-__global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
+__global__ void __launch_bounds__(256, BEAMS ? 1 : 3) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
                                                   const UndTableEntry* __restrict__ table, ParticlesF32 pt,
                                                   const float* __restrict__ E, const float* __restrict__ B,
                                                   long long cstride, long long plane, int P1, StateDev* st,
@@ -192,16 +192,37 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
   const double tb = st->time_bunch;
   const double tshift = C.bc * (tb + C.dt_shift);  // beta c0 (timeBunch + dt_)
   unsigned long long local_cross = 0, local_nt = 0;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-       p += (long long)gridDim.x * blockDim.x) {
+  // The next particle's state is loaded before the current one's gather and Boris step, so each
+  // thread keeps two particles' loads in flight.
+  struct Loaded {
+    long long cell;
+    float fx, fy, fz, gx, gy, gz;
+    uint8_t status, e;
+  };
+  auto load = [&](long long q) {
+    Loaded L;
+    L.status = pt.status[q];
+    L.cell = pt.cell[q];
+    L.fx = pt.fx[q]; L.fy = pt.fy[q]; L.fz = pt.fz[q];
+    L.gx = pt.gx[q]; L.gy = pt.gy[q]; L.gz = pt.gz[q];
+    L.e = pt.e[q];
+    return L;
+  };
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  Loaded cur{};
+  if (p < n) cur = load(p);
+  for (; p < n; p += stride) {
+    Loaded nxt{};
+    if (p + stride < n) nxt = load(p + stride);
     int8_t cross = 0;
-    if (!(pt.status[p] & 1)) {
-      const long long cell = pt.cell[p];
+    if (!(cur.status & 1)) {
+      const long long cell = cur.cell;
       int i, j, k;
       unpack_cell(cell, i, j, k);
       const int Lk = C.N2 - 1;
       const int kw = ((k % Lk) + Lk) % Lk;  // wrapped cell of pmod(z - zmin, Lz)
-      float fx = pt.fx[p], fy = pt.fy[p], fz = pt.fz[p];
+      float fx = cur.fx, fy = cur.fy, fz = cur.fz;
       if (save_rnm) { pt.mcell[p] = cell; pt.mfx[p] = fx; pt.mfy[p] = fy; pt.mfz[p] = fz; }
       const float x = C.xmin + ((float)i + fx) * C.dx, y = C.ymin + ((float)j + fy) * C.dy;
       const bool b1x = (i >= 1 && i <= C.N0 - 3 && (i > 1 || fx > 0.0f));
@@ -221,7 +242,7 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
         laser_beams_add(C.P64, und, C.n_und, tb, xd, yd, zd, b64, e64);
         for (int c = 0; c < 3; c++) { bt[c] += (float)b64[c]; et[c] += (float)e64[c]; }
       }
-      uint8_t e = pt.e[p];
+      uint8_t e = cur.e;
       if (e) {
         if (b1x && b1y && b1z) {
           const long long m = (long long)k * plane + (long long)i * P1 + j;
@@ -255,7 +276,7 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
         pt.e[p] = 1;
       }
       // Boris rotation and drift (src/solver.cpp:1519-1541) in FP32.
-      float gx = pt.gx[p], gy = pt.gy[p], gz = pt.gz[p];
+      float gx = cur.gx, gy = cur.gy, gz = cur.gz;
       const float mx = fmaf(C.r1, et[0], gx), my = fmaf(C.r1, et[1], gy), mz = fmaf(C.r1, et[2], gz);
       const float d1 = sqrtf(1.0f + (mx * mx + my * my + mz * mz));
       const float f = C.r2 / d1;
@@ -285,6 +306,7 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
     }
     pt.cross[p] = cross;
     local_cross += (cross != 0);
+    cur = nxt;
   }
   for (int o = 16; o > 0; o >>= 1) {
     local_cross += __shfl_down_sync(0xffffffffu, local_cross, o);
