@@ -7,11 +7,67 @@
 
 using namespace mithra;
 
+namespace {
+
+typedef CUresult (*EncodeTiledFnGemm)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                      const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                      CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFnGemm encode_fn() {
+  static EncodeTiledFnGemm fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFnGemm)p;
+  }
+  return fn;
+}
+
+// Row-major BF16 [rows x K] operand as a tensor map with 64 x box_rows boxes and 128-byte swizzle.
+bool operand_map(CUtensorMap* map, const void* base, int rows, int K, int box_rows) {
+  EncodeTiledFnGemm enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
 extern "C" int mithra_tc_gemm(const void* A, const void* B, float* C, void* C_bf16, const float* bias, int M, int N,
                               int K, int act, void* stream, int* err_dev) {
   if (!A || !B || (!C && !C_bf16) || !err_dev || M <= 0 || N <= 0 || K <= 0) return MITHRA_ERR_ARG;
   if (M % tc::BM || N % tc::BN || K % tc::BK) return MITHRA_ERR_ARG;
   if (((uintptr_t)A | (uintptr_t)B) & 15) return MITHRA_ERR_ARG;
+  // Long K loops go through the pipelined TMA kernel; one or two K blocks through the simple one
+  // (nothing to overlap, and no tensor maps to encode).
+  if (K >= 4 * tc::BK) {
+    static bool attr_tma = false;
+    if (!attr_tma) {
+      if (cudaFuncSetAttribute(tc::k_gemm_bf16_tma<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tc::gemm_tma_smem<128>()) != cudaSuccess ||
+          cudaFuncSetAttribute(tc::k_gemm_bf16_tma<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tc::gemm_tma_smem<256>()) != cudaSuccess)
+        return MITHRA_ERR_CUDA;
+      attr_tma = true;
+    }
+    const bool wide = N % 256 == 0;  // 128 x 256 tiles halve the A traffic per flop
+    CUtensorMap ma, mb;
+    if (!operand_map(&ma, A, M, K, tc::BM) || !operand_map(&mb, B, N, K, wide ? 256 : 128)) return MITHRA_ERR_CUDA;
+    if (wide)
+      tc::k_gemm_bf16_tma<256><<<dim3(M / tc::BM, N / 256), 128, tc::gemm_tma_smem<256>(), (cudaStream_t)stream>>>(
+          ma, mb, C, (__nv_bfloat16*)C_bf16, bias, M, N, K, act, err_dev);
+    else
+      tc::k_gemm_bf16_tma<128><<<dim3(M / tc::BM, N / 128), 128, tc::gemm_tma_smem<128>(), (cudaStream_t)stream>>>(
+          ma, mb, C, (__nv_bfloat16*)C_bf16, bias, M, N, K, act, err_dev);
+    return cudaGetLastError() == cudaSuccess ? MITHRA_OK : MITHRA_ERR_CUDA;
+  }
   static bool attr = false;
   if (!attr) {
     if (cudaFuncSetAttribute(tc::k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kGemmSmem) !=

@@ -13,6 +13,7 @@
 // Requirements (checked by the host launcher): M % 128 == 0, N % 128 == 0, K % 64 == 0, 16-byte
 // aligned rows.
 #pragma once
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cstdint>
 
@@ -183,6 +184,143 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(const __nv_bfloat16* __restri
 // CTAs share an SM and their 4 x 128 TMEM columns fit the SM's 512 (tcgen05.alloc never waits).
 constexpr size_t kGemmSmem = 56 * 1024;
 static_assert(2 * kTileBytes + 1024 <= kGemmSmem, "tiles fit");
+
+// ---- pipelined form: TMA loads, a ring of stages, one producer and one MMA thread ------------
+//
+// A 128 x TBN tile per CTA (TBN = 128 or 256) and K blocks of 64; the operand tiles arrive by
+// cp.async.bulk.tensor with 128-byte swizzle into a ring of kStages stages: one thread issues
+// the loads of a stage once the tensor core has released it (an mbarrier armed by
+// tcgen05.commit), another waits for a stage's bytes to land (an mbarrier with the expected
+// transaction count) and issues its four MMAs.  Loads of later stages overlap the MMAs of
+// earlier ones.  Shared-memory descriptors use the 128-byte-swizzle K-major layout: rows of 128
+// bytes (64 BF16), 8-row groups 1024 bytes apart, the K step of 16 advancing the start by 32 bytes.
+constexpr int kStages = 4;
+// A 128 x 64 tile and a TBN x 64 tile per stage (TBN = 128 or 256 columns of C per CTA).
+template <int TBN>
+constexpr int stage_bytes() { return kTileBytes + TBN * BK * 2; }
+template <int TBN>
+constexpr size_t gemm_tma_smem() { return (size_t)kStages * stage_bytes<TBN>() + 1024; }
+
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;                       // leading byte offset (unused within one swizzle atom)
+  d |= (uint64_t)((1024u >> 4) & 0x3FFFu) << 32;  // 8-row groups 1024 bytes apart
+  d |= (uint64_t)1 << 46;                       // descriptor version
+  d |= (uint64_t)2 << 61;                       // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void mbar_init_count(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared.b64 [%0], %1;" ::"r"(saddr(b)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared.b64 _, [%0], %1;" ::"r"(saddr(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(saddr(bar))
+      : "memory");
+}
+
+template <int TBN>
+__global__ void __launch_bounds__(128, 1) k_gemm_bf16_tma(const __grid_constant__ CUtensorMap map_a,
+                                                        const __grid_constant__ CUtensorMap map_b,
+                                                        float* __restrict__ C, __nv_bfloat16* __restrict__ Cb,
+                                                        const float* __restrict__ bias, int M, int N, int K, int act,
+                                                        int* err) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* tiles = smem_raw + ((1024u - (saddr(smem_raw) & 1023u)) & 1023u);
+  __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint32_t tmem_base;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * TBN;
+  const int nk = K / BK;
+  constexpr int kSB = stage_bytes<TBN>();
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tmem_base)), "n"(TBN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < kStages; s++) {
+      mbar_init_count(&full[s], 1);
+      mbar_init_count(&empty[s], 1);
+    }
+    mbar_init_count(&done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_abort = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+
+  if (warp == 0 && lane == 0) {  // producer
+    int issued = 0;
+    volatile int* abort_flag = &s_abort;
+    for (int kb = 0; kb < nk && !*abort_flag; kb++) {
+      const int s = kb % kStages;
+      if (kb >= kStages && !mbar_wait(&empty[s], (uint32_t)(((kb / kStages) - 1) & 1))) {
+        s_abort = 1;
+        break;
+      }
+      uint8_t* sa = tiles + s * kSB;
+      mbar_expect_tx(&full[s], kSB);
+      tma_load_2d(saddr(sa), &map_a, kb * BK, m0, &full[s]);
+      tma_load_2d(saddr(sa + kTileBytes), &map_b, kb * BK, n0, &full[s]);
+      issued = kb + 1;
+    }
+    // no copy may still be landing when the CTA leaves: wait (bounded) for the last stages
+    for (int kb = issued > kStages ? issued - kStages : 0; kb < issued; kb++)
+      if (!mbar_wait(&full[kb % kStages], (uint32_t)((kb / kStages) & 1))) s_abort = 1;
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    const uint32_t idesc = instr_desc(BM, TBN);
+    volatile int* abort_flag = &s_abort;
+    for (int kb = 0; kb < nk && !*abort_flag; kb++) {
+      const int s = kb % kStages;
+      if (!mbar_wait(&full[s], (uint32_t)((kb / kStages) & 1))) {
+        s_abort = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a = saddr(tiles + s * kSB), b = a + kTileBytes;
+#pragma unroll
+      for (int ks = 0; ks < BK / 16; ks++)
+        mma_bf16(tmem, smem_desc_sw128(a + ks * 32), smem_desc_sw128(b + ks * 32), idesc, (kb > 0 || ks > 0) ? 1u : 0u);
+      mma_commit(&empty[s]);  // the stage is free once these MMAs have read it
+    }
+    mma_commit(&done);
+  }
+  // every thread: the accumulator is complete when `done` fires
+  const bool ok = mbar_wait(&done, 0u);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (ok && !s_abort) {
+    const int row = m0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < TBN; c0 += 32) {
+      float v[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+      for (int i = 0; i < 32; i++) {
+        const int col = n0 + c0 + i;
+        float x = v[i] + (bias ? bias[col] : 0.0f);
+        if (act == kRelu) x = fmaxf(x, 0.0f);
+        if (C) C[(size_t)row * N + col] = x;
+        if (Cb) Cb[(size_t)row * N + col] = __float2bfloat16_rn(x);
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(TBN) : "memory");
+}
 
 }  // namespace tc
 }  // namespace mithra

@@ -18,7 +18,9 @@ def test_tc_gemm_matches_fp32(torch_cuda):
     from mithra_gb300 import surrogate
     torch = torch_cuda
     g = torch.Generator(device="cuda").manual_seed(3)
-    for M, N, K in ((128, 128, 64), (256, 384, 192), (512, 256, 512)):
+    # K >= 256 runs the pipelined TMA kernel (ring of 4 stages; K = 2048 wraps it 8 times), with
+    # 128 x 256 tiles when N is a multiple of 256 and 128 x 128 tiles otherwise
+    for M, N, K in ((128, 128, 64), (256, 384, 192), (256, 384, 512), (512, 256, 512), (1024, 512, 2048)):
         A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
         B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
         bias = torch.randn(N, device="cuda", generator=g)
