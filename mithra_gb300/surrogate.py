@@ -290,6 +290,38 @@ def evaluate(model: FelSurrogate, ps: list[dict], workdir: str, threshold: float
     return psat, fb, _time.perf_counter() - t0
 
 
+def gemm_bench(sizes=((512, 512, 512), (4096, 4096, 4096), (8192, 8192, 8192)), reps: int = 10) -> list[dict]:
+    """Throughput of mithra_tc_gemm (BF16 in, FP32 out) on random operands, CUDA-event timed on
+    the default stream after three warm-up calls, with the largest error against a float64 product."""
+    import torch
+    out = []
+    g = torch.Generator(device="cuda").manual_seed(0)
+    for M, N, K in sizes:
+        A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+        C = torch.empty(M, N, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+        def call():
+            _ck(_lib().mithra_tc_gemm(A.data_ptr(), B.data_ptr(), C.data_ptr(), None, None, M, N, K, 0, None,
+                                      err.data_ptr()), "mithra_tc_gemm")
+        for _ in range(3):
+            call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ref = A.double() @ B.double().T
+        rel = float(((C.double() - ref).abs().max() / ref.abs().max()).item())
+        out.append(dict(M=M, N=N, K=K, ms=ms, tflops=2.0 * M * N * K / ms / 1e9, max_rel_err=rel,
+                        wait_error=int(err.item())))
+    return out
+
+
 def main(argv=None):
     """Dataset from batched solves, ensemble training, and screening of held-out designs against
     the full solver; prints one JSON line with the errors, fallback fractions and speed-up."""
@@ -311,8 +343,12 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--save", default="", help="npz file for the dataset")
     ap.add_argument("--load", default="", help="npz dataset written by --save (no solves)")
+    ap.add_argument("--gemm-bench", action="store_true", help="time mithra_tc_gemm and exit")
     a = ap.parse_args(argv)
 
+    if a.gemm_bench:
+        print(json.dumps(gemm_bench()))
+        return
     if a.load:
         d = np.load(a.load)
         X, curves, spectra, psat = (d[k].astype(np.float64) for k in ("X", "curves", "spectra", "psat"))
