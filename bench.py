@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--autotune-steps", type=int, default=0,
                     help="sweep-192: autotune every instance on this many steps per candidate shape")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--sweep-designs", type=int, default=384,
+                    help="sweep-192: designs marched to their exits through a refilled queue (0: skip)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp32-compare", action="store_true",
@@ -420,6 +422,15 @@ def run_sweep(args, dist):
     batch.close()
     for c in ctxs:
         c.close()
+    measured = None
+    if args.sweep_designs > 0:
+        # measured: that many further designs of the family marched to their exits through a
+        # refilled queue of 192 slots (device set-up, prelude and batch rebuilds included)
+        extra = sweep.sweep_parameters(192 + args.sweep_designs)[192:]
+        done, wall, rebuilds = sweep.run_queue(extra, tempfile.mkdtemp(prefix="mithra-queue-"), slots=192,
+                                               device=dist.local)
+        measured = {"designs": len(done), "wall_s": wall, "runs_per_hour": dist.world * len(done) * 3600.0 / wall,
+                    "batch_rebuilds": rebuilds}
     if dist.rank != 0:
         return
     out = {
@@ -430,7 +441,7 @@ def run_sweep(args, dist):
                    "nodes": total_nodes, "particles": total_particles,
                    "autotune_steps": args.autotune_steps, "parallelism": "one graph launch per step for all instances",
                    "l2": "inputs larger than L2"},
-        "fel_runs_per_hour": {"lockstep": runs_lockstep, "refilled": runs_refill,
+        "fel_runs_per_hour": {"lockstep": runs_lockstep, "refilled": runs_refill, "measured_queue": measured,
                               "steps_to_exit": {"min": min(steps_to_end), "mean": float(np.mean(steps_to_end)),
                                                 "max": max(steps_to_end)}},
         "tuning": [[t.blocks_per_sm, t.slab_planes, ms] for t, ms in tuned][:8],

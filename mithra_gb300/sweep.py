@@ -12,7 +12,9 @@ and stepped together on one device by `mithra_gb300.Batch`.
 """
 from __future__ import annotations
 
+import math
 import os
+import time
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -184,3 +186,50 @@ def steps_to_exit(setup: Setup, ctx: Context) -> int:
         time += dt
         n += 1
     return n
+
+
+def run_queue(params: list[dict], workdir: str, slots: int = 192, precision: int = FP32, device: int = 0,
+              device_init: bool = True, min_chunk: int = 30, spectrum_points: int = 0):
+    """Marches every design to its undulator exit with at most `slots` instances on the device:
+    the batch runs until its earliest design exits (at least `min_chunk` steps, a multiple of six
+    so that every instance stays in the same step phase), finished designs leave with their
+    power rows and new designs take their slots (set up on the device when `device_init`).
+    Returns ({index: power rows}, wall seconds, batch rebuilds)."""
+    from . import Batch, Context, Setup
+    os.makedirs(workdir, exist_ok=True)
+    queue = list(params)
+    active = []  # [params, context, field steps left]
+    done = {}
+    rebuilds = 0
+    t0 = time.perf_counter()
+
+    def admit():
+        while queue and len(active) < slots:
+            p = queue.pop(0)
+            path = os.path.join(workdir, "queue-%06d.job" % p["index"])
+            with open(path, "w") as f:
+                f.write(job_text(p, spectrum_points))
+            s = Setup.from_job(path, device_init=device_init, device=device)
+            c = Context.from_setup(s, precision, device)
+            c.run_prelude()
+            active.append([p, c, steps_to_exit(s, c)])
+
+    admit()
+    while active:
+        n = max(min_chunk, min(a[2] for a in active))
+        n = 6 * math.ceil(n / 6)
+        batch = Batch([a[1] for a in active])
+        batch.run(n)
+        batch.close()
+        rebuilds += 1
+        keep = []
+        for a in active:
+            a[2] -= n
+            if a[2] <= 0:
+                done[a[0]["index"]] = a[1].power_rows()
+                a[1].close()
+            else:
+                keep.append(a)
+        active[:] = keep
+        admit()
+    return done, time.perf_counter() - t0, rebuilds

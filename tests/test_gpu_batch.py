@@ -72,3 +72,24 @@ def test_autotune_steps_are_part_of_the_march(gpu_available):
     run = load("kat-small-fd", "run")
     assert rel_l2(c.download_fields()[1], run["an12"]) <= MARCH_RTOL
     assert c.tuning().blocks_per_sm == t.blocks_per_sm
+
+
+def test_refilled_queue_matches_standalone_runs(gpu_available, tmp_path):
+    """sweep.run_queue: six designs through four slots (two refills); every design's power rows
+    equal those of its own standalone march to the undulator exit."""
+    from mithra_gb300 import surrogate, sweep
+    ps = surrogate.design_parameters(6, 11, small=True)
+    done, wall, rebuilds = sweep.run_queue(ps, str(tmp_path / "q"), slots=4, min_chunk=12)
+    assert sorted(done) == [p["index"] for p in ps] and rebuilds >= 2
+    for p in ps[:2] + ps[-1:]:
+        path = tmp_path / ("alone-%d.job" % p["index"])
+        path.write_text(sweep.job_text(p))
+        s = mg.Setup.from_job(str(path), device_init=True)
+        c = mg.Context.from_setup(s, mg.FP32)
+        c.run_prelude()
+        n = sweep.steps_to_exit(s, c)
+        c.run(n)
+        alone = c.power_rows().reshape(n, -1)
+        queued = done[p["index"]].reshape(-1, alone.shape[1])[:n]
+        np.testing.assert_allclose(queued, alone, rtol=1e-4, atol=1e-6 * np.abs(alone).max())
+        c.close()
