@@ -150,3 +150,17 @@ def test_fp32_error_statement_p_spectrum_bunching(gpu_available):
           "(relative L2), bunching factor %.2e (%.4g vs %.4g)" % (psat, curve, spec, bunch, b32, b64))
     assert psat <= PSAT_RTOL
     assert curve <= 0.05 and spec <= 0.05 and bunch <= 0.05
+
+
+def test_fp32_space_charge_march(gpu_available):
+    """FdTdSC in the mixed form: A and phi after 12 steps against the reference's own FP64 run."""
+    run = load("kat-small-sc", "run")
+    ctx = mg.Context.from_setup(mg.Setup.from_job(job("kat-small-sc.job")), mg.FP32)
+    ctx.run_prelude()
+    ctx.run(12)
+    _, an, _ = ctx.download_fields()
+    _, fn, _ = ctx.download_scalar()
+    ea, ef = rel_l2(an, run["an12"]), rel_l2(fn, run["fn12"])
+    print("kat-small-sc: FP32 relative L2 after 12 steps: A %.3e, phi %.3e" % (ea, ef))
+    assert ea <= BEAM_MARCH_RTOL and ef <= BEAM_MARCH_RTOL
+    assert ctx.download_particles().shape == run["particles12"].shape
