@@ -17,6 +17,9 @@ def meta(tag: str) -> dict:
 
 TAGS = {"kat-small-fd": ("kat-small.job", 0), "kat-small-nsfd": ("kat-small-nsfd.job", 1)}
 
+# Jobs with an initial state and a 12-step march of the reference, for layout edge cases.
+LAYOUT_TAGS = {"kat-small-ragged": ("kat-small-ragged.job", 0)}
+
 # Jobs with only an initial state and a 12-step march of the reference (no single-stage vectors):
 # the TF/SF seed, the external laser fields and the optical undulator.
 BEAM_TAGS = {"kat-small-seed": ("kat-small-seed.job", 1), "kat-small-ext": ("kat-small-ext.job", 0),

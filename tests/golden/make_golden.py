@@ -5,7 +5,7 @@ against the single-rank MPI stand-in) on the small known-answer jobs and stores 
 outputs as compressed .npz files.  Run from the repository root in a checkout that has the
 reference tree:
 
-    python tests/golden/make_golden.py [REF_SRC] [--only=screen|--only=vtk]
+    python tests/golden/make_golden.py [REF_SRC] [--only=screen|--only=vtk|--only=ragged]
 
 Seeded random inputs (numpy default_rng) make every fixture reproducible.
 """
@@ -202,6 +202,10 @@ def main():
         screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
         print("golden vectors written to", OUT)
         return
+    if only == ["ragged"]:  # the ragged-mesh march alone
+        fixtures_for(harness, "kat-small-ragged.job", "kat-small-ragged", with_kats=False)
+        print("golden vectors written to", OUT)
+        return
     if only == ["vtk"]:  # the field visualization fixtures alone
         fixtures_for(harness, "kat-small-vtk.job", "kat-small-vtk", with_kats=False)
         vtk_fixture(harness, "kat-small-vtk.job", "kat-small-vtk")
@@ -217,6 +221,7 @@ def main():
     screen_fixture(harness, "kat-small-screen.job", "kat-small-screen")
     fixtures_for(harness, "kat-small-vtk.job", "kat-small-vtk", with_kats=False)
     vtk_fixture(harness, "kat-small-vtk.job", "kat-small-vtk")
+    fixtures_for(harness, "kat-small-ragged.job", "kat-small-ragged", with_kats=False)
     print("golden vectors written to", OUT)
 
 

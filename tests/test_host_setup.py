@@ -3,14 +3,14 @@ import numpy as np
 import pytest
 
 import mithra_gb300 as mg
-from tests._golden import BEAM_TAGS, TAGS, load, meta
+from tests._golden import BEAM_TAGS, LAYOUT_TAGS, TAGS, load, meta
 from tests.conftest import job
 
 
-@pytest.mark.parametrize("tag", sorted(TAGS) + sorted(BEAM_TAGS))
+@pytest.mark.parametrize("tag", sorted(TAGS) + sorted(BEAM_TAGS) + sorted(LAYOUT_TAGS))
 def test_setup_matches_reference(tag):
     ref = meta(tag)
-    s = mg.Setup.from_job(job({**TAGS, **BEAM_TAGS}[tag][0]))
+    s = mg.Setup.from_job(job({**TAGS, **BEAM_TAGS, **LAYOUT_TAGS}[tag][0]))
     m = s.meta()
     for k, v in ref.items():
         assert k in m, k
