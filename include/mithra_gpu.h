@@ -315,6 +315,13 @@ int mithra_setup_from_job_device(const char* job_path, int device, mithra_setup*
  * i-th field-visualization output; the other parameters of the outputs are in the meta text
  * (vtk<i>_type, _plane, _rhythm (bunch frame), _pos0..2 (bunch frame), _nfield, _f<l>). */
 int mithra_setup_vtk_basename(const mithra_setup* s, int i, char* buf, size_t len, size_t* needed);
+/* Base name (directory prefixed, src/radiation.cpp:74-76) of the o-th radiation-power output (the
+ * FEL-OUTPUT entries that sample power, in order); its files are <base>-<l>.txt, one per
+ * frequency, written by the caller from mithra_gpu_power_rows. */
+int mithra_setup_power_basename(const mithra_setup* s, int o, char* buf, size_t len, size_t* needed);
+/* Base name (directory prefixed) of the lab-frame screens of FEL-OUTPUT entry jf; their files are
+ * <base>-p0-screen<i>.txt, i counting that entry's screens in position order. */
+int mithra_setup_screen_basename(const mithra_setup* s, int jf, char* buf, size_t len, size_t* needed);
 
 /* ---- field visualization files ----------------------------------------------------------- */
 

@@ -160,6 +160,8 @@ _SIGS = {
     "mithra_setup_total_time": [_vp, _dp],
     "mithra_setup_meta": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_vtk_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_power_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_screen_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_from_job_device": [C.c_char_p, C.c_int, _P(_vp), C.c_char_p, C.c_size_t],
     "mithra_gpu_upload_particles_device": [_vp, _vp, C.c_size_t],
     "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
@@ -299,6 +301,27 @@ class Setup:
         lib().mithra_setup_fields(self._h, dptr(anp1), dptr(an), dptr(anm1))
         return anp1, an, anm1
 
+    def _string(self, fn: str, i: int) -> str:
+        need = C.c_size_t()
+        if getattr(lib(), fn)(self._h, int(i), None, 0, C.byref(need)) != 0:
+            raise MithraError("%s: no entry %d" % (fn, i))
+        buf = C.create_string_buffer(need.value)
+        getattr(lib(), fn)(self._h, int(i), buf, need.value, C.byref(need))
+        return buf.value.decode()
+
+    def screen_basename(self, jf: int) -> str:
+        """Base name of the screens of FEL-OUTPUT entry jf (directory prefixed)."""
+        return self._string("mithra_setup_screen_basename", jf)
+
+    def power_basename(self, o: int) -> str:
+        """Base name of radiation-power output o (directory prefixed); files <base>-<l>.txt."""
+        need = C.c_size_t()
+        if lib().mithra_setup_power_basename(self._h, int(o), None, 0, C.byref(need)) != 0:
+            raise MithraError("no radiation-power output %d" % o)
+        buf = C.create_string_buffer(need.value)
+        lib().mithra_setup_power_basename(self._h, int(o), buf, need.value, C.byref(need))
+        return buf.value.decode()
+
     def vtk_basename(self, i: int) -> str:
         """Base name of field-visualization output i (directory prefixed)."""
         need = C.c_size_t()
@@ -364,6 +387,23 @@ def write_field_vtk(meta: dict, i: int, basename: str, n_time: int, en, bn, an, 
                                      dptr(an), dptr(fn))
     if r != 0:
         raise MithraError("mithra_vtk_write_field failed with status %d (output %d)" % (r, i))
+
+
+def format_power_text(rows, n_planes: int, n_freq: int, freq: int, first_in_file: bool = True) -> str:
+    """One frequency's power file as the reference writes it (src/radiation.cpp:80-82, :222-229):
+    per step, for each sampling plane, z_lab and P tab-terminated, in %.15e, the stream's width of
+    40 applying once, to the first value of the file.  rows: the row log of one power output,
+    steps x (n_planes x (1 + n_freq)) as mithra_gpu_power_rows returns it."""
+    rows = np.asarray(rows, dtype=np.float64).reshape(-1, n_planes, 1 + n_freq)
+    out = []
+    for r, step in enumerate(rows):
+        vals = []
+        for k in range(n_planes):
+            vals += ["%.15e" % step[k, 0], "%.15e" % step[k, 1 + freq]]
+        if r == 0 and first_in_file:
+            vals[0] = vals[0].rjust(40)
+        out.append("\t".join(vals) + "\t\n")
+    return "".join(out)
 
 
 def format_screen_text(rows, first_in_file: bool = True) -> str:
@@ -701,8 +741,13 @@ class FdTd:
 
     precision = FP64
 
-    def __init__(self, setup: Setup, precision: int | None = None, device: int = 0, capacity_factor: float = 1.25):
+    def __init__(self, setup: Setup, precision: int | None = None, device: int = 0, capacity_factor: float = 1.25,
+                 write_files: bool = True):
+        """write_files: solve() writes the job's output files where the reference does (power
+        per frequency, field visualization, lab-frame screens), relative to the working
+        directory for relative names."""
         self.setup = setup
+        self.write_files = write_files
         self.meta = setup.meta()
         self.ctx = Context.from_setup(setup, self.precision if precision is None else precision, device, capacity_factor)
         screens = setup.screens()
@@ -751,7 +796,7 @@ class FdTd:
         m = self.meta
         nv = int(m.get("n_vtk", 0))
         due = []
-        if nv:
+        if nv and self.write_files:
             t, dt = self.ctx.get_time().time, m["dt"]
             for s in range(n):
                 outs = [i for i in range(nv) if vtk_due(m, i, t)]
@@ -764,7 +809,57 @@ class FdTd:
             self._step_with_vtk(outs)
             done = s + 1
         self.ctx.run(n - done)
-        return self.ctx.power_rows()
+        rows = self.ctx.power_rows()
+        if self.write_files:
+            self.write_power_files(rows)
+            self.write_screen_files()
+        return rows
+
+    def write_power_files(self, rows=None):
+        """<base>-<l>.txt for every radiation-power output and frequency, in the reference's
+        layout (Solver::powerSample, src/radiation.cpp:222-229)."""
+        m = self.meta
+        jfs = [jf for jf in range(int(m.get("n_fel", 0))) if "rp%d_N" % jf in m]
+        if not jfs:
+            return []
+        shape = [(int(m["rp%d_N" % jf]), int(m["rp%d_Nl" % jf])) for jf in jfs]
+        per_step = sum(N * (1 + nl) for N, nl in shape)
+        rows = (self.ctx.power_rows() if rows is None else np.asarray(rows)).reshape(-1, per_step)
+        names, off = [], 0
+        for o, (N, nl) in enumerate(shape):
+            block = rows[:, off:off + N * (1 + nl)]
+            off += N * (1 + nl)
+            base = self.setup.power_basename(o)
+            d = os.path.dirname(base)
+            if d:
+                os.makedirs(d, exist_ok=True)
+            for l in range(nl):
+                name = "%s-%d.txt" % (base, l)
+                with open(name, "w") as f:
+                    f.write(format_power_text(block, N, nl, l))
+                names.append(name)
+        return names
+
+    def write_screen_files(self):
+        """<base>-p0-screen<i>.txt per FEL-OUTPUT entry with screens (src/solver.cpp:2186-2252)."""
+        m = self.meta
+        n = int(m.get("n_screens", 0))
+        names, i = [], 0
+        while i < n:
+            jf = int(m["scr%d_fel" % i])
+            base = self.setup.screen_basename(jf)
+            d = os.path.dirname(base)
+            if d:
+                os.makedirs(d, exist_ok=True)
+            local = 0
+            while i < n and int(m["scr%d_fel" % i]) == jf:
+                name = "%s-p0-screen%d.txt" % (base, local)
+                with open(name, "w") as f:
+                    f.write(format_screen_text(self.ctx.screen_records(i)[:, :6]))
+                names.append(name)
+                i += 1
+                local += 1
+        return names
 
     def _step_with_vtk(self, outs):
         c = self.ctx
@@ -780,8 +875,9 @@ class FdTd:
         en, bn = c.download_eb()
         _, an, _ = c.download_fields()
         fn = c.download_scalar()[1] if isinstance(self, FdTdSC) else None
-        for i in outs:
-            write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
+        if self.write_files:
+            for i in outs:
+                write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
         if getattr(c, "n_screens", 0):
             c.call("mithra_gpu_screen_profile")
         c.power_sample()

@@ -202,6 +202,31 @@ int mithra_setup_vtk_basename(const mithra_setup* s, int i, char* buf, size_t le
   return MITHRA_OK;
 }
 
+int mithra_setup_power_basename(const mithra_setup* s, int o, char* buf, size_t len, size_t* needed) {
+  if (!s || o < 0 || o >= (int)s->s.power_fel_index.size()) return MITHRA_ERR_ARG;
+  const auto& rp = s->s.job.fel[(size_t)s->s.power_fel_index[(size_t)o]].radiationPower;
+  // Solver::initializePowerSample, src/radiation.cpp:74-76
+  const std::string b = (!rp.basename.empty() && rp.basename[0] == '/') ? rp.basename : rp.directory + rp.basename;
+  if (needed) *needed = b.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < b.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, b.c_str(), b.size() + 1);
+  return MITHRA_OK;
+}
+
+int mithra_setup_screen_basename(const mithra_setup* s, int jf, char* buf, size_t len, size_t* needed) {
+  if (!s || jf < 0 || jf >= (int)s->s.job.fel.size()) return MITHRA_ERR_ARG;
+  const auto& sp = s->s.job.fel[(size_t)jf].screenProfile;
+  if (!sp.sampling) return MITHRA_ERR_ARG;
+  // Solver::initializeScreenProfile, src/solver.cpp:2154
+  const std::string b = (!sp.basename.empty() && sp.basename[0] == '/') ? sp.basename : sp.directory + sp.basename;
+  if (needed) *needed = b.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < b.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, b.c_str(), b.size() + 1);
+  return MITHRA_OK;
+}
+
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
   if (!s) return MITHRA_ERR_ARG;
   const std::string m = s->s.meta();

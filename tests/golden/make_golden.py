@@ -103,10 +103,16 @@ def vtk_fixture(harness, jobname, tag, nsteps=12):
         run(harness, "vtk", job, nsteps, os.path.join(tmp, "vtk_out"), cwd=tmp)
         files = sorted(os.listdir(os.path.join(tmp, "vtk")))
         texts = [open(os.path.join(tmp, "vtk", f), "rb").read() for f in files]
+        # the power files Solver::powerSample writes in the same run
+        pfiles = sorted(os.listdir(os.path.join(tmp, "power-sampling")))
+        ptexts = [open(os.path.join(tmp, "power-sampling", f), "rb").read() for f in pfiles]
         np.savez_compressed(os.path.join(dst, "vtk.npz"), names=np.array(files),
                             text=np.frombuffer(b"".join(texts), dtype=np.uint8),
                             text_sizes=np.array([len(t) for t in texts]),
-                            steps=np.fromfile(os.path.join(tmp, "vtk_out", "steps.bin")))
+                            steps=np.fromfile(os.path.join(tmp, "vtk_out", "steps.bin")),
+                            power_names=np.array(pfiles),
+                            power_text=np.frombuffer(b"".join(ptexts), dtype=np.uint8),
+                            power_sizes=np.array([len(t) for t in ptexts]))
     finally:
         shutil.rmtree(tmp)
 

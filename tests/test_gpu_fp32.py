@@ -78,7 +78,7 @@ def test_fp32_deposit(gpu_available):
 
 def full_march_power(precision, jobname="fel-ir-48x48x384.job"):
     s = mg.Setup.from_job(job(jobname))
-    fd = mg.FdTd(s, precision=precision)
+    fd = mg.FdTd(s, precision=precision, write_files=False)
     rows = fd.solve()
     return rows.reshape(-1, 2)
 
@@ -135,7 +135,7 @@ def test_fp32_error_statement_p_spectrum_bunching(gpu_available):
     k = 4 * np.pi * m["gamma"] / m["und0_lu"]
     res = {}
     for prec in (mg.FP64, mg.FP32):
-        fd = mg.FdTd(s, precision=prec)
+        fd = mg.FdTd(s, precision=prec, write_files=False)
         rows = fd.solve().reshape(-1, 1 + nl)
         res[prec] = (rows[:, 1:], fd.ctx.bunching_factor(k))
         fd.ctx.close()

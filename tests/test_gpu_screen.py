@@ -102,3 +102,17 @@ def test_screens_off_and_capacity():
     ctx.set_screens([])              # no screens: the step graphs drop the kernel
     ctx.run(2)
     assert ctx.n_screens == 0
+
+
+def test_solve_writes_screen_files(tmp_path, monkeypatch):
+    """FdTd.solve() writes the screen files where the reference does (screen/scr-p0-screen<i>.txt)."""
+    monkeypatch.chdir(tmp_path)
+    z, texts = golden()
+    mg.FdTd(mg.Setup.from_job(job(JOB))).solve(max_steps=12)
+    for name, ref in zip(z["names"], texts):
+        mine = (tmp_path / "screen" / str(name)).read_text().splitlines()
+        b = ref.splitlines()
+        assert len(mine) == len(b)
+        A = np.array([[float(x) for x in l.split()] for l in mine])
+        B = np.array([[float(x) for x in l.split()] for l in b])
+        assert np.all(np.abs(A - B) <= 1e-11 * (np.abs(B).max(axis=0) + 1e-300))

@@ -34,6 +34,14 @@ def test_solve_writes_reference_vtk(gpu_available, tmp_path, monkeypatch, precis
     monkeypatch.chdir(tmp_path)        # the job writes to ./vtk/ like the reference
     setup = mg.Setup.from_job(job("kat-small-vtk.job"))
     mg.FdTd(setup, precision=precision).solve(max_steps=12)
+    # the power file written at the end of solve()
+    z = load("kat-small-vtk", "vtk")
+    pref = bytes(z["power_text"][:int(z["power_sizes"][0])]).decode().splitlines()
+    pmine = (tmp_path / "power-sampling" / str(z["power_names"][0])).read_text().splitlines()
+    assert len(pmine) == len(pref) and len(pmine[0].split("\t")[0]) == 40
+    A = np.array([[float(x) for x in l.split()] for l in pmine])
+    B = np.array([[float(x) for x in l.split()] for l in pref])
+    assert np.all(np.abs(A - B) <= max(rtol, 1e-9) * 10 * (np.abs(B).max(axis=0) + 1e-300))
     ref = reference_files()
     mine = {p.name: p.read_text() for p in (tmp_path / "vtk").iterdir()}
     assert sorted(mine) == sorted(ref)

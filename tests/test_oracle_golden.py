@@ -254,3 +254,19 @@ def test_oracle_ragged_mesh_march_matches_reference():
         assert np.array_equal(np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)])), run["power"][step - 1])
     assert np.array_equal(r.an, run["an12"]) and np.array_equal(r.anm1, run["anm1_12"])
     assert np.array_equal(r.particles, run["particles12"])
+
+
+def test_power_file_format_matches_reference():
+    """The power-file writer reproduces the reference's power-sampling file byte for byte from
+    the oracle's power rows (12 steps of kat-small-vtk, one plane, one frequency)."""
+    import mithra_gb300 as mg
+    m = meta("kat-small-vtk")
+    init = load("kat-small-vtk", "init")
+    z = load("kat-small-vtk", "vtk")
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    for _ in range(12):
+        r.step()
+    rows = np.array([np.ravel(np.column_stack([zl, pg.reshape(len(zl), -1)])) for zl, pg in r.power_rows])
+    N, nl = int(m["rp0_N"]), int(m["rp0_Nl"])
+    ref = bytes(z["power_text"][:int(z["power_sizes"][0])]).decode()
+    assert mg.format_power_text(rows, N, nl, 0) == ref
