@@ -322,6 +322,9 @@ int mithra_setup_power_basename(const mithra_setup* s, int o, char* buf, size_t 
 /* Base name (directory prefixed) of the lab-frame screens of FEL-OUTPUT entry jf; their files are
  * <base>-p0-screen<i>.txt, i counting that entry's screens in position order. */
 int mithra_setup_screen_basename(const mithra_setup* s, int jf, char* buf, size_t len, size_t* needed);
+/* File of the bunch-sampling group (directory prefixed, ".txt"), src/solver.cpp:1066-1068; its
+ * rows are mithra_gpu_bunch_sample at the bunch-frame rhythm (meta bunch_rhythm). */
+int mithra_setup_bunch_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed);
 
 /* ---- field visualization files ----------------------------------------------------------- */
 

@@ -162,6 +162,7 @@ _SIGS = {
     "mithra_setup_vtk_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_power_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_screen_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_bunch_sample_file": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_from_job_device": [C.c_char_p, C.c_int, _P(_vp), C.c_char_p, C.c_size_t],
     "mithra_gpu_upload_particles_device": [_vp, _vp, C.c_size_t],
     "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
@@ -309,6 +310,15 @@ class Setup:
         getattr(lib(), fn)(self._h, int(i), buf, need.value, C.byref(need))
         return buf.value.decode()
 
+    def bunch_sample_file(self) -> str:
+        """File of the bunch-sampling group (directory prefixed, .txt)."""
+        need = C.c_size_t()
+        if lib().mithra_setup_bunch_sample_file(self._h, None, 0, C.byref(need)) != 0:
+            raise MithraError("the job does not sample the bunch")
+        buf = C.create_string_buffer(need.value)
+        lib().mithra_setup_bunch_sample_file(self._h, buf, need.value, C.byref(need))
+        return buf.value.decode()
+
     def screen_basename(self, jf: int) -> str:
         """Base name of the screens of FEL-OUTPUT entry jf (directory prefixed)."""
         return self._string("mithra_setup_screen_basename", jf)
@@ -387,6 +397,18 @@ def write_field_vtk(meta: dict, i: int, basename: str, n_time: int, en, bn, an, 
                                      dptr(an), dptr(fn))
     if r != 0:
         raise MithraError("mithra_vtk_write_field failed with status %d (output %d)" % (r, i))
+
+
+def format_bunch_sample(row) -> str:
+    """One line of the bunch-sampling file (Solver::bunchSample, src/solver.cpp:1623-1635):
+    timeBunch, <r>, <gb>, rms r, rms gb in %.4e, tab-separated."""
+    return "\t".join("%.4e" % v for v in np.asarray(row, dtype=np.float64)[:13]) + "\n"
+
+
+def bunch_sample_due(meta: dict, time: float) -> bool:
+    """Solver::solve's condition for a bunch sample at field time `time` (src/solver.cpp:1252, :1356)."""
+    t = time + meta["time_shift"]
+    return bool(meta.get("bunch_sampling", 0)) and float(np.fmod(t, meta["bunch_rhythm"])) < meta["dt"] and t > 0.0
 
 
 def format_power_text(rows, n_planes: int, n_freq: int, freq: int, first_in_file: bool = True) -> str:
@@ -786,34 +808,97 @@ class FdTd:
 
     def solve(self, max_steps: int | None = None):
         """Solver::solve: the prelude, then field steps to the total time.  Steps at which a
-        field-visualization output is due (src/solver.cpp:1328-1340) run stage by stage and
-        write their files where the reference does (after the recycling); all others replay the
+        field-visualization output or a bunch sample is due (src/solver.cpp:1252, :1328-1356) run
+        stage by stage and write their files where the reference does; all others replay the
         captured step graph."""
-        self.ctx.run_prelude()
+        m = self.meta
+        c = self.ctx
+        sampling = self.write_files and bool(m.get("bunch_sampling", 0))
+        self._bunch_lines = []
+        if sampling:
+            self._prelude_with_samples()
+        else:
+            c.run_prelude()
         n = self.steps_to_total_time()
         if max_steps is not None:
             n = min(n, max_steps)
-        m = self.meta
-        nv = int(m.get("n_vtk", 0))
+        nv = int(m.get("n_vtk", 0)) if self.write_files else 0
         due = []
-        if nv and self.write_files:
-            t, dt = self.ctx.get_time().time, m["dt"]
+        if nv or sampling:
+            t, dt = c.get_time().time, m["dt"]
             for s in range(n):
                 outs = [i for i in range(nv) if vtk_due(m, i, t)]
-                if outs:
-                    due.append((s, outs))
+                bs = sampling and bunch_sample_due(m, t)
+                if outs or bs:
+                    due.append((s, outs, bs))
                 t += dt
         done = 0
-        for s, outs in due:
-            self.ctx.run(s - done)
-            self._step_with_vtk(outs)
+        for s, outs, bs in due:
+            c.run(s - done)
+            self._step_with_outputs(outs, bs)
             done = s + 1
-        self.ctx.run(n - done)
-        rows = self.ctx.power_rows()
+        c.run(n - done)
+        rows = c.power_rows()
         if self.write_files:
             self.write_power_files(rows)
             self.write_screen_files()
+            if sampling:
+                path = self.setup.bunch_sample_file()
+                d = os.path.dirname(path)
+                if d:
+                    os.makedirs(d, exist_ok=True)
+                with open(path, "w") as f:
+                    f.write("".join(self._bunch_lines))
         return rows
+
+    def _substeps(self):
+        t = 0.0
+        while t < self.meta["nUpdateBunch"]:
+            self.ctx.bunch_update()
+            t += 1.0
+
+    def _prelude_with_samples(self):
+        """The time_ < 0 loop of Solver::solve (src/solver.cpp:1232-1291) stage by stage, with its
+        screen profile and bunch samples."""
+        c = self.ctx
+        if not c.get_time().time < 0.0:
+            return
+        c.field_evaluate()  # no field update before time zero: E/B of the initial potentials
+        while True:
+            t = c.get_time()
+            if not t.time < 0.0:
+                break
+            c.save_positions()
+            self._substeps()
+            if getattr(c, "n_screens", 0):
+                c.call("mithra_gpu_screen_profile")
+            if bunch_sample_due(self.meta, t.time):
+                self._bunch_lines.append(format_bunch_sample(c.bunch_sample()))
+            c.recycle()
+            c.advance_time()
+
+    def _step_with_outputs(self, outs, bunch_sample: bool):
+        c = self.ctx
+        n_time = c.get_time().n_time
+        c.field_update()
+        c.save_positions()
+        self._substeps()
+        c.recycle()
+        if outs:
+            c.field_evaluate()
+            en, bn = c.download_eb()
+            _, an, _ = c.download_fields()
+            fn = c.download_scalar()[1] if isinstance(self, FdTdSC) else None
+            for i in outs:
+                write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
+        if bunch_sample:
+            self._bunch_lines.append(format_bunch_sample(c.bunch_sample()))
+        if getattr(c, "n_screens", 0):
+            c.call("mithra_gpu_screen_profile")
+        c.power_sample()
+        c.field_shift()
+        c.current_update()
+        c.advance_time()
 
     def write_power_files(self, rows=None):
         """<base>-<l>.txt for every radiation-power output and frequency, in the reference's
@@ -860,31 +945,6 @@ class FdTd:
                 i += 1
                 local += 1
         return names
-
-    def _step_with_vtk(self, outs):
-        c = self.ctx
-        n_time = c.get_time().n_time
-        c.field_update()
-        c.save_positions()
-        t = 0.0
-        while t < self.meta["nUpdateBunch"]:
-            c.bunch_update()
-            t += 1.0
-        c.recycle()
-        c.field_evaluate()
-        en, bn = c.download_eb()
-        _, an, _ = c.download_fields()
-        fn = c.download_scalar()[1] if isinstance(self, FdTdSC) else None
-        if self.write_files:
-            for i in outs:
-                write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
-        if getattr(c, "n_screens", 0):
-            c.call("mithra_gpu_screen_profile")
-        c.power_sample()
-        c.field_shift()
-        c.current_update()
-        c.advance_time()
-
 
 class FdTdSC(FdTd):
     """Drop-in for FdTdSC (src/fdtdSC.h): the same loop with the scalar potential."""

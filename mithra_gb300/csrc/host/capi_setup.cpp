@@ -227,6 +227,18 @@ int mithra_setup_screen_basename(const mithra_setup* s, int jf, char* buf, size_
   return MITHRA_OK;
 }
 
+int mithra_setup_bunch_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
+  if (!s || !s->s.job.bunch.sampling) return MITHRA_ERR_ARG;
+  const auto& b = s->s.job.bunch;
+  // Solver::initializeBunchUpdate, src/solver.cpp:1066-1068
+  const std::string f = ((!b.basename.empty() && b.basename[0] == '/') ? b.basename : b.directory + b.basename) + ".txt";
+  if (needed) *needed = f.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < f.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, f.c_str(), f.size() + 1);
+  return MITHRA_OK;
+}
+
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
   if (!s) return MITHRA_ERR_ARG;
   const std::string m = s->s.meta();

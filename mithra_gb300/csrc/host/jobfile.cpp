@@ -316,6 +316,7 @@ void read_bunch(Cursor& c, Job& J) {
           else if (grp == "bunch-visualization") J.bunch.vtk = v;
           else J.bunch.profile = v;
         } else if (n == "directory" || n == "base-name") {
+          if (grp == "bunch-sampling") (n == "directory" ? J.bunch.directory : J.bunch.basename) = string_of(l);
         } else if (n == "rhythm") {
           double v = double_of(l);
           if (grp == "bunch-sampling") J.bunch.rhythm = v;

@@ -512,6 +512,9 @@ void Setup::initialize() {
 
   // Solver::lorentzBoostBunch, src/solver.cpp:263-423.
   bunch.timeStep /= gamma;
+  bunch.rhythm /= gamma;  // src/solver.cpp:281
+  if (bunch.sampling && bunch.rhythm == 0)
+    die("The sampling rhythm of the bunch is zero although sampling is activated !!!");
   if (bunch.timeStep == 0) bunch.timeStep = mesh.timeStep;
   else bunch.timeStep = mesh.timeStep / std::ceil(mesh.timeStep / bunch.timeStep);
   nUpdateBunch = mesh.timeStep / bunch.timeStep;
@@ -873,6 +876,9 @@ std::string Setup::meta() const {
     for (int i = 0; i < pc.Nl; i++) kv(p + "w" + std::to_string(i), pc.w[i]);
     for (int i = 0; i < pc.N; i++) kv(p + "z" + std::to_string(i), pc.z[i]);
   }
+  kv("time_shift", mesh.timeShift);
+  kv("bunch_sampling", job.bunch.sampling ? 1.0 : 0.0);
+  kv("bunch_rhythm", job.bunch.rhythm);
   kv("n_vtk", (double)job.seed.vtk.size());
   for (size_t i = 0; i < job.seed.vtk.size(); i++) {
     const FieldVtk& v = job.seed.vtk[i];

@@ -17,7 +17,8 @@
  *   vtk     JOB N OUT               prelude and N steps with the field visualization where solve()
  *                                   calls it (the reference writes its .vts/.pvts files into the
  *                                   job's directory); OUT/steps.bin lists the nTime_ of each step
- *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile where solve()
+ *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile (and bunchSample,
+ *                                   when the job samples the bunch) where solve()
  *                                   calls it; the reference writes its own screen files into the
  *                                   job's directory, OUT/offsets.bin holds each screen file's size
  *                                   after the prelude and after every step
@@ -388,6 +389,9 @@ int main(int argc, char** argv) {
         ++s->nTimeBunch_;
       }
       s->screenProfile();
+      if (s->bunch_.sampling_ && fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.rhythm_) < s->mesh_.timeStep_ &&
+          (s->time_ + s->mesh_.timeShift_ > 0.0))
+        s->bunchSample();
       s->recycleParticles();
       s->timem1_ += s->mesh_.timeStep_;
       s->time_ += s->mesh_.timeStep_;
@@ -404,6 +408,9 @@ int main(int argc, char** argv) {
         ++s->nTimeBunch_;
       }
       s->recycleParticles();
+      if (s->bunch_.sampling_ && fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.rhythm_) < s->mesh_.timeStep_ &&
+          (s->time_ + s->mesh_.timeShift_ > 0.0))
+        s->bunchSample();
       s->screenProfile();
       s->powerSample();
       s->fieldShift();

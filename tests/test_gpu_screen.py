@@ -104,11 +104,18 @@ def test_screens_off_and_capacity():
     assert ctx.n_screens == 0
 
 
-def test_solve_writes_screen_files(tmp_path, monkeypatch):
-    """FdTd.solve() writes the screen files where the reference does (screen/scr-p0-screen<i>.txt)."""
+def test_solve_writes_screen_and_bunch_sample_files(tmp_path, monkeypatch):
+    """FdTd.solve() writes the screen files (screen/scr-p0-screen<i>.txt) and the bunch-sampling
+    file (bunch-sampling/bunch.txt, prelude and field steps) where the reference does."""
     monkeypatch.chdir(tmp_path)
     z, texts = golden()
     mg.FdTd(mg.Setup.from_job(job(JOB))).solve(max_steps=12)
+    bref = bytes(z["bunch_text"]).decode().splitlines()
+    bmine = (tmp_path / "bunch-sampling" / "bunch.txt").read_text().splitlines()
+    assert len(bmine) == len(bref)
+    A = np.array([[float(x) for x in l.split()] for l in bmine])
+    B = np.array([[float(x) for x in l.split()] for l in bref])
+    assert np.all(np.abs(A - B) <= 2e-4 * np.abs(B) + 1e-12 * np.abs(B).max(axis=0))
     for name, ref in zip(z["names"], texts):
         mine = (tmp_path / "screen" / str(name)).read_text().splitlines()
         b = ref.splitlines()

@@ -270,3 +270,26 @@ def test_power_file_format_matches_reference():
     N, nl = int(m["rp0_N"]), int(m["rp0_Nl"])
     ref = bytes(z["power_text"][:int(z["power_sizes"][0])]).decode()
     assert mg.format_power_text(rows, N, nl, 0) == ref
+
+
+def test_bunch_sample_file_matches_reference():
+    """Solver::bunchSample lines of the field steps (the last lines of the reference's file; the
+    first come from the prelude) byte for byte from the oracle's moments and format_bunch_sample."""
+    import mithra_gb300 as mg
+    from tests.conftest import job
+    m = meta("kat-small-screen")
+    sm = mg.Setup.from_job(job("kat-small-screen.job")).meta()
+    init = load("kat-small-screen", "init")
+    ref = bytes(load("kat-small-screen", "screen")["bunch_text"]).decode().splitlines(keepends=True)
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    lines = []
+
+    def sample(run):
+        if mg.bunch_sample_due(sm, run.time):
+            lines.append(mg.format_bunch_sample(np.concatenate([[run.time_bunch], po.bunch_sample(m, run.particles)])))
+
+    r.after_recycle = sample
+    for _ in range(12):
+        r.step()
+    assert 0 < len(lines) < len(ref)
+    assert lines == ref[len(ref) - len(lines):]
