@@ -325,6 +325,10 @@ int mithra_setup_screen_basename(const mithra_setup* s, int jf, char* buf, size_
 /* File of the bunch-sampling group (directory prefixed, ".txt"), src/solver.cpp:1066-1068; its
  * rows are mithra_gpu_bunch_sample at the bunch-frame rhythm (meta bunch_rhythm). */
 int mithra_setup_bunch_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed);
+/* File of the field-sampling group, <dir><base>-0.txt (src/solver.cpp:916-918); its points (bunch
+ * frame, inside the mesh), fields, rhythm and unit factors are in the meta text (fs_*); a row is
+ * time_ gamma_ and, per point, the position and the lab-frame fields of mithra_gpu_field_sample. */
+int mithra_setup_field_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed);
 
 /* ---- field visualization files ----------------------------------------------------------- */
 

@@ -14,6 +14,7 @@ with nvcc, and if that is impossible the import raises.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -163,6 +164,7 @@ _SIGS = {
     "mithra_setup_power_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_screen_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_bunch_sample_file": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_field_sample_file": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_from_job_device": [C.c_char_p, C.c_int, _P(_vp), C.c_char_p, C.c_size_t],
     "mithra_gpu_upload_particles_device": [_vp, _vp, C.c_size_t],
     "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
@@ -310,14 +312,21 @@ class Setup:
         getattr(lib(), fn)(self._h, int(i), buf, need.value, C.byref(need))
         return buf.value.decode()
 
+    def _file(self, fn: str, what: str) -> str:
+        need = C.c_size_t()
+        if getattr(lib(), fn)(self._h, None, 0, C.byref(need)) != 0:
+            raise MithraError("the job does not %s" % what)
+        buf = C.create_string_buffer(need.value)
+        getattr(lib(), fn)(self._h, buf, need.value, C.byref(need))
+        return buf.value.decode()
+
     def bunch_sample_file(self) -> str:
         """File of the bunch-sampling group (directory prefixed, .txt)."""
-        need = C.c_size_t()
-        if lib().mithra_setup_bunch_sample_file(self._h, None, 0, C.byref(need)) != 0:
-            raise MithraError("the job does not sample the bunch")
-        buf = C.create_string_buffer(need.value)
-        lib().mithra_setup_bunch_sample_file(self._h, buf, need.value, C.byref(need))
-        return buf.value.decode()
+        return self._file("mithra_setup_bunch_sample_file", "sample the bunch")
+
+    def field_sample_file(self) -> str:
+        """File of the field-sampling group (directory prefixed, -0.txt)."""
+        return self._file("mithra_setup_field_sample_file", "sample the field")
 
     def screen_basename(self, jf: int) -> str:
         """Base name of the screens of FEL-OUTPUT entry jf (directory prefixed)."""
@@ -403,6 +412,41 @@ def format_bunch_sample(row) -> str:
     """One line of the bunch-sampling file (Solver::bunchSample, src/solver.cpp:1623-1635):
     timeBunch, <r>, <gb>, rms r, rms gb in %.4e, tab-separated."""
     return "\t".join("%.4e" % v for v in np.asarray(row, dtype=np.float64)[:13]) + "\n"
+
+
+def field_sample_points(meta: dict) -> np.ndarray:
+    """The field-sampling points of a job (bunch frame, inside the mesh), (n, 3)."""
+    return np.array([[meta["fs_p%d_%d" % (i, d)] for d in range(3)] for i in range(int(meta.get("fs_n", 0)))])
+
+
+def field_sample_due(meta: dict, time: float) -> bool:
+    """Solver::solve's condition for a field sample at field time `time` (src/solver.cpp:1329)."""
+    return bool(meta.get("fs_sampling", 0)) and float(np.fmod(time, meta["fs_rhythm"])) < meta["dt"] and time > 0.0
+
+
+def format_field_sample(meta: dict, time: float, points, samples) -> str:
+    """One row of the field-sampling file (FdTd::fieldSample, src/fdtd.cpp:851-950): time_ gamma_,
+    then per point its position and the requested fields transformed to the lab frame and the
+    file's units, %.4e, tab-separated.  samples: (n, 9) E, B, A^n of Context.field_sample."""
+    g, c0 = meta["gamma"], meta["c0"]
+    Ce, Cb, Ca = meta["fs_Ce"], meta["fs_Cb"], meta["fs_Ca"]
+    gb = math.sqrt(math.pow(g, 2) - 1)
+    fields = [int(meta["fs_f%d" % l]) for l in range(int(meta.get("fs_nfield", 0)))]
+    out = ["%.4e" % (time * g)]
+    for p, v in zip(np.asarray(points, dtype=np.float64), np.asarray(samples, dtype=np.float64)):
+        e, b, a = v[0:3], v[3:6], v[6:9]
+        out += ["%.4e" % p[0], "%.4e" % p[1], "%.4e" % p[2]]
+        for f in fields:
+            if f == 0: x = (g * e[0] + c0 * gb * b[1]) * Ce
+            elif f == 1: x = (g * e[1] - c0 * gb * b[0]) * Ce
+            elif f == 2: x = e[2] * Ce
+            elif f == 3: x = (g * b[0] - gb / c0 * e[1]) * Cb
+            elif f == 4: x = (g * b[1] + gb / c0 * e[0]) * Cb
+            elif f == 5: x = b[2] * Cb
+            elif f < 9: x = a[f - 6] * Ca
+            else: continue  # FdTd writes nothing for the scalar potential
+            out.append("%.4e" % x)
+    return "\t".join(out) + "\t\n"
 
 
 def bunch_sample_due(meta: dict, time: float) -> bool:
@@ -814,7 +858,10 @@ class FdTd:
         m = self.meta
         c = self.ctx
         sampling = self.write_files and bool(m.get("bunch_sampling", 0))
+        fsampling = self.write_files and int(m.get("fs_n", 0)) > 0
         self._bunch_lines = []
+        self._field_lines = []
+        self._fs_points = field_sample_points(m) if fsampling else None
         if sampling:
             self._prelude_with_samples()
         else:
@@ -824,31 +871,35 @@ class FdTd:
             n = min(n, max_steps)
         nv = int(m.get("n_vtk", 0)) if self.write_files else 0
         due = []
-        if nv or sampling:
+        if nv or sampling or fsampling:
             t, dt = c.get_time().time, m["dt"]
             for s in range(n):
                 outs = [i for i in range(nv) if vtk_due(m, i, t)]
                 bs = sampling and bunch_sample_due(m, t)
-                if outs or bs:
-                    due.append((s, outs, bs))
+                fs = fsampling and field_sample_due(m, t)
+                if outs or bs or fs:
+                    due.append((s, outs, bs, fs))
                 t += dt
         done = 0
-        for s, outs, bs in due:
+        for s, outs, bs, fs in due:
             c.run(s - done)
-            self._step_with_outputs(outs, bs)
+            self._step_with_outputs(outs, bs, fs)
             done = s + 1
         c.run(n - done)
         rows = c.power_rows()
         if self.write_files:
             self.write_power_files(rows)
             self.write_screen_files()
-            if sampling:
-                path = self.setup.bunch_sample_file()
+            for on, getter, lines in ((sampling, "bunch_sample_file", self._bunch_lines),
+                                      (fsampling, "field_sample_file", self._field_lines)):
+                if not on:
+                    continue
+                path = getattr(self.setup, getter)()
                 d = os.path.dirname(path)
                 if d:
                     os.makedirs(d, exist_ok=True)
                 with open(path, "w") as f:
-                    f.write("".join(self._bunch_lines))
+                    f.write("".join(lines))
         return rows
 
     def _substeps(self):
@@ -877,13 +928,17 @@ class FdTd:
             c.recycle()
             c.advance_time()
 
-    def _step_with_outputs(self, outs, bunch_sample: bool):
+    def _step_with_outputs(self, outs, bunch_sample: bool, field_sample: bool = False):
         c = self.ctx
-        n_time = c.get_time().n_time
+        tm = c.get_time()
+        n_time = tm.n_time
         c.field_update()
         c.save_positions()
         self._substeps()
         c.recycle()
+        if field_sample:
+            self._field_lines.append(format_field_sample(self.meta, tm.time, self._fs_points,
+                                                         c.field_sample(self._fs_points)))
         if outs:
             c.field_evaluate()
             en, bn = c.download_eb()

@@ -239,6 +239,19 @@ int mithra_setup_bunch_sample_file(const mithra_setup* s, char* buf, size_t len,
   return MITHRA_OK;
 }
 
+int mithra_setup_field_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
+  if (!s || !s->s.job.seed.sampling) return MITHRA_ERR_ARG;
+  const auto& f = s->s.job.seed.samp;
+  // Solver::initializeSeedSampling, src/solver.cpp:916-918 (rank 0 of one)
+  const std::string name =
+      ((!f.basename.empty() && f.basename[0] == '/') ? f.basename : f.directory + f.basename) + "-0.txt";
+  if (needed) *needed = name.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < name.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, name.c_str(), name.size() + 1);
+  return MITHRA_OK;
+}
+
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
   if (!s) return MITHRA_ERR_ARG;
   const std::string m = s->s.meta();

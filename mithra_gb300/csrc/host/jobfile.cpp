@@ -385,7 +385,45 @@ void read_field(Cursor& c, Job& J) {
         c.next();
       } while (c.cur() != "}");
       J.seed.vtk.push_back(v);
-    } else if (g == "field-sampling" || g == "field-profile") {
+    } else if (g == "field-sampling") {
+      // src/datainput.cpp:331-366 with Seed::samplingType (src/classes.cpp:871-876)
+      c.open("field-sampling");
+      FieldSampling& f = J.seed.samp;
+      do {
+        const std::string& l = c.cur();
+        const std::string n = name_of(l);
+        auto vec3 = [&](Vec3& v) {
+          const std::vector<double> p = vector_of(l);
+          for (size_t q = 0; q < 3 && q < p.size(); q++) v[q] = p[q];
+        };
+        if (n == "sample") J.seed.sampling = bool_of(l);
+        else if (n == "type") {
+          const std::string t = string_of(l);
+          if (t == "at-point") f.type = ATPOINT;
+          else if (t == "over-line") f.type = OVERLINE;
+          else die(t + " is an unknown sampling type.");
+        } else if (n == "field") {
+          static const char* names[] = {"Ex", "Ey", "Ez", "Bx", "By", "Bz", "Ax", "Ay", "Az", "F"};
+          const std::string t = string_of(l);
+          int code = -1;
+          for (int q = 0; q < 10; q++)
+            if (t == names[q]) code = q;
+          if (code < 0) die(t + " is an unknown sampling field.");
+          f.field.push_back(code);
+        } else if (n == "directory") f.directory = string_of(l);
+        else if (n == "base-name") f.basename = string_of(l);
+        else if (n == "rhythm") f.rhythm = double_of(l);
+        else if (n == "position") {
+          Vec3 v{0, 0, 0};
+          vec3(v);
+          f.position.push_back(v);
+        } else if (n == "line-begin") vec3(f.lineBegin);
+        else if (n == "line-end") vec3(f.lineEnd);
+        else if (n == "number-of-points") f.res = int_of(l);
+        else die(n + " is not defined in seed-sampling group.");
+        c.next();
+      } while (c.cur() != "}");
+    } else if (g == "field-profile") {
       // Diagnostics outside the time-marching path: accepted and validated, not produced.
       const std::string grp = g;
       c.open(grp.c_str());

@@ -97,9 +97,21 @@ struct FieldVtk {
   Vec3 position{0, 0, 0};
 };
 
+// field-sampling group (src/datainput.cpp:331-366): E, B, A at points or along a line.
+struct FieldSampling {
+  SamplingType type = ATPOINT;
+  std::vector<int> field;  // codes as FieldVtk
+  std::string directory, basename;
+  double rhythm = 0.0;
+  std::vector<Vec3> position;
+  Vec3 lineBegin{0, 0, 0}, lineEnd{0, 0, 0};
+  int res = 0;
+};
+
 struct Seed : Beam {  // src/classes.h Seed
   double beta = 0.0, gamma = 1.0, dt = 0.0;
   bool sampling = false, profile = false;
+  FieldSampling samp;
   std::vector<FieldVtk> vtk;
   // Seed::fields (src/classes.cpp:740-855): the vector potential of the seed at a bunch-frame
   // point and time.  `a` is accumulated into for super-Gaussian beams, as in the reference.

@@ -669,6 +669,36 @@ void Setup::initialize() {
   ub_r1 = -EC / (EM * c0) * bunch.timeStep / 2.0;
   ub_r2 = -EC / EM * bunch.timeStep / 2.0;
 
+  // Solver::initializeSeedSampling, src/solver.cpp:848-932: bunch-frame rhythm and positions, the
+  // points of a line, and only points inside the mesh kept.  The range check reads ub_.dx ...
+  // before initializeBunchUpdate sets them; the mesh resolution is used here.
+  if (seed.sampling) {
+    FieldSampling& f = seed.samp;
+    if (f.rhythm == 0) die("The sampling rhythm of the field is zero although sampling is activated !!!");
+    f.rhythm /= gamma;
+    for (auto& p : f.position) p[2] *= gamma;
+    f.lineBegin[2] *= gamma;
+    f.lineEnd[2] *= gamma;
+    if (f.type == OVERLINE) {
+      Vec3 l = f.lineEnd;
+      for (int d = 0; d < 3; d++) l[d] -= f.lineBegin[d];
+      const double n = f.res;
+      for (int d = 0; d < 3; d++) l[d] /= n;
+      for (unsigned i = 0; i < (unsigned)f.res; i++) {
+        Vec3 p;
+        for (int d = 0; d < 3; d++) p[d] = f.lineBegin[d] + i * l[d];
+        f.position.push_back(p);
+      }
+    }
+    std::vector<Vec3> kept;
+    const double* res = mesh.meshResolution.data();
+    for (const auto& p : f.position)
+      if (p[0] < xmax - res[0] && p[0] > xmin + res[0] && p[1] < ymax - res[1] && p[1] > ymin + res[1] &&
+          p[2] < zmax - res[2] && p[2] > zmin + res[2] && p[2] < zp[1] && p[2] >= zp[0])
+        kept.push_back(p);
+    f.position = kept;
+  }
+
   // Solver::initializeSeedVTK, src/solver.cpp:938-1016: the rhythm and the plane position go to
   // the bunch frame, the directory is prefixed to a relative base name, and an in-plane output
   // whose plane lies outside the mesh is dropped.  The reference drops it from the vector it is
@@ -877,6 +907,20 @@ std::string Setup::meta() const {
     for (int i = 0; i < pc.N; i++) kv(p + "z" + std::to_string(i), pc.z[i]);
   }
   kv("time_shift", mesh.timeShift);
+  {
+    const FieldSampling& f = job.seed.samp;
+    kv("fs_sampling", job.seed.sampling ? 1.0 : 0.0);
+    kv("fs_rhythm", f.rhythm);
+    kv("fs_n", job.seed.sampling ? (double)f.position.size() : 0.0);
+    for (size_t i = 0; job.seed.sampling && i < f.position.size(); i++)
+      for (int d = 0; d < 3; d++) kv("fs_p" + std::to_string(i) + "_" + std::to_string(d), f.position[i][d]);
+    kv("fs_nfield", (double)f.field.size());
+    for (size_t l = 0; l < f.field.size(); l++) kv("fs_f" + std::to_string(l), (double)f.field[l]);
+    // unit factors of the file (src/solver.cpp:925-927)
+    kv("fs_Ce", mesh.lengthScale / std::pow(mesh.timeScale, 2));
+    kv("fs_Cb", 1.0 / (mesh.lengthScale * mesh.timeScale));
+    kv("fs_Ca", 1.0 / mesh.timeScale);
+  }
   kv("bunch_sampling", job.bunch.sampling ? 1.0 : 0.0);
   kv("bunch_rhythm", job.bunch.rhythm);
   kv("n_vtk", (double)job.seed.vtk.size());

@@ -14,7 +14,7 @@
  *   run     JOB NSTEPS OUT EVERY    initialise, march NSTEPS field steps, dump every EVERY steps
  *   field   JOB IN OUT              load an/anm1/anp1(=J), FdTd::fieldUpdate, evaluate E/B eagerly
  *   push    JOB IN OUT              load an/anp1/particles/timeBunch, one Solver::bunchUpdate
- *   vtk     JOB N OUT               prelude and N steps with the field visualization where solve()
+ *   vtk     JOB N OUT               prelude and N steps with the field sampling and visualization where solve()
  *                                   calls it (the reference writes its .vts/.pvts files into the
  *                                   job's directory); OUT/steps.bin lists the nTime_ of each step
  *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile (and bunchSample,
@@ -356,6 +356,8 @@ int main(int argc, char** argv) {
         ++s->nTimeBunch_;
       }
       s->recycleParticles();
+      if (s->seed_.sampling_ && fmod(s->time_, s->seed_.samplingRhythm_) < s->mesh_.timeStep_ && s->time_ > 0.0)
+        s->fieldSample();
       for (unsigned int i = 0; i < s->seed_.vtk_.size(); i++) {
         if (s->seed_.vtk_[i].sample_ && fmod(s->time_, s->seed_.vtk_[i].rhythm_) < s->mesh_.timeStep_ && s->time_ > 0.0) {
           if (s->seed_.vtk_[i].type_ == ALLDOMAIN) s->fieldVisualizeAllDomain(i);

@@ -113,6 +113,10 @@ def vtk_fixture(harness, jobname, tag, nsteps=12):
                             text=np.frombuffer(b"".join(texts), dtype=np.uint8),
                             text_sizes=np.array([len(t) for t in texts]),
                             steps=np.fromfile(os.path.join(tmp, "vtk_out", "steps.bin")),
+                            field_sample_text=np.frombuffer(
+                                open(os.path.join(tmp, "field-sampling", "field-0.txt"), "rb").read()
+                                if os.path.exists(os.path.join(tmp, "field-sampling", "field-0.txt")) else b"",
+                                dtype=np.uint8),
                             power_names=np.array(pfiles),
                             power_text=np.frombuffer(b"".join(ptexts), dtype=np.uint8),
                             power_sizes=np.array([len(t) for t in ptexts]))

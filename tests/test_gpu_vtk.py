@@ -42,6 +42,13 @@ def test_solve_writes_reference_vtk(gpu_available, tmp_path, monkeypatch, precis
     A = np.array([[float(x) for x in l.split()] for l in pmine])
     B = np.array([[float(x) for x in l.split()] for l in pref])
     assert np.all(np.abs(A - B) <= max(rtol, 1e-9) * 10 * (np.abs(B).max(axis=0) + 1e-300))
+    # the field-sampling file (over-line points, lab-frame fields)
+    fref = bytes(z["field_sample_text"]).decode().splitlines()
+    fmine = (tmp_path / "field-sampling" / "field-0.txt").read_text().splitlines()
+    assert len(fmine) == len(fref) > 0
+    A = np.array([[float(x) for x in l.split()] for l in fmine])
+    B = np.array([[float(x) for x in l.split()] for l in fref])
+    assert np.all(np.abs(A - B) <= np.maximum(rtol, 1.01e-4) * (np.abs(B).max(axis=0) + 1e-300))
     ref = reference_files()
     mine = {p.name: p.read_text() for p in (tmp_path / "vtk").iterdir()}
     assert sorted(mine) == sorted(ref)

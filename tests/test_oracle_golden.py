@@ -293,3 +293,28 @@ def test_bunch_sample_file_matches_reference():
         r.step()
     assert 0 < len(lines) < len(ref)
     assert lines == ref[len(ref) - len(lines):]
+
+
+def test_field_sample_file_matches_reference():
+    """FdTd::fieldSample rows (over-line points, six components, lab transform and units) byte for
+    byte from the oracle's E, B, A^n and format_field_sample."""
+    import mithra_gb300 as mg
+    from tests.conftest import job
+    m = meta("kat-small-vtk")
+    sm = mg.Setup.from_job(job("kat-small-vtk.job")).meta()
+    pts = mg.field_sample_points(sm)
+    assert pts.shape == (5, 3)
+    init = load("kat-small-vtk", "init")
+    ref = bytes(load("kat-small-vtk", "vtk")["field_sample_text"]).decode().splitlines(keepends=True)
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    lines = []
+
+    def sample(run):
+        if mg.field_sample_due(sm, run.time):
+            lines.append(mg.format_field_sample(sm, run.time, pts, po.field_sample(m, run.an, run.en, run.bn, pts)))
+
+    r.after_recycle = sample
+    for _ in range(12):
+        r.step()
+    assert len(lines) == len(ref) > 0
+    assert lines == ref
