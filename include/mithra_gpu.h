@@ -329,6 +329,10 @@ int mithra_setup_bunch_sample_file(const mithra_setup* s, char* buf, size_t len,
  * frame, inside the mesh), fields, rhythm and unit factors are in the meta text (fs_*); a row is
  * time_ gamma_ and, per point, the position and the lab-frame fields of mithra_gpu_field_sample. */
 int mithra_setup_field_sample_file(const mithra_setup* s, char* buf, size_t len, size_t* needed);
+/* Base name of the bunch-profile dumps (src/solver.cpp:1109); a dump <base>-p0-<nTime>.txt holds
+ * time_ gamma_ and q, rnp, gb of every particle (Solver::bunchProfile, src/solver.cpp:1763-1792),
+ * written by the caller from mithra_gpu_download_particles at the times and rhythm in the meta text. */
+int mithra_setup_bunch_profile_basename(const mithra_setup* s, char* buf, size_t len, size_t* needed);
 
 /* ---- field visualization files ----------------------------------------------------------- */
 

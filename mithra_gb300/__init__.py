@@ -165,6 +165,7 @@ _SIGS = {
     "mithra_setup_screen_basename": [_vp, C.c_int, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_bunch_sample_file": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_field_sample_file": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
+    "mithra_setup_bunch_profile_basename": [_vp, C.c_char_p, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_from_job_device": [C.c_char_p, C.c_int, _P(_vp), C.c_char_p, C.c_size_t],
     "mithra_gpu_upload_particles_device": [_vp, _vp, C.c_size_t],
     "mithra_vtk_write_field": [_vp, C.c_char_p, C.c_longlong, _fp, _fp, _dp, _dp],
@@ -328,6 +329,10 @@ class Setup:
         """File of the field-sampling group (directory prefixed, -0.txt)."""
         return self._file("mithra_setup_field_sample_file", "sample the field")
 
+    def bunch_profile_basename(self) -> str:
+        """Base name of the bunch-profile dumps (directory prefixed)."""
+        return self._file("mithra_setup_bunch_profile_basename", "dump bunch profiles")
+
     def screen_basename(self, jf: int) -> str:
         """Base name of the screens of FEL-OUTPUT entry jf (directory prefixed)."""
         return self._string("mithra_setup_screen_basename", jf)
@@ -447,6 +452,33 @@ def format_field_sample(meta: dict, time: float, points, samples) -> str:
             else: continue  # FdTd writes nothing for the scalar potential
             out.append("%.4e" % x)
     return "\t".join(out) + "\t\n"
+
+
+def bunch_profile_due(meta: dict, time: float) -> int:
+    """How many times Solver::solve writes a bunch profile at field time `time`
+    (src/solver.cpp:1258-1266, :1362-1370): once per listed time just passed, once on the rhythm."""
+    if not meta.get("bunch_profile", 0):
+        return 0
+    n, dt = 0, meta["dt"]
+    for i in range(int(meta.get("bunch_profile_ntime", 0))):
+        t = meta["bunch_profile_t%d" % i]
+        if time - t < dt and time > t:
+            n += 1
+    r, ts = meta["bunch_profile_rhythm"], time + meta["time_shift"]
+    if r != 0.0 and float(np.fmod(ts, r)) < dt and ts > 0.0:
+        n += 1
+    return n
+
+
+def format_bunch_profile(time_lab: float, rec) -> str:
+    """A bunch-profile dump (Solver::bunchProfile, src/solver.cpp:1763-1792): time_ gamma_ on the
+    first line (width 40), then q, rnp, gb of every particle, %.15e, tab-separated.  rec: particle
+    records (q, rnp, rnm, gb, e) in list order."""
+    rec = np.asarray(rec, dtype=np.float64).reshape(-1, 11)
+    out = [("%.15e" % time_lab).rjust(40) + "\n"]
+    cols = rec[:, [0, 1, 2, 3, 7, 8, 9]]
+    out += ["\t".join("%.15e" % v for v in row) + "\n" for row in cols]
+    return "".join(out)
 
 
 def bunch_sample_due(meta: dict, time: float) -> bool:
@@ -857,7 +889,7 @@ class FdTd:
         captured step graph."""
         m = self.meta
         c = self.ctx
-        sampling = self.write_files and bool(m.get("bunch_sampling", 0))
+        sampling = self.write_files and (bool(m.get("bunch_sampling", 0)) or bool(m.get("bunch_profile", 0)))
         fsampling = self.write_files and int(m.get("fs_n", 0)) > 0
         self._bunch_lines = []
         self._field_lines = []
@@ -875,7 +907,7 @@ class FdTd:
             t, dt = c.get_time().time, m["dt"]
             for s in range(n):
                 outs = [i for i in range(nv) if vtk_due(m, i, t)]
-                bs = sampling and bunch_sample_due(m, t)
+                bs = sampling and (bunch_sample_due(m, t) or bunch_profile_due(m, t) > 0)
                 fs = fsampling and field_sample_due(m, t)
                 if outs or bs or fs:
                     due.append((s, outs, bs, fs))
@@ -890,7 +922,7 @@ class FdTd:
         if self.write_files:
             self.write_power_files(rows)
             self.write_screen_files()
-            for on, getter, lines in ((sampling, "bunch_sample_file", self._bunch_lines),
+            for on, getter, lines in ((bool(m.get("bunch_sampling", 0)), "bunch_sample_file", self._bunch_lines),
                                       (fsampling, "field_sample_file", self._field_lines)):
                 if not on:
                     continue
@@ -923,10 +955,22 @@ class FdTd:
             self._substeps()
             if getattr(c, "n_screens", 0):
                 c.call("mithra_gpu_screen_profile")
-            if bunch_sample_due(self.meta, t.time):
-                self._bunch_lines.append(format_bunch_sample(c.bunch_sample()))
+            self._bunch_outputs(t)
             c.recycle()
             c.advance_time()
+
+    def _bunch_outputs(self, t):
+        """bunchSample and bunchProfile where Solver::solve calls them (t: the step's time state)."""
+        m, c = self.meta, self.ctx
+        if self.write_files and m.get("bunch_sampling", 0) and bunch_sample_due(m, t.time):
+            self._bunch_lines.append(format_bunch_sample(c.bunch_sample()))
+        if self.write_files and bunch_profile_due(m, t.time):
+            base = self.setup.bunch_profile_basename()
+            d = os.path.dirname(base)
+            if d:
+                os.makedirs(d, exist_ok=True)
+            with open("%s-p0-%d.txt" % (base, t.n_time), "w") as f:
+                f.write(format_bunch_profile(t.time * m["gamma"], c.download_particles()))
 
     def _step_with_outputs(self, outs, bunch_sample: bool, field_sample: bool = False):
         c = self.ctx
@@ -947,7 +991,7 @@ class FdTd:
             for i in outs:
                 write_field_vtk(self.meta, i, self.setup.vtk_basename(i), n_time, en, bn, an, fn)
         if bunch_sample:
-            self._bunch_lines.append(format_bunch_sample(c.bunch_sample()))
+            self._bunch_outputs(tm)
         if getattr(c, "n_screens", 0):
             c.call("mithra_gpu_screen_profile")
         c.power_sample()

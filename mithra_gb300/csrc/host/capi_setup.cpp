@@ -252,6 +252,19 @@ int mithra_setup_field_sample_file(const mithra_setup* s, char* buf, size_t len,
   return MITHRA_OK;
 }
 
+int mithra_setup_bunch_profile_basename(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
+  if (!s || !s->s.job.bunch.profile) return MITHRA_ERR_ARG;
+  const auto& b = s->s.job.bunch;
+  // Solver::initializeBunchUpdate, src/solver.cpp:1109
+  const std::string f = (!b.profileBasename.empty() && b.profileBasename[0] == '/') ? b.profileBasename
+                                                                                  : b.profileDirectory + b.profileBasename;
+  if (needed) *needed = f.size() + 1;
+  if (!buf) return MITHRA_OK;
+  if (len < f.size() + 1) return MITHRA_ERR_ARG;
+  memcpy(buf, f.c_str(), f.size() + 1);
+  return MITHRA_OK;
+}
+
 int mithra_setup_meta(const mithra_setup* s, char* buf, size_t len, size_t* needed) {
   if (!s) return MITHRA_ERR_ARG;
   const std::string m = s->s.meta();

@@ -317,6 +317,8 @@ void read_bunch(Cursor& c, Job& J) {
           else J.bunch.profile = v;
         } else if (n == "directory" || n == "base-name") {
           if (grp == "bunch-sampling") (n == "directory" ? J.bunch.directory : J.bunch.basename) = string_of(l);
+          if (grp == "bunch-profile")
+            (n == "directory" ? J.bunch.profileDirectory : J.bunch.profileBasename) = string_of(l);
         } else if (n == "rhythm") {
           double v = double_of(l);
           if (grp == "bunch-sampling") J.bunch.rhythm = v;

@@ -62,11 +62,12 @@ struct BunchInit {  // src/database.h:19-100, defaults src/database.cpp:15-36
 struct Bunch {
   std::vector<BunchInit> inits;
   double timeStep = 0.0;
-  // bunch-sampling (written by FdTd.solve); bunch-visualization and bunch-profile are parsed for
+  // bunch-sampling and bunch-profile (written by FdTd.solve); bunch-visualization is parsed for
   // compatibility and not produced.
   bool sampling = false, vtk = false, profile = false;
   double rhythm = 0.0, vtkRhythm = 0.0, profileRhythm = 0.0;
   std::string directory, basename;  // bunch-sampling file
+  std::string profileDirectory, profileBasename;  // bunch-profile files
   std::vector<double> profileTime;
   double zu = 0.0, beta = 0.0;
 };

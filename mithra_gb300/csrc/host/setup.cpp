@@ -512,7 +512,12 @@ void Setup::initialize() {
 
   // Solver::lorentzBoostBunch, src/solver.cpp:263-423.
   bunch.timeStep /= gamma;
-  bunch.rhythm /= gamma;  // src/solver.cpp:281
+  bunch.rhythm /= gamma;  // src/solver.cpp:281-285
+  bunch.vtkRhythm /= gamma;
+  for (auto& t : bunch.profileTime) t /= gamma;
+  bunch.profileRhythm /= gamma;
+  if (bunch.profile && bunch.profileRhythm == 0 && bunch.profileTime.empty())
+    die("The profiling rhythm of the bunch is zero and no time is set although profiling of the bunch is activated !!!");
   if (bunch.sampling && bunch.rhythm == 0)
     die("The sampling rhythm of the bunch is zero although sampling is activated !!!");
   if (bunch.timeStep == 0) bunch.timeStep = mesh.timeStep;
@@ -921,6 +926,10 @@ std::string Setup::meta() const {
     kv("fs_Cb", 1.0 / (mesh.lengthScale * mesh.timeScale));
     kv("fs_Ca", 1.0 / mesh.timeScale);
   }
+  kv("bunch_profile", job.bunch.profile ? 1.0 : 0.0);
+  kv("bunch_profile_rhythm", job.bunch.profileRhythm);
+  kv("bunch_profile_ntime", (double)job.bunch.profileTime.size());
+  for (size_t i = 0; i < job.bunch.profileTime.size(); i++) kv("bunch_profile_t" + std::to_string(i), job.bunch.profileTime[i]);
   kv("bunch_sampling", job.bunch.sampling ? 1.0 : 0.0);
   kv("bunch_rhythm", job.bunch.rhythm);
   kv("n_vtk", (double)job.seed.vtk.size());

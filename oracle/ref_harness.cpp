@@ -18,7 +18,7 @@
  *                                   calls it (the reference writes its .vts/.pvts files into the
  *                                   job's directory); OUT/steps.bin lists the nTime_ of each step
  *   screen  JOB N OUT               prelude and N steps with Solver::screenProfile (and bunchSample,
- *                                   when the job samples the bunch) where solve()
+ *                                   bunchProfile, when the job asks for them) where solve()
  *                                   calls it; the reference writes its own screen files into the
  *                                   job's directory, OUT/offsets.bin holds each screen file's size
  *                                   after the prelude and after every step
@@ -394,6 +394,14 @@ int main(int argc, char** argv) {
       if (s->bunch_.sampling_ && fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.rhythm_) < s->mesh_.timeStep_ &&
           (s->time_ + s->mesh_.timeShift_ > 0.0))
         s->bunchSample();
+      if (s->bunch_.bunchProfile_) {
+        for (unsigned int i = 0; i < s->bunch_.bunchProfileTime_.size(); i++)
+          if (s->time_ - s->bunch_.bunchProfileTime_[i] < s->mesh_.timeStep_ && s->time_ > s->bunch_.bunchProfileTime_[i])
+            s->bunchProfile();
+        if (fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.bunchProfileRhythm_) < s->mesh_.timeStep_ &&
+            (s->time_ + s->mesh_.timeShift_ > 0.0) && (s->bunch_.bunchProfileRhythm_ != 0.0))
+          s->bunchProfile();
+      }
       s->recycleParticles();
       s->timem1_ += s->mesh_.timeStep_;
       s->time_ += s->mesh_.timeStep_;
@@ -413,6 +421,14 @@ int main(int argc, char** argv) {
       if (s->bunch_.sampling_ && fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.rhythm_) < s->mesh_.timeStep_ &&
           (s->time_ + s->mesh_.timeShift_ > 0.0))
         s->bunchSample();
+      if (s->bunch_.bunchProfile_) {
+        for (unsigned int i = 0; i < s->bunch_.bunchProfileTime_.size(); i++)
+          if (s->time_ - s->bunch_.bunchProfileTime_[i] < s->mesh_.timeStep_ && s->time_ > s->bunch_.bunchProfileTime_[i])
+            s->bunchProfile();
+        if (fmod(s->time_ + s->mesh_.timeShift_, s->bunch_.bunchProfileRhythm_) < s->mesh_.timeStep_ &&
+            (s->time_ + s->mesh_.timeShift_ > 0.0) && (s->bunch_.bunchProfileRhythm_ != 0.0))
+          s->bunchProfile();
+      }
       s->screenProfile();
       s->powerSample();
       s->fieldShift();

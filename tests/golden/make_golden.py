@@ -84,10 +84,15 @@ def screen_fixture(harness, jobname, tag, nsteps=12):
                     screen.append(i)
                     step.append(n)
                 start = end
+        pdir = os.path.join(tmp, "bunch-profile")
+        pnames = sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []
+        ptexts = [open(os.path.join(pdir, f), "rb").read() for f in pnames]
         bfile = os.path.join(tmp, "bunch-sampling", "bunch.txt")
         btext = open(bfile, "rb").read() if os.path.exists(bfile) else b""
         np.savez_compressed(os.path.join(dst, "screen.npz"), names=np.array(files), offsets=offsets,
                             bunch_text=np.frombuffer(btext, dtype=np.uint8),
+                            profile_names=np.array(pnames), profile_sizes=np.array([len(t) for t in ptexts]),
+                            profile_text=np.frombuffer(b"".join(ptexts), dtype=np.uint8),
                             text=np.frombuffer(b"".join(texts), dtype=np.uint8),
                             text_sizes=np.array([len(t) for t in texts]),
                             rows=np.array(rows).reshape(-1, 6), screen=np.array(screen), step=np.array(step))

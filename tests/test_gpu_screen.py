@@ -116,6 +116,17 @@ def test_solve_writes_screen_and_bunch_sample_files(tmp_path, monkeypatch):
     A = np.array([[float(x) for x in l.split()] for l in bmine])
     B = np.array([[float(x) for x in l.split()] for l in bref])
     assert np.all(np.abs(A - B) <= 2e-4 * np.abs(B) + 1e-12 * np.abs(B).max(axis=0))
+    # bunch-profile dumps (prelude and field steps): same files, same particles, values to 1e-11
+    start = 0
+    for name, size in zip(z["profile_names"], z["profile_sizes"]):
+        ref = bytes(z["profile_text"][start:start + size]).decode().splitlines()
+        start += size
+        mine = (tmp_path / "bunch-profile" / str(name)).read_text().splitlines()
+        assert len(mine) == len(ref) and len(mine[0]) == 40
+        A = np.array([[float(x) for x in l.split()] for l in mine[1:]])
+        B = np.array([[float(x) for x in l.split()] for l in ref[1:]])
+        assert float(mine[0]) == pytest.approx(float(ref[0]), rel=1e-13)
+        assert np.all(np.abs(A - B) <= 1e-11 * (np.abs(B).max(axis=0) + 1e-300))
     for name, ref in zip(z["names"], texts):
         mine = (tmp_path / "screen" / str(name)).read_text().splitlines()
         b = ref.splitlines()

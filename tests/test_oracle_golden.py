@@ -318,3 +318,31 @@ def test_field_sample_file_matches_reference():
         r.step()
     assert len(lines) == len(ref) > 0
     assert lines == ref
+
+
+def test_bunch_profile_dumps_match_reference():
+    """Solver::bunchProfile dumps written during the field steps (listed time and rhythm) byte for
+    byte from the oracle's particles and format_bunch_profile."""
+    import mithra_gb300 as mg
+    from tests.conftest import job
+    m = meta("kat-small-screen")
+    sm = mg.Setup.from_job(job("kat-small-screen.job")).meta()
+    init = load("kat-small-screen", "init")
+    z = load("kat-small-screen", "screen")
+    ref, start = {}, 0
+    for name, size in zip(z["profile_names"], z["profile_sizes"]):
+        ref[str(name)] = bytes(z["profile_text"][start:start + size]).decode()
+        start += size
+    r = po.OracleRun(m, init["an"], init["anm1"], init["anp1"], init["particles"], solver=0, order=2)
+    mine = {}
+
+    def dump(run):
+        if mg.bunch_profile_due(sm, run.time):
+            mine["prof-p0-%d.txt" % run.n_time] = mg.format_bunch_profile(run.time * m["gamma"], run.particles)
+
+    r.after_recycle = dump
+    for _ in range(12):
+        r.step()
+    assert len(mine) >= 2 and set(mine) <= set(ref)
+    for name, text in mine.items():
+        assert text == ref[name], name
