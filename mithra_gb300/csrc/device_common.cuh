@@ -104,6 +104,21 @@ struct StateDev {
   long long next_id;         // mixed form: id given to the next z-face copy
 };
 
+// Min/max of particle cells along z, reduced per warp and folded into the state with atomics.
+// Every warp of a deposit reaches this with a range, and atomics on the two words serialise in
+// one L2 slice, so a warp reads the words first and issues an atomic only when its range extends
+// them; a stale read costs an extra atomic, never a wrong range.
+__device__ __forceinline__ void slab_update(StateDev* st, int kmin, int kmax) {
+  for (int o = 16; o > 0; o >>= 1) {
+    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
+    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
+  }
+  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
+    if (kmin < *reinterpret_cast<volatile int*>(&st->k_lo_next)) atomicMin(&st->k_lo_next, kmin);
+    if (kmax > *reinterpret_cast<volatile int*>(&st->k_hi_next)) atomicMax(&st->k_hi_next, kmax);
+  }
+}
+
 template <typename T>
 struct ParticlesDev {
   T *x, *y, *z;        // rnp

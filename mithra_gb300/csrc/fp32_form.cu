@@ -333,7 +333,7 @@ int fp32_current(mithra_ctx* ctx) {
   if (r) return r;
   fp32_after_step(ctx);  // the sorted set becomes current
   return timed(ctx, "deposit", [&] {
-    k_deposit_tiled<<<T.n_bins - 1, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
+    k_deposit_tiled<<<T.n_tiles + kOutsideBlocks, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
         D, T, f.pt, f.offsets, ctx->st, J, rho, g.cstride, g.plane, g.P1);
   });
 }

@@ -481,14 +481,7 @@ __global__ void __launch_bounds__(256) k_deposit_f32(DepositF32 D, ParticlesF32 
       deposit_half_f32(J, cs, m, sI, sK, qh, ax, ay, az, (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
-    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
-  }
-  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
-    atomicMin(&st->k_lo_next, kmin);
-    atomicMax(&st->k_hi_next, kmax);
-  }
+  slab_update(st, kmin, kmax);
 }
 
 // Records (11 doubles) <-> mixed-form particles.  Cell = floor((x - xmin)/dx) in FP64.

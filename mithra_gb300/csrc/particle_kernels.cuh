@@ -271,18 +271,6 @@ __device__ __forceinline__ void deposit_half_edges(double* Je, long long cs, lon
   atomicAdd(Jz + m + sI + 1, qz * (x2 * y2));
 }
 
-// Min/max of particle cells along z, reduced per warp and folded into the state with atomics.
-__device__ __forceinline__ void slab_update(StateDev* st, int kmin, int kmax) {
-  for (int o = 16; o > 0; o >>= 1) {
-    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
-    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
-  }
-  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
-    atomicMin(&st->k_lo_next, kmin);
-    atomicMax(&st->k_hi_next, kmax);
-  }
-}
-
 // J: the edge-form current buffer (zeroed by the caller); rho: node charge, or null.
 __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<double> pt, StateDev* st,
                                                       double* J, double* rho) {

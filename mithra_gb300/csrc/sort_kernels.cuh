@@ -227,16 +227,84 @@ __device__ __forceinline__ void tile_half(float* sJ, float* J, long long cs, lon
   }
 }
 
-constexpr int kDepositBlock = 128;
+// The cell's nodes (cell .. cell + 1 along each axis) lie in the tile's shared copy.
+__device__ __forceinline__ bool cell_in_tile(int i0, int j0, int k0, int ic, int jc, int kc) {
+  const int li = ic - i0, lj = jc - j0, lk = kc - k0;
+  return li >= 0 && lj >= 0 && lk >= 0 && li + 1 < HX && lj + 1 < HY && lk + 1 < HZ;
+}
 
-__global__ void __launch_bounds__(kDepositBlock, 7) k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets,
-                                                       StateDev* st, float* J, float* rho, long long cs,
-                                                       long long plane, int P1) {
+// Both half segments of a particle that stayed in one cell (the common case in the boosted frame,
+// where a particle moves a small fraction of a cell per step): the two halves weight the same
+// twelve edges, so their sums are formed in registers and added with 12 shared atomics, not 24.
+__device__ __forceinline__ void tile_both(float* sJ, int i0, int j0, int k0, int ic, int jc, int kc, float qh,
+                                          float axp, float ayp, float azp, float jxp, float jyp, float jzp,
+                                          float axm, float aym, float azm, float jxm, float jym, float jzm) {
+  const int li = ic - i0, lj = jc - j0, lk = kc - k0;
+  const float x1p = 1.0f - axp, y1p = 1.0f - ayp, z1p = 1.0f - azp;
+  const float x1m = 1.0f - axm, y1m = 1.0f - aym, z1m = 1.0f - azm;
+  constexpr int SI = HY, SK = HX * HY;
+  const int s = (lk * HX + li) * HY + lj;
+  // the four edges of one component: the sum over both halves of q j u v, where u and v are the
+  // linear weights along the two other axes (u1 = 1 - a, u2 = a at the half's midpoint a)
+  auto four = [&](float* e, int s1, int s2, float qp, float qm, float u1p, float u2p, float u1m, float u2m,
+                  float v1p, float v2p, float v1m, float v2m) {
+    const float a = qp * v1p, b = qp * v2p, c = qm * v1m, d = qm * v2m;
+    atomicAdd(e + s, a * u1p + c * u1m);
+    atomicAdd(e + s + s1, a * u2p + c * u2m);
+    atomicAdd(e + s + s2, b * u1p + d * u1m);
+    atomicAdd(e + s + s1 + s2, b * u2p + d * u2m);
+  };
+  four(sJ, 1, SK, qh * jxp, qh * jxm, y1p, ayp, y1m, aym, z1p, azp, z1m, azm);
+  four(sJ + TILE_NODES, SI, SK, qh * jyp, qh * jym, x1p, axp, x1m, axm, z1p, azp, z1m, azm);
+  four(sJ + 2 * TILE_NODES, SI, 1, qh * jzp, qh * jzm, x1p, axp, x1m, axm, y1p, ayp, y1m, aym);
+}
+
+// Both halves of a one-cell particle straight to J in node form (24 atomics instead of 48).
+__device__ __forceinline__ void global_both(float* J, long long cs, long long m, long long sI, long long sK,
+                                            float qh, float axp, float ayp, float azp, float jxp, float jyp,
+                                            float jzp, float axm, float aym, float azm, float jxm, float jym,
+                                            float jzm) {
+  const float x1p = 1.0f - axp, y1p = 1.0f - ayp, z1p = 1.0f - azp;
+  const float x1m = 1.0f - axm, y1m = 1.0f - aym, z1m = 1.0f - azm;
+  // one component: edge values w(u, v) at the four (u, v) corners, each added at both ends (s0)
+  auto four = [&](float* e, long long s0, long long s1, long long s2, float qp, float qm, float u1p, float u2p,
+                  float u1m, float u2m, float v1p, float v2p, float v1m, float v2m) {
+    const float a = qp * v1p, b = qp * v2p, c = qm * v1m, d = qm * v2m;
+    const float w00 = a * u1p + c * u1m, w10 = a * u2p + c * u2m, w01 = b * u1p + d * u1m, w11 = b * u2p + d * u2m;
+    atomicAdd(e + m, w00);
+    atomicAdd(e + m + s0, w00);
+    atomicAdd(e + m + s1, w10);
+    atomicAdd(e + m + s1 + s0, w10);
+    atomicAdd(e + m + s2, w01);
+    atomicAdd(e + m + s2 + s0, w01);
+    atomicAdd(e + m + s1 + s2, w11);
+    atomicAdd(e + m + s1 + s2 + s0, w11);
+  };
+  four(J, sI, 1, sK, qh * jxp, qh * jxm, y1p, ayp, y1m, aym, z1p, azp, z1m, azm);
+  four(J + cs, 1, sI, sK, qh * jyp, qh * jym, x1p, axp, x1m, axm, z1p, azp, z1m, azm);
+  four(J + 2 * cs, sK, sI, 1, qh * jzp, qh * jzm, x1p, axp, x1m, axm, y1p, ayp, y1m, aym);
+}
+
+constexpr int kDepositBlock = 128;
+constexpr int kOutsideBlocks = 304;  // blocks for the particles outside the tiles (2 per SM)
+// Tiles with fewer particles than this skip the shared copy (zeroing and flushing its 1452 chunks
+// costs more than the particles' global atomics).
+constexpr int kSparseTile = 32;
+
+__global__ void __launch_bounds__(kDepositBlock, 6)
+    k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets, StateDev* st, float* J,
+                    float* rho, long long cs, long long plane, int P1) {
   extern __shared__ float sJ[];  // 3 * TILE_NODES
   const int b = blockIdx.x;
-  const int beg = offsets[b], end = offsets[b + 1];
-  if (beg == end) return;
-  const bool tiled = b < T.n_tiles;
+  const bool tile_block = b < T.n_tiles;
+  // Blocks past the tiles share the bin of particles outside the tiled cells (one block for that
+  // bin would serialise its particles, which can number 10^5): block n_tiles + r takes the
+  // particles r * kDepositBlock + t, stepping by kOutsideBlocks * kDepositBlock.
+  const int bin = tile_block ? b : T.bin_outside;
+  const int stride = tile_block ? kDepositBlock : kOutsideBlocks * kDepositBlock;
+  const int beg = offsets[bin] + (tile_block ? 0 : (b - T.n_tiles) * kDepositBlock), end = offsets[bin + 1];
+  if (beg >= end) return;
+  const bool tiled = tile_block && end - beg >= kSparseTile;
   int i0 = 0, j0 = 0, k0 = 0;
   if (tiled) {
     const int ti = b % T.ntx, tj = (b / T.ntx) % T.nty, tk = b / (T.ntx * T.nty);
@@ -264,9 +332,9 @@ __global__ void __launch_bounds__(kDepositBlock, 7) k_deposit_tiled(DepositF32 D
   int p = beg + threadIdx.x;
   Loaded cur{};
   if (p < end) cur = load(p);
-  for (; p < end; p += kDepositBlock) {
+  for (; p < end; p += stride) {
     Loaded nxt{};
-    if (p + kDepositBlock < end) nxt = load(p + kDepositBlock);
+    if (p + stride < end) nxt = load(p + stride);
     int ip, jp, kp, im, jm, km;
     unpack_cell(cur.cell, ip, jp, kp);
     unpack_cell(cur.mcell, im, jm, km);
@@ -283,78 +351,103 @@ __global__ void __launch_bounds__(kDepositBlock, 7) k_deposit_tiled(DepositF32 D
       const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
       const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
       const float qh = 0.5f * cur.q;
-      float* sj = tiled ? sJ : nullptr;
-      if (bp) {
-        const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
-                    az = 0.5f * (rzp + rz) - (float)(kp - bz);
-        if (sj)
-          tile_half(sj, J, cs, plane, P1, i0, j0, k0, ip, jp, kp, qh, ax, ay, az, (rxp - rx) * D.dx,
-                    (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+      const bool one_cell = bp && bm && ip == im && jp == jm && kp == km;
+      if (one_cell) {  // base = the cell itself: both halves in one pass
+        const float axp = 0.5f * (rxp + rx), ayp = 0.5f * (ryp + ry), azp = 0.5f * (rzp + rz);
+        const float axm = 0.5f * (rxm + rx), aym = 0.5f * (rym + ry), azm = 0.5f * (rzm + rz);
+        const float jxp = (rxp - rx) * D.dx, jyp = (ryp - ry) * D.dy, jzp = (rzp - rz) * D.dz;
+        const float jxm = (rx - rxm) * D.dx, jym = (ry - rym) * D.dy, jzm = (rz - rzm) * D.dz;
+        if (tiled && cell_in_tile(i0, j0, k0, ip, jp, kp))
+          tile_both(sJ, i0, j0, k0, ip, jp, kp, qh, axp, ayp, azp, jxp, jyp, jzp, axm, aym, azm, jxm, jym, jzm);
         else
-          deposit_half_f32(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, ax, ay, az,
-                           (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
-        if (rho) {
-          const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
-          const float q = cur.q;
-          const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
-          atomicAdd(rho + m, q * x1 * y1 * z1);
-          atomicAdd(rho + m + sI, q * fxp * y1 * z1);
-          atomicAdd(rho + m + 1, q * x1 * fyp * z1);
-          atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
-          atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
-          atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
-          atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
-          atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
+          global_both(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, axp, ayp, azp, jxp, jyp,
+                      jzp, axm, aym, azm, jxm, jym, jzm);
+      } else {
+        if (bp) {
+          const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
+                      az = 0.5f * (rzp + rz) - (float)(kp - bz);
+          if (tiled)
+            tile_half(sJ, J, cs, plane, P1, i0, j0, k0, ip, jp, kp, qh, ax, ay, az, (rxp - rx) * D.dx,
+                      (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+          else
+            deposit_half_f32(J, cs, (long long)kp * plane + (long long)ip * P1 + jp, sI, sK, qh, ax, ay, az,
+                             (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
+        }
+        if (bm) {
+          const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
+                      az = 0.5f * (rzm + rz) - (float)(km - bz);
+          if (tiled)
+            tile_half(sJ, J, cs, plane, P1, i0, j0, k0, im, jm, km, qh, ax, ay, az, (rx - rxm) * D.dx,
+                      (ry - rym) * D.dy, (rz - rzm) * D.dz);
+          else
+            deposit_half_f32(J, cs, (long long)km * plane + (long long)im * P1 + jm, sI, sK, qh, ax, ay, az,
+                             (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
         }
       }
-      if (bm) {
-        const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
-                    az = 0.5f * (rzm + rz) - (float)(km - bz);
-        if (sj)
-          tile_half(sj, J, cs, plane, P1, i0, j0, k0, im, jm, km, qh, ax, ay, az, (rx - rxm) * D.dx,
-                    (ry - rym) * D.dy, (rz - rzm) * D.dz);
-        else
-          deposit_half_f32(J, cs, (long long)km * plane + (long long)im * P1 + jm, sI, sK, qh, ax, ay, az,
-                           (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
+      if (bp && rho) {
+        const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
+        const float q = cur.q;
+        const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
+        atomicAdd(rho + m, q * x1 * y1 * z1);
+        atomicAdd(rho + m + sI, q * fxp * y1 * z1);
+        atomicAdd(rho + m + 1, q * x1 * fyp * z1);
+        atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
+        atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
+        atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
+        atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
+        atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
       }
     }
     cur = nxt;
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    kmin = min(kmin, __shfl_down_sync(0xffffffffu, kmin, o));
-    kmax = max(kmax, __shfl_down_sync(0xffffffffu, kmax, o));
-  }
-  if ((threadIdx.x & 31) == 0 && kmin <= kmax) {
-    atomicMin(&st->k_lo_next, kmin);
-    atomicMax(&st->k_hi_next, kmax);
-  }
+  slab_update(st, kmin, kmax);
   if (!tiled) return;
   __syncthreads();
   // Flush: the node values of every chunk of four nodes along j, node(n) = edge(n) + edge(n - unit
-  // step along the component), are added to J with one vector atomic; consecutive threads take
-  // consecutive chunks of a row.  A chunk lies wholly inside or wholly outside a padded row of J
-  // (both are aligned to four nodes), and only non-zero chunks, which hold nodes of real cells,
-  // are added.
-  const float4* s4 = reinterpret_cast<const float4*>(sJ);
-  constexpr int CH = HY / 4, CHUNKS = TILE_NODES / 4;
-  for (int s = threadIdx.x; s < 3 * CHUNKS; s += blockDim.x) {
-    const int c = s / CHUNKS, r = s % CHUNKS;
-    const int q = r % CH, li = (r / CH) % HX, lk = r / (CH * HX);
+  // step along the component), are added to J with one vector atomic.  A component holds
+  // HX * HZ rows of CH chunks; thread t takes the chunks t + u * kDepositBlock (u < 4) of every
+  // component, so their positions and bounds are worked out once.  A chunk lies wholly inside or
+  // wholly outside a padded row of J (both are aligned to four nodes), and only non-zero chunks,
+  // which hold nodes of real cells, are added.
+  constexpr int CH = HY / 4, ITEMS = HX * HZ * CH, U = 4;
+  static_assert(ITEMS <= U * kDepositBlock, "flush items per thread");
+  long long goff[U];
+  int flags[U];  // bit 0: chunk in the mesh, bit 1: li > 0, bit 2: lk > 0, bit 3: q > 0
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    const int item = threadIdx.x + u * kDepositBlock;
+    const int q = item % CH, row = item / CH, li = row % HX, lk = row / HX;
     const int gi = i0 + li, gj = j0 + 4 * q, gk = k0 + lk;
-    if (gi < 0 || gj < 0 || gk < 0 || gi >= D.N0 || gj >= P1 || gk >= D.N2) continue;
-    float4 v = s4[s];
-    if (c == 0) {
-      if (li > 0) { const float4 w = s4[s - CH]; v.x += w.x; v.y += w.y; v.z += w.z; v.w += w.w; }
-    } else if (c == 1) {
-      const float* e = sJ + 4 * s;  // 4 * s is the flat index of the chunk's first node
-      v.w += e[2]; v.z += e[1]; v.y += e[0];
-      if (q > 0) v.x += e[-1];
-    } else {
-      if (lk > 0) { const float4 w = s4[s - CH * HX]; v.x += w.x; v.y += w.y; v.z += w.z; v.w += w.w; }
+    const bool ok = item < ITEMS && gi >= 0 && gj >= 0 && gk >= 0 && gi < D.N0 && gj < P1 && gk < D.N2;
+    flags[u] = (ok ? 1 : 0) | (li > 0 ? 2 : 0) | (lk > 0 ? 4 : 0) | (q > 0 ? 8 : 0);
+    goff[u] = (long long)gk * plane + (long long)gi * P1 + gj;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    const float* e = sJ + c * TILE_NODES;
+    const float4* e4 = reinterpret_cast<const float4*>(e);
+    float4 v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int item = threadIdx.x + u * kDepositBlock;
+      v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!(flags[u] & 1)) continue;
+      v[u] = e4[item];
+      if (c == 0) {
+        if (flags[u] & 2) { const float4 w = e4[item - CH]; v[u].x += w.x; v[u].y += w.y; v[u].z += w.z; v[u].w += w.w; }
+      } else if (c == 1) {
+        const float* n = e + 4 * item;  // the chunk's first node
+        v[u].w += n[2]; v[u].z += n[1]; v[u].y += n[0];
+        if (flags[u] & 8) v[u].x += n[-1];
+      } else {
+        if (flags[u] & 4) { const float4 w = e4[item - CH * HX]; v[u].x += w.x; v[u].y += w.y; v[u].z += w.z; v[u].w += w.w; }
+      }
     }
-    if (v.x == 0.0f && v.y == 0.0f && v.z == 0.0f && v.w == 0.0f) continue;
-    const long long m = (long long)c * cs + (long long)gk * plane + (long long)gi * P1 + gj;
-    atomicAdd(reinterpret_cast<float4*>(J + m), v);
+    float* Jc = J + c * cs;
+#pragma unroll
+    for (int u = 0; u < U; u++)
+      if (v[u].x != 0.0f || v[u].y != 0.0f || v[u].z != 0.0f || v[u].w != 0.0f)
+        atomicAdd(reinterpret_cast<float4*>(Jc + goff[u]), v[u]);
   }
 }
 
