@@ -289,7 +289,7 @@ constexpr int kDepositBlock = 128;
 constexpr int kOutsideBlocks = 304;  // blocks for the particles outside the tiles (2 per SM)
 // Tiles with fewer particles than this skip the shared copy (zeroing and flushing its 1452 chunks
 // costs more than the particles' global atomics).
-constexpr int kSparseTile = 32;
+constexpr int kSparseTile = 64;
 
 __global__ void __launch_bounds__(kDepositBlock, 6)
     k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets, StateDev* st, float* J,
