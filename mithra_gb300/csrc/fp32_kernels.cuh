@@ -183,7 +183,7 @@ __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, co
 // BEAMS: the job defines optical undulators or external fields (a separate instantiation keeps
 // the FP64 laser-beam code, and its registers, out of the common kernel).
 template <bool BEAMS>
-__global__ void __launch_bounds__(256, BEAMS ? 1 : 3) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
+__global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
                                                   const UndTableEntry* __restrict__ table, ParticlesF32 pt,
                                                   const float* __restrict__ E, const float* __restrict__ B,
                                                   long long cstride, long long plane, int P1, StateDev* st,
