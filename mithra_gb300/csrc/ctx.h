@@ -14,7 +14,7 @@ namespace mithra {
 struct PowerOut {
   PowerDev dev{};
   double *z = nullptr, *dzr = nullptr, *tw_re = nullptr, *tw_im = nullptr, *fdt = nullptr,
-         *partial = nullptr, *rows = nullptr;
+         *partial = nullptr, *rows = nullptr, *run = nullptr;
   int *plane_k = nullptr, *plane_slot = nullptr;
 };
 

@@ -169,6 +169,7 @@ struct PowerDev {
   const double* tw_re;      // Nl*Nf twiddles cos(w_l j dt)
   const double* tw_im;      // Nl*Nf twiddles sin(w_l j dt)
   double* fdt;              // ring buffer: Nf slots x 4 values x nz planes x nodes
+  double* run;              // mixed form: running DFT sums, (Nl x 8) x nz planes x nodes; null: full sums
   double* partial;          // (blocks) x Nl
   double* rows;             // row log: row_cap rows of N*(1+Nl) doubles
   int nodes_i, nodes_j;     // N0-4, N1-4

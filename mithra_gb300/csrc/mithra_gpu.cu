@@ -542,7 +542,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   cudaFree(ctx->screen_lz); cudaFree(ctx->screen_rec); cudaFree(ctx->screen_key); cudaFree(ctx->screen_count);
   if (ctx->st_host) cudaFreeHost(ctx->st_host);
   for (auto& po : ctx->power) {
-    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
+    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot, po.run};
     for (void* q : qs) cudaFree(q);
   }
   for (auto& pe : ctx->pending) { cudaEventDestroy(pe.second.first); cudaEventDestroy(pe.second.second); }
@@ -629,7 +629,7 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
   if (!ctx || n < 0 || n > MITHRA_MAX_POWER_OUTPUTS || (n && !outs)) return MITHRA_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   for (auto& po : ctx->power) {
-    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot};
+    void* qs[] = {po.z, po.dzr, po.tw_re, po.tw_im, po.fdt, po.partial, po.rows, po.plane_k, po.plane_slot, po.run};
     for (void* q : qs) cudaFree(q);
   }
   ctx->power.clear();
@@ -671,6 +671,12 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
     const size_t fdt_n = (size_t)d.Nf * 4 * pw.nz * (size_t)std::max<long long>(nodes, 1);
     CK(dalloc(&po.fdt, fdt_n));
     CK(cudaMemsetAsync(po.fdt, 0, fdt_n * sizeof(double), ctx->stream));
+    if (ctx->precision == MITHRA_PRECISION_FP32 && d.Nl) {
+      // The mixed form keeps the DFT sums per node and updates them with the slot that changes.
+      const size_t run_n = (size_t)d.Nl * 8 * pw.nz * (size_t)std::max<long long>(nodes, 1);
+      CK(dalloc(&po.run, run_n));
+      CK(cudaMemsetAsync(po.run, 0, run_n * sizeof(double), ctx->stream));
+    }
     CK(dalloc(&po.partial, (size_t)d.N * pw.blocks_per_plane * std::max(d.Nl, 1)));
     CK(cudaMemcpyAsync(po.z, d.z, d.N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(po.dzr, pz.data(), d.N * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
@@ -682,7 +688,7 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
     }
     CK(cudaStreamSynchronize(ctx->stream));
     pw.z = po.z; pw.plane_k = po.plane_k; pw.plane_dzr = po.dzr; pw.plane_slot = po.plane_slot;
-    pw.tw_re = po.tw_re; pw.tw_im = po.tw_im; pw.fdt = po.fdt; pw.partial = po.partial;
+    pw.tw_re = po.tw_re; pw.tw_im = po.tw_im; pw.fdt = po.fdt; pw.partial = po.partial; pw.run = po.run;
     pw.rows = nullptr; pw.row_cap = 0;
     ctx->power.push_back(po);
   }

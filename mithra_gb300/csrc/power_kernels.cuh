@@ -2,8 +2,10 @@
 //
 // Per sampling plane and transverse node (i, j in [2, N-3]): interpolate E and B in z, transform
 // them into the lab frame, store the four values in ring slot nTime % Nf, and run the Nf-tap DFT
-// at each frequency.  Per-node contributions are summed per block into a partial buffer that a
-// second, single-block kernel reduces in a fixed order, so a run is reproducible.
+// at each frequency (the FP64 form sums the whole ring as the reference does; the mixed form keeps
+// the sums per node and adds the change of the one slot that was overwritten).  Per-node
+// contributions are summed per block into a partial buffer that a second, single-block kernel
+// reduces in a fixed order, so a run is reproducible.
 #pragma once
 #include "device_common.cuh"
 
@@ -34,23 +36,42 @@ __global__ void __launch_bounds__(BLOCK) k_power_sample(GridDev g, PowerDev pw, 
     const long long ni = (long long)pw.plane_slot[plane] * nodes + t;
     double* f = pw.fdt + (long long)slot * sstride + ni;
     // Lab-frame fields, src/radiation.cpp:187-191.
-    f[0] = pw.gamma * (et0 + pw.c0 * pw.beta * bt1);
-    f[vstride] = pw.gamma * (et1 - pw.c0 * pw.beta * bt0);
-    f[2 * vstride] = pw.gamma * (bt0 - pw.beta / pw.c0 * et1);
-    f[3 * vstride] = pw.gamma * (bt1 + pw.beta / pw.c0 * et0);
-    for (int l = 0; l < pw.Nl; l++) {
-      double ew1r = 0.0, ew1i = 0.0, bw1r = 0.0, bw1i = 0.0, ew2r = 0.0, ew2i = 0.0, bw2r = 0.0, bw2i = 0.0;
-      const double* h = pw.fdt + ni;
-      for (int m = 0; m < pw.Nf; m++) {
-        const double g0 = h[0], g1 = h[vstride], g2 = h[2 * vstride], g3 = h[3 * vstride];
-        const double cr = __ldg(pw.tw_re + l * pw.Nf + m), ci = __ldg(pw.tw_im + l * pw.Nf + m);
-        ew1r += g0 * cr; ew1i += g0 * ci;
-        bw1r += g3 * cr; bw1i -= g3 * ci;
-        ew2r += g1 * cr; ew2i += g1 * ci;
-        bw2r += g2 * cr; bw2i -= g2 * ci;
-        h += sstride;
+    const double f0 = pw.gamma * (et0 + pw.c0 * pw.beta * bt1);
+    const double f1 = pw.gamma * (et1 - pw.c0 * pw.beta * bt0);
+    const double f2 = pw.gamma * (bt0 - pw.beta / pw.c0 * et1);
+    const double f3 = pw.gamma * (bt1 + pw.beta / pw.c0 * et0);
+    if (pw.run) {
+      // Running sums (mixed form): the sum over the ring changes only in this step's slot, by
+      // (new - old) times that slot's twiddle.  Same terms as the loop below, O(1) per step.
+      const double d0 = f0 - f[0], d1 = f1 - f[vstride], d2 = f2 - f[2 * vstride], d3 = f3 - f[3 * vstride];
+      f[0] = f0; f[vstride] = f1; f[2 * vstride] = f2; f[3 * vstride] = f3;
+      const long long all = (long long)pw.nz * nodes;
+      for (int l = 0; l < pw.Nl; l++) {
+        double* r = pw.run + (long long)l * 8 * all + ni;
+        const double cr = __ldg(pw.tw_re + l * pw.Nf + slot), ci = __ldg(pw.tw_im + l * pw.Nf + slot);
+        const double ew1r = r[0] + d0 * cr, ew1i = r[all] + d0 * ci, bw1r = r[2 * all] + d3 * cr,
+                     bw1i = r[3 * all] - d3 * ci, ew2r = r[4 * all] + d1 * cr, ew2i = r[5 * all] + d1 * ci,
+                     bw2r = r[6 * all] + d2 * cr, bw2i = r[7 * all] - d2 * ci;
+        r[0] = ew1r; r[all] = ew1i; r[2 * all] = bw1r; r[3 * all] = bw1i;
+        r[4 * all] = ew2r; r[5 * all] = ew2i; r[6 * all] = bw2r; r[7 * all] = bw2i;
+        s_red[l * BLOCK + threadIdx.x] = pw.pc * ((ew1r * bw1r - ew1i * bw1i) - (ew2r * bw2r - ew2i * bw2i));
       }
-      s_red[l * BLOCK + threadIdx.x] = pw.pc * ((ew1r * bw1r - ew1i * bw1i) - (ew2r * bw2r - ew2i * bw2i));
+    } else {
+      f[0] = f0; f[vstride] = f1; f[2 * vstride] = f2; f[3 * vstride] = f3;
+      for (int l = 0; l < pw.Nl; l++) {
+        double ew1r = 0.0, ew1i = 0.0, bw1r = 0.0, bw1i = 0.0, ew2r = 0.0, ew2i = 0.0, bw2r = 0.0, bw2i = 0.0;
+        const double* h = pw.fdt + ni;
+        for (int m = 0; m < pw.Nf; m++) {
+          const double g0 = h[0], g1 = h[vstride], g2 = h[2 * vstride], g3 = h[3 * vstride];
+          const double cr = __ldg(pw.tw_re + l * pw.Nf + m), ci = __ldg(pw.tw_im + l * pw.Nf + m);
+          ew1r += g0 * cr; ew1i += g0 * ci;
+          bw1r += g3 * cr; bw1i -= g3 * ci;
+          ew2r += g1 * cr; ew2i += g1 * ci;
+          bw2r += g2 * cr; bw2i -= g2 * ci;
+          h += sstride;
+        }
+        s_red[l * BLOCK + threadIdx.x] = pw.pc * ((ew1r * bw1r - ew1i * bw1i) - (ew2r * bw2r - ew2i * bw2i));
+      }
     }
   }
   __syncthreads();
