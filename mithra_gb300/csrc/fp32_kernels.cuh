@@ -299,6 +299,11 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
       fx -= ix; fy -= iy; fz -= iz;
       pt.cell[p] = pack_cell(i, j, k);
       pt.fx[p] = fx; pt.fy[p] = fy; pt.fz[p] = fz;
+      // The erase of non-finite particles (k_erase_f32), done here while the values are in registers.
+      if (!isfinite(gx + gy + gz + fx + fy + fz)) {
+        pt.status[p] = cur.status | 1;
+        atomicAdd(&st->nonfinite, 1);
+      }
       // z-face crossing of the wrapped position (src/solver.cpp:1544-1548), in cells.
       const int kwn = kw + (int)iz;
       if (kwn < 0) cross = 1;

@@ -275,7 +275,9 @@ int enqueue_step(mithra_ctx* ctx) {
   for (int s = 0; s < ns; s++)
     if ((r = stage_push(ctx, s == 0))) return r;
   if (ns == 0 && (r = stage_save_positions(ctx))) return r;
-  if ((r = stage_erase(ctx))) return r;
+  // The mixed-form push flags non-finite particles itself, so its erase pass is needed only
+  // when no push ran.
+  if ((ctx->precision != MITHRA_PRECISION_FP32 || ns == 0) && (r = stage_erase(ctx))) return r;
   if ((r = stage_screen(ctx))) return r;
   if ((r = stage_power(ctx))) return r;
   rotate(ctx);
