@@ -178,6 +178,8 @@ int fp32_push(mithra_ctx* ctx, int save_rnm);
 int fp32_save_positions(mithra_ctx* ctx);
 int fp32_erase(mithra_ctx* ctx);
 int fp32_current(mithra_ctx* ctx);
+int fp32_sort(mithra_ctx* ctx);          // tile sort into the other buffer set, which becomes current
+bool fp32_sorts_this_step(const mithra_ctx* ctx);
 void fp32_after_step(mithra_ctx* ctx);  // swap the particle buffer sets as one step's sort did
 
 }  // namespace mithra

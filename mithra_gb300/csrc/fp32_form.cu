@@ -313,6 +313,26 @@ int fp32_current(mithra_ctx* ctx) {
   DepositF32 D{g.N0, g.N1, g.N2, (float)g.dx, (float)g.dy, (float)g.dz};
   Fp32State& f = ctx->f32;
   const TileGrid T = tile_grid(ctx);
+  if (fp32_sorts_this_step(ctx)) {
+    const int r = fp32_sort(ctx);
+    if (r) return r;
+  }
+  return timed(ctx, "deposit", [&] {
+    k_deposit_tiled<<<T.n_tiles + kOutsideBlocks, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
+        D, T, f.pt, f.offsets, ctx->st, J, rho, g.cstride, g.plane, g.P1);
+  });
+}
+
+// The particles are sorted by tile on one step in three (the step whose rotation puts the new
+// potential in buffer 0), so a cycle of six steps swaps the buffer sets twice and a step's graph
+// stays a function of (rotation, buffer set).  In between, a particle deposits from the tile of
+// the last sort: in the boosted frame it moves a fraction of a cell per step, so it stays inside
+// that tile's one-cell halo almost always, and the deposit sends it to global atomics when not.
+bool fp32_sorts_this_step(const mithra_ctx* ctx) { return ctx->idx[0] == 0; }
+
+int fp32_sort(mithra_ctx* ctx) {
+  Fp32State& f = ctx->f32;
+  const TileGrid T = tile_grid(ctx);
   const int blocks = grid_stride_blocks(ctx, (long long)ctx->capacity, 256);
   int r = timed(ctx, "tile_hist", [&] {
     k_tile_hist<<<blocks, 256, 0, ctx->stream>>>(T, f.pt, ctx->st, f.counts, f.key, f.rank);
@@ -332,10 +352,7 @@ int fp32_current(mithra_ctx* ctx) {
   });
   if (r) return r;
   fp32_after_step(ctx);  // the sorted set becomes current
-  return timed(ctx, "deposit", [&] {
-    k_deposit_tiled<<<T.n_tiles + kOutsideBlocks, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
-        D, T, f.pt, f.offsets, ctx->st, J, rho, g.cstride, g.plane, g.P1);
-  });
+  return MITHRA_OK;
 }
 
 }  // namespace mithra

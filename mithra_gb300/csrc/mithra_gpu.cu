@@ -384,7 +384,7 @@ int capture_step(mithra_ctx* ctx, cudaGraph_t* out) {
 
 void after_step(mithra_ctx* ctx) {
   rotate(ctx);
-  if (ctx->precision == MITHRA_PRECISION_FP32) fp32_after_step(ctx);
+  if (ctx->precision == MITHRA_PRECISION_FP32 && fp32_sorts_this_step(ctx)) fp32_after_step(ctx);
 }
 
 int prepare_run(mithra_ctx* ctx, int64_t nsteps) {
@@ -878,6 +878,11 @@ int particles_from_device_records(mithra_ctx* ctx, const double* staging, size_t
   ctx->st_host->k_hi_next = -0x7fffffff;
   ctx->st_host->next_id = (long long)n;
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->precision == MITHRA_PRECISION_FP32) {
+    // The deposit of a step that does not sort uses the tiles of the last sort: sort now.
+    const int r = fp32_sort(ctx);
+    if (r) return r;
+  }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->particles_loaded = true;
   return MITHRA_OK;

@@ -1,6 +1,6 @@
 // Tile sort and tiled current deposit of the mixed form.
 //
-// Every field step the particles are counting-sorted by deposit tile (TX x TY x TZ cells).  The
+// Every third field step the particles are counting-sorted by deposit tile (TX x TY x TZ cells).  The
 // deposit then gives one block to each tile: the block accumulates the zigzag currents of its
 // particles in a shared-memory copy of the tile's nodes (with a one-cell halo on each side, since
 // the previous position may lie in a neighbouring cell) and adds that copy to J once.  Compared
@@ -297,12 +297,15 @@ __global__ void __launch_bounds__(kDepositBlock, 6)
   extern __shared__ float sJ[];  // 3 * TILE_NODES
   const int b = blockIdx.x;
   const bool tile_block = b < T.n_tiles;
-  // Blocks past the tiles share the bin of particles outside the tiled cells (one block for that
-  // bin would serialise its particles, which can number 10^5): block n_tiles + r takes the
-  // particles r * kDepositBlock + t, stepping by kOutsideBlocks * kDepositBlock.
+  // Blocks past the tiles share the particles that follow the tiles' bins (one block for them
+  // would serialise 10^5 particles): block n_tiles + r takes the particles r * kDepositBlock + t,
+  // stepping by kOutsideBlocks * kDepositBlock.  Those are the bin of particles outside the tiled
+  // cells and, on a step that did not sort, the particles appended since the last sort (they
+  // follow the live particles of the sort, where the bin of erased particles began).
   const int bin = tile_block ? b : T.bin_outside;
   const int stride = tile_block ? kDepositBlock : kOutsideBlocks * kDepositBlock;
-  const int beg = offsets[bin] + (tile_block ? 0 : (b - T.n_tiles) * kDepositBlock), end = offsets[bin + 1];
+  const int beg = offsets[bin] + (tile_block ? 0 : (b - T.n_tiles) * kDepositBlock);
+  const int end = tile_block ? offsets[b + 1] : (int)st->n_particles;
   if (beg >= end) return;
   const bool tiled = tile_block && end - beg >= kSparseTile;
   int i0 = 0, j0 = 0, k0 = 0;
@@ -320,9 +323,11 @@ __global__ void __launch_bounds__(kDepositBlock, 6)
   struct Loaded {
     long long cell, mcell;
     float fx, fy, fz, mfx, mfy, mfz, q;
+    uint8_t status;
   };
   auto load = [&](int p) {
     Loaded L;
+    L.status = pt.status[p];  // particles erased since the last sort stay in their bins until the next
     L.cell = pt.cell[p]; L.mcell = pt.mcell[p];
     L.fx = pt.fx[p]; L.fy = pt.fy[p]; L.fz = pt.fz[p];
     L.mfx = pt.mfx[p]; L.mfy = pt.mfy[p]; L.mfz = pt.mfz[p];
@@ -338,12 +343,15 @@ __global__ void __launch_bounds__(kDepositBlock, 6)
     int ip, jp, kp, im, jm, km;
     unpack_cell(cur.cell, ip, jp, kp);
     unpack_cell(cur.mcell, im, jm, km);
-    kmin = min(kmin, kp);
-    kmax = max(kmax, kp);
+    const bool live = !(cur.status & 1);
+    if (live) {
+      kmin = min(kmin, kp);
+      kmax = max(kmax, kp);
+    }
     const float fxp = cur.fx, fyp = cur.fy, fzp = cur.fz;
     const float fxm = cur.mfx, fym = cur.mfy, fzm = cur.mfz;
-    const bool bp = inside_f32(D, ip, jp, kp, fxp, fyp);
-    const bool bm = inside_f32(D, im, jm, km, fxm, fym);
+    const bool bp = live && inside_f32(D, ip, jp, kp, fxp, fyp);
+    const bool bm = live && inside_f32(D, im, jm, km, fxm, fym);
     if (bp || bm) {
       int bx, by, bz;
       float rxm, rxp, rym, ryp, rzm, rzp;
