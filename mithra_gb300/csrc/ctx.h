@@ -179,6 +179,7 @@ int fp32_save_positions(mithra_ctx* ctx);
 int fp32_erase(mithra_ctx* ctx);
 int fp32_current(mithra_ctx* ctx);
 int fp32_sort(mithra_ctx* ctx);          // tile sort into the other buffer set, which becomes current
+int fp32_unsorted(mithra_ctx* ctx, long long n);  // bins that hold all n particles outside the tiles
 bool fp32_sorts_this_step(const mithra_ctx* ctx);
 void fp32_after_step(mithra_ctx* ctx);  // swap the particle buffer sets as one step's sort did
 

@@ -330,6 +330,14 @@ int fp32_current(mithra_ctx* ctx) {
 // that tile's one-cell halo almost always, and the deposit sends it to global atomics when not.
 bool fp32_sorts_this_step(const mithra_ctx* ctx) { return ctx->idx[0] == 0; }
 
+int fp32_unsorted(mithra_ctx* ctx, long long n) {
+  const TileGrid T = tile_grid(ctx);
+  k_offsets_unsorted<<<(T.n_bins + 1 + 255) / 256, 256, 0, ctx->stream>>>(ctx->f32.offsets, T.n_tiles, T.n_bins,
+                                                                          (int)n);
+  CK(cudaGetLastError());
+  return MITHRA_OK;
+}
+
 int fp32_sort(mithra_ctx* ctx) {
   Fp32State& f = ctx->f32;
   const TileGrid T = tile_grid(ctx);

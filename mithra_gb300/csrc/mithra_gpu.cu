@@ -879,8 +879,9 @@ int particles_from_device_records(mithra_ctx* ctx, const double* staging, size_t
   ctx->st_host->next_id = (long long)n;
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->precision == MITHRA_PRECISION_FP32) {
-    // The deposit of a step that does not sort uses the tiles of the last sort: sort now.
-    const int r = fp32_sort(ctx);
+    // Until the first sort, the deposit takes every particle as one outside the tiles (the
+    // particles keep their upload order, which z-face copies and downloads follow).
+    const int r = fp32_unsorted(ctx, (long long)n);
     if (r) return r;
   }
   CK(cudaStreamSynchronize(ctx->stream));

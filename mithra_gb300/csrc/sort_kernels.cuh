@@ -129,6 +129,13 @@ __global__ void __launch_bounds__(1024) k_scan_add(int* counts, int* offsets, co
   }
 }
 
+// Bin offsets before the first sort: every tile empty, all n particles in the bin outside the
+// tiles, no erased ones.
+__global__ void k_offsets_unsorted(int* offsets, int n_tiles, int n_bins, int n) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b <= n_bins) offsets[b] = b <= n_tiles ? 0 : n;
+}
+
 // Pass 3: scatter every particle to its sorted slot in the other buffer set.
 // Each thread moves two particles per iteration: all their loads are issued before any store,
 // so a thread keeps the destination lookups and 2 x 15 loads in flight (the kernel is bound by
