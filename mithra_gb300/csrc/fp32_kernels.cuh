@@ -325,9 +325,25 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
 
 // The ordered append of z-face copies (src/solver.cpp:1551-1568) and the bunch time advance,
 // for the mixed-form particle arrays (one block).
+// Copies of the particles that crossed a z face in one pass, ordered by id when they fit here
+// (the reference appends them in its list order, which the ids follow); more than this many in
+// one pass are appended in array order.
+constexpr int kCrossSorted = 2048;
+
+__device__ __forceinline__ void copy_particle(const ParticlesF32& pt, long long d, long long p, int id) {
+  pt.cell[d] = pt.cell[p]; pt.fx[d] = pt.fx[p]; pt.fy[d] = pt.fy[p]; pt.fz[d] = pt.fz[p];
+  pt.gx[d] = pt.gx[p]; pt.gy[d] = pt.gy[p]; pt.gz[d] = pt.gz[p];
+  pt.mcell[d] = pt.mcell[p]; pt.mfx[d] = pt.mfx[p]; pt.mfy[d] = pt.mfy[p]; pt.mfz[d] = pt.mfz[p];
+  pt.q[d] = pt.q[p]; pt.e[d] = pt.e[p]; pt.status[d] = pt.status[p]; pt.cross[d] = 0;
+  pt.id[d] = id;
+}
+
 __global__ void __launch_bounds__(1024) k_substep_end_f32(ParticlesF32 pt, StateDev* st, double bunch_time_step) {
   __shared__ long long s_base;
   __shared__ int s_warp[32];
+  __shared__ int s_count;
+  __shared__ int s_idx[kCrossSorted];
+  __shared__ int s_key[kCrossSorted];
   const unsigned long long ncross = st->n_cross;
   if (ncross) {
     const long long n = st->n_particles;
@@ -336,12 +352,15 @@ __global__ void __launch_bounds__(1024) k_substep_end_f32(ParticlesF32 pt, State
     if ((long long)(n + ncross) > st->capacity) {
       if (threadIdx.x == 0) st->overflow = 1;
     } else {
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
       for (int pass = 1; pass <= 2; pass++) {
+        // this pass's crossing particles, in array order, into s_idx
+        if (threadIdx.x == 0) s_count = 0;
+        __syncthreads();
         for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
           const long long p = c0 + threadIdx.x;
           const int take = (p < n) && (pt.cross[p] == pass);
           const unsigned bal = __ballot_sync(0xffffffffu, take);
-          const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
           if (lane == 0) s_warp[warp] = __popc(bal);
           __syncthreads();
           int before = 0, total = 0;
@@ -350,18 +369,50 @@ __global__ void __launch_bounds__(1024) k_substep_end_f32(ParticlesF32 pt, State
             total += s_warp[w];
           }
           before += __popc(bal & ((1u << lane) - 1u));
-          if (take) {
-            const long long d = s_base + before;
-            pt.cell[d] = pt.cell[p]; pt.fx[d] = pt.fx[p]; pt.fy[d] = pt.fy[p]; pt.fz[d] = pt.fz[p];
-            pt.gx[d] = pt.gx[p]; pt.gy[d] = pt.gy[p]; pt.gz[d] = pt.gz[p];
-            pt.mcell[d] = pt.mcell[p]; pt.mfx[d] = pt.mfx[p]; pt.mfy[d] = pt.mfy[p]; pt.mfz[d] = pt.mfz[p];
-            pt.q[d] = pt.q[p]; pt.e[d] = pt.e[p]; pt.status[d] = pt.status[p]; pt.cross[d] = 0;
-            pt.id[d] = st->next_id + (d - n);
-          }
+          const int slot = s_count + before;
+          if (take && slot < kCrossSorted) s_idx[slot] = (int)p;
           __syncthreads();
-          if (threadIdx.x == 0) s_base += total;
+          if (threadIdx.x == 0) s_count += total;
           __syncthreads();
         }
+        const int m = s_count;
+        if (m <= kCrossSorted) {
+          // rank by id (ids are distinct): copy t goes to s_base + #{u : id_u < id_t}
+          for (int t = threadIdx.x; t < m; t += blockDim.x) s_key[t] = pt.id[s_idx[t]];
+          __syncthreads();
+          for (int t = threadIdx.x; t < m; t += blockDim.x) {
+            const int key = s_key[t];
+            int r = 0;
+            for (int u = 0; u < m; u++) r += s_key[u] < key;
+            const long long d = s_base + r;
+            copy_particle(pt, d, s_idx[t], (int)(st->next_id + (d - n)));
+          }
+        } else {
+          for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
+            const long long p = c0 + threadIdx.x;
+            const int take = (p < n) && (pt.cross[p] == pass);
+            const unsigned bal = __ballot_sync(0xffffffffu, take);
+            if (lane == 0) s_warp[warp] = __popc(bal);
+            __syncthreads();
+            int before = 0, total = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+              if (w < warp) before += s_warp[w];
+              total += s_warp[w];
+            }
+            before += __popc(bal & ((1u << lane) - 1u));
+            if (take) {
+              const long long d = s_base + before;
+              copy_particle(pt, d, p, (int)(st->next_id + (d - n)));
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) s_base += total;
+            __syncthreads();
+          }
+          continue;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_base += m;
+        __syncthreads();
       }
       if (threadIdx.x == 0) {
         st->next_id += s_base - n;

@@ -164,3 +164,20 @@ def test_fp32_space_charge_march(gpu_available):
     print("kat-small-sc: FP32 relative L2 after 12 steps: A %.3e, phi %.3e" % (ea, ef))
     assert ea <= BEAM_MARCH_RTOL and ef <= BEAM_MARCH_RTOL
     assert ctx.download_particles().shape == run["particles12"].shape
+
+
+def test_fp32_particle_rows_follow_the_list_order_across_sorts(gpu_available):
+    """Nine field steps (three tile sorts) with z-face copies: the mixed form's download lists the
+    particles, copies included, in the FP64 form's (the reference's) list order."""
+    s = mg.Setup.from_job(job(TAGS["kat-small-fd"][0]))
+    rows = {}
+    for prec in (mg.FP64, mg.FP32):
+        ctx = mg.Context.from_setup(s, prec)
+        ctx.run_prelude()
+        ctx.run(9)
+        rows[prec] = ctx.download_particles()
+    a, b = rows[mg.FP32], rows[mg.FP64]
+    assert a.shape == b.shape
+    for col in (1, 2, 3):  # positions, relative to their range
+        span = b[:, col].max() - b[:, col].min()
+        assert np.abs(a[:, col] - b[:, col]).max() <= 1e-3 * span, col
