@@ -255,20 +255,23 @@ __device__ __forceinline__ void deposit_half_edges(double* Je, long long cs, lon
                                                    double jy, double jz) {
   const double x1 = 1.0 - dxh, x2 = dxh, y1 = 1.0 - dyh, y2 = dyh, z1 = 1.0 - dzh, z2 = dzh;
   const double qx = qh * jx, qy = qh * jy, qz = qh * jz;
-  atomicAdd(Je + m, qx * (y1 * z1));
-  atomicAdd(Je + m + 1, qx * (y2 * z1));
-  atomicAdd(Je + m + sK, qx * (y1 * z2));
-  atomicAdd(Je + m + 1 + sK, qx * (y2 * z2));
+  // q j w_u w_v as (q j w_v) w_u: six FP64 multiplies per component instead of eight (the kernel
+  // is bound by the FP64 pipe); the values differ from the reference's products by rounding only.
+  const double ax = qx * z1, bx = qx * z2, ay = qy * z1, by = qy * z2, az = qz * y1, bz = qz * y2;
+  atomicAdd(Je + m, ax * y1);
+  atomicAdd(Je + m + 1, ax * y2);
+  atomicAdd(Je + m + sK, bx * y1);
+  atomicAdd(Je + m + 1 + sK, bx * y2);
   double* Jy = Je + cs;
-  atomicAdd(Jy + m, qy * (x1 * z1));
-  atomicAdd(Jy + m + sI, qy * (x2 * z1));
-  atomicAdd(Jy + m + sK, qy * (x1 * z2));
-  atomicAdd(Jy + m + sI + sK, qy * (x2 * z2));
+  atomicAdd(Jy + m, ay * x1);
+  atomicAdd(Jy + m + sI, ay * x2);
+  atomicAdd(Jy + m + sK, by * x1);
+  atomicAdd(Jy + m + sI + sK, by * x2);
   double* Jz = Je + 2 * cs;
-  atomicAdd(Jz + m, qz * (x1 * y1));
-  atomicAdd(Jz + m + sI, qz * (x2 * y1));
-  atomicAdd(Jz + m + 1, qz * (x1 * y2));
-  atomicAdd(Jz + m + sI + 1, qz * (x2 * y2));
+  atomicAdd(Jz + m, az * x1);
+  atomicAdd(Jz + m + sI, az * x2);
+  atomicAdd(Jz + m + 1, bz * x1);
+  atomicAdd(Jz + m + sI + 1, bz * x2);
 }
 
 // J: the edge-form current buffer (zeroed by the caller); rho: node charge, or null.
