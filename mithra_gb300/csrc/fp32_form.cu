@@ -239,7 +239,12 @@ int fp32_soa_to_records(mithra_ctx* ctx, double* staging, long long slots, long 
 int fp32_eval_eb(mithra_ctx* ctx, bool full) {
   const GridDev& g = ctx->g;
   const float* fn = g.space_charge ? ctx->f32.F[ctx->idx[1]] : nullptr;
-  dim3 blk(32, 8), grd((g.N1 - 2 + 31) / 32, (g.N0 - 2 + 7) / 8, g.N2 - 2);
+  // Blocks of 256 threads whose rows span as much of a j row as possible (up to 128 nodes): on a
+  // 128-node row, 128 x 2 blocks evaluate in 0.291 ms where 32 x 8 take 0.316 (128x128x2048).
+  int bx = 32;
+  while (bx < 128 && bx < g.N1 - 2) bx *= 2;
+  const int by = 256 / bx;
+  dim3 blk(bx, by), grd((g.N1 - 2 + bx - 1) / bx, (g.N0 - 2 + by - 1) / by, g.N2 - 2);
   return timed(ctx, "eval_eb", [&] {
     const EBConstF32 c{(float)(1.0 / g.dt), (float)(0.5 / (2.0 * g.dx)), (float)(0.5 / (2.0 * g.dy)),
                        (float)(0.5 / (2.0 * g.dz))};
