@@ -63,6 +63,12 @@ def parse_args():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--sweep-designs", type=int, default=384,
                     help="sweep-192: designs marched to their exits through a refilled queue (0: skip)")
+    ap.add_argument("--sweep-leg-designs", type=int, default=192,
+                    help="default workload: sweep-family designs marched through the refilled queue for the "
+                         "FEL runs/h figure (0: skip the sweep leg)")
+    ap.add_argument("--sweep-leg-slots", type=int, default=96)
+    ap.add_argument("--sweep-check-designs", type=int, default=8,
+                    help="designs marched in both forms for the P_sat error of the sweep leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp32-compare", action="store_true",
@@ -195,15 +201,21 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
+STATE_DIR = os.path.join(REPO, "oracle", "_build", "state")
+
+
+def initial_state_dir(jobpath):
+    return os.path.join(STATE_DIR, os.path.splitext(os.path.basename(jobpath))[0])
+
+
 def oracle_run_for(jobpath):
-    """The CPU restatement (oracle/) started from the same host initialisation."""
-    import mithra_gb300 as mg
+    """The CPU restatement (oracle/) started from the job's seeded initial state, read from the
+    file that build() (or a child process) wrote: this process does not load the CUDA library."""
+    from oracle import initial_state
     from oracle import pyoracle as po
-    s = mg.Setup.from_job(jobpath)
-    m = s.meta()
-    g = s.grid()
-    anp1, an, anm1 = s.fields()
-    return po, po.OracleRun(m, an, anm1, anp1, s.particles(), solver=g.solver, order=g.truncation_order), m
+    d = initial_state.ensure(jobpath, initial_state_dir(jobpath))
+    m, anp1, an, anm1, parts, solver, order, _ = initial_state.load(d)
+    return po, po.OracleRun(m, an, anm1, anp1, parts, solver=solver, order=order), m
 
 
 def units_per_step(meta, n_particles):
@@ -216,33 +228,67 @@ def units_per_step(meta, n_particles):
     return nodes, n_particles * nsub, nsub
 
 
-def cpu_baseline(jobpath, sample_seconds):
-    po, run, m = oracle_run_for(jobpath)
-    threads = cpu_threads()
+def run_config(workload, nodes, particles, nsub, precision, world):
+    """The `config` object both arms print for one workload."""
+    return {"workload": workload, "nodes": nodes, "particles": particles, "substeps": nsub, "precision": precision,
+            "parallelism": "replicas" if world > 1 else "single-gpu",
+            "l2": "inputs larger than L2 (%.1f GB of field state)" % (nodes * 3 * 3 * 8 / 1e9)}
+
+
+def host_cpu():
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k = line.split(":")[0].strip().lower()
+                if k in ("model name", "cpu model"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        import platform
+        model = platform.machine()
+    return {"model": model, "logical_cpus": os.cpu_count(), "threads_available": cpu_threads()}
+
+
+def time_oracle(run, po, threads, min_seconds, max_steps):
+    """Steps of the oracle at `threads` OpenMP threads until `min_seconds` or `max_steps`."""
     po.set_threads(threads)
-    nodes, pushes, _ = units_per_step(m, run.n)
-    run.step()  # first-touch of the arrays
     steps, t0 = 0, time.perf_counter()
     while True:
         run.step()
         steps += 1
         el = time.perf_counter() - t0
-        if el >= sample_seconds or steps >= 200:
+        if el >= min_seconds or steps >= max_steps:
             break
     po.set_threads(1)
+    return steps, el
+
+
+def cpu_baseline(jobpath, sample_seconds):
+    po, run, m = oracle_run_for(jobpath)
+    threads = cpu_threads()
+    nodes, pushes, _ = units_per_step(m, run.n)
+    po.set_threads(threads)
+    run.step()  # first-touch of the arrays
+    steps, el = time_oracle(run, po, threads, sample_seconds, 200)
     return {"value": (nodes + pushes) * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": "%d field steps of the same job (after one untimed step), C restatement of the "
                       "reference with OpenMP over %d host threads, %.1f s" % (steps, threads, el)}
 
 
 def run_reference(args, dist):
+    """The reference algorithm on the host cores: the oracle's C restatement (pinned bit for bit
+    to the reference in the container that has the reference tree; that tree is not on the GPU
+    host, so its binary cannot be built here), all host threads, then one thread."""
     jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
     if dist.rank != 0:
         return
     po, run, m = oracle_run_for(jobpath)
     threads = cpu_threads()
-    po.set_threads(threads)
     nodes, pushes, nsub = units_per_step(m, run.n)
+    po.set_threads(threads)
     for _ in range(args.warmup):
         run.step()
     t0 = time.perf_counter()
@@ -250,33 +296,36 @@ def run_reference(args, dist):
         run.step()
     el = time.perf_counter() - t0
     value = (nodes + pushes) * args.steps / el
+    # one thread on a bounded sample of the same march (continues from the state reached)
+    s1, el1 = time_oracle(run, po, 1, args.cpu_sample_seconds, 3)
+    po.set_threads(1)
+    v1 = (nodes + pushes) * s1 / el1
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Halton bunch of the job file)",
-        "config": {"workload": args.workload, "nodes": nodes, "particles": run.n, "substeps": nsub,
-                   "precision": "fp64", "l2": "inputs larger than L2"},
+        "config": run_config(args.workload, nodes, run.n, nsub, "fp64", dist.world),
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": "%d timed field steps after %d warm-up steps, C restatement of the reference "
-                                   "(oracle/) with OpenMP over %d host threads" % (args.steps, args.warmup, threads)},
+                                   "(oracle/) with OpenMP over %d host threads, one process (the reference's "
+                                   "MPI decomposition is not used: a single domain)" % (args.steps, args.warmup, threads)},
+        "one_thread": {"value": v1, "unit": METRIC, "cores": 1, "threads": 1, "ms_per_step": 1e3 * el1 / s1,
+                       "sample": "%d further field steps of the same march on one thread" % s1,
+                       "threads_speedup": value / v1},
+        "host": host_cpu(),
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
 
 
-def run_gpu(args, dist):
-    import numpy as np
-
-    import mithra_gb300 as mg
-    prec = mg.FP64 if args.precision == "fp64" else mg.FP32
-    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
-    setup = mg.Setup.from_job(jobpath)
-    meta = setup.meta()
+def measure_form(mg, setup, prec_name, args, dist, units, interior, clocks=True):
+    """One precision form on the workload: K timed graph-replayed steps (CUDA events on the context
+    stream), the per-kernel breakdown and roofline of an instrumented pass over K more steps, and
+    the end-to-end rate through the public API with host buffers."""
+    prec = mg.FP64 if prec_name == "fp64" else mg.FP32
     ctx = mg.Context.from_setup(setup, prec, device=dist.local)
     n_part = ctx.particle_count()
-    nodes, pushes, nsub = units_per_step(meta, n_part)
-    units = nodes + pushes
     ctx.run_prelude()
     ctx.run(args.warmup)
     ctx.synchronize()
@@ -285,7 +334,8 @@ def run_gpu(args, dist):
         ms = ctx.run_timed(args.steps)
     dist.barrier()
     ms_max = dist.max(ms)
-    value = dist.world * units * args.steps / (ms_max / 1e3)
+    out = {"ms_total": ms_max, "ms_per_step": ms_max / args.steps,
+           "value": dist.world * units * args.steps / (ms_max / 1e3), "clocks": clk.summary()}
 
     # Per-kernel device times: the same K steps again, each kernel bracketed by CUDA events on
     # the context stream (direct launches instead of the step graph).
@@ -296,30 +346,29 @@ def run_gpu(args, dist):
     total_k = sum(v[0] for v in kt.values())
     dominant = max(kt.items(), key=lambda kv: kv[1][0])[0]
     dom_ms, dom_launches = kt[dominant]
-    g = setup.grid()
-    interior = (g.N0 - 2) * (g.N1 - 2) * (g.N2 - 2)
-    unit_count = n_part if dominant in ("push", "deposit", "erase") else interior
-    per_unit = ALGO_BYTES[args.precision].get(dominant)
+    unit_count = n_part if dominant in ("push", "deposit", "erase", "tile_scatter") else interior
+    per_unit = ALGO_BYTES[prec_name].get(dominant)
     peak, peak_kind = measured_peaks()
     roof = None
     if per_unit:
         avg_s = dom_ms / dom_launches / 1e3
         achieved = per_unit * unit_count / avg_s / 1e9
-        tr = traffic_table().get(args.precision, {}).get(dominant)
+        tr = traffic_table().get(prec_name, {}).get(dominant)
         roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": per_unit * unit_count,
                 "traffic": (tr * unit_count if tr else None),
                 "avg_launch_ms": dom_ms / dom_launches, "share": dom_ms / total_k}
-    kernels = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k} for k, v in kt.items()}
-    # The FP64 form is bound by GB300's FP64 pipe, not by HBM: its dominant kernel is also placed
-    # against the FP64 rate (FLOPs per unit counted by ncu on the profiling case, FMA = 2).
-    fp64_pipe = None
-    flop = traffic_table().get("fp64_flop_per_unit", {}).get(dominant) if args.precision == "fp64" else None
-    if flop:
-        tflops = flop * unit_count / (dom_ms / dom_launches / 1e3) / 1e12
-        fp64_pipe = {"kernel": dominant, "flop_per_unit": flop, "achieved": tflops, "peak": FP64_NOMINAL_TFLOPS,
-                     "unit": "TFLOP/s", "frac": tflops / FP64_NOMINAL_TFLOPS, "peak_source": "nominal"}
+    out["roofline"] = roof
+    out["dominant"] = (dominant, dom_ms / dom_launches, unit_count)
+    out["kernels"] = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k}
+                      for k, v in kt.items()}
+    # per-kernel HBM fractions for the kernels with an algorithmic byte count
+    for k, v in out["kernels"].items():
+        pu = ALGO_BYTES[prec_name].get(k)
+        if pu:
+            cnt = n_part if k in ("push", "deposit", "erase") else interior
+            v["hbm_frac"] = pu * cnt / (v["ms_per_launch"] / 1e3) / 1e9 / peak
 
     # End to end through the public API with host buffers: upload the initial state from pinned
     # host memory, march K steps, read the power rows back.
@@ -347,21 +396,81 @@ def run_gpu(args, dist):
                "ms_per_step": 1e3 * el / args.steps}
         for b in bufs:
             b.free()
-    launches = ctx.launches_per_step() * args.steps
+    out["e2e"] = e2e
+    out["launches"] = ctx.launches_per_step() * args.steps
+    out["n_part"] = n_part
     ctx.close()
+    return out
 
-    # "FP32 vs FP64": the mixed form on the same workload and step count.
+
+def sweep_leg(args, dist):
+    """FEL runs per hour of the sweep family (C4 designs, mixed form) measured through the
+    refilled queue, and the mixed form's P_sat error against the FP64 form on a fixed subset."""
+    import tempfile
+
+    import mithra_gb300 as mg
+    from mithra_gb300 import sweep
+    params = sweep.sweep_parameters(args.sweep_leg_designs, seed=20261205)
+    done, wall, rebuilds = sweep.run_queue(params, tempfile.mkdtemp(prefix="mithra-leg-"), slots=args.sweep_leg_slots,
+                                           device=dist.local)
+    runs_h = dist.sum(len(done) * 3600.0 / wall)
+    # P_sat of a fixed subset of the family in both forms, each design marched to its exit
+    sub = sweep.sweep_parameters(args.sweep_check_designs, seed=20261206)
+    psat = {}
+    for prec in (mg.FP64, mg.FP32):
+        d, _, _ = sweep.run_queue(sub, tempfile.mkdtemp(prefix="mithra-chk-"), slots=len(sub), precision=prec,
+                                  device=dist.local)
+        psat[prec] = {i: float(r.reshape(-1, 2)[:, 1].max()) for i, r in d.items()}
+    errs = sorted(abs(psat[mg.FP32][i] - psat[mg.FP64][i]) / psat[mg.FP64][i] for i in psat[mg.FP64])
+    return {"value": runs_h, "unit": "FEL runs/h", "designs": len(done), "slots": args.sweep_leg_slots,
+            "wall_s": wall, "batch_rebuilds": rebuilds, "precision": "fp32",
+            "how": "designs of the sweep family (gamma 80-400, K 0.8-2, lambda_u 1.5-3 cm, 50-500 pC, "
+                   "32-96 x 32-96 x 128-768 cells, 5e4-1e6 particles) marched to their undulator exits "
+                   "through a queue of slots refilled as designs exit; device set-up, prelude and batch "
+                   "rebuilds inside the clock",
+            "psat_error_vs_fp64": {"designs": len(errs), "max": errs[-1], "median": errs[len(errs) // 2],
+                                   "bound": 0.02, "within_bound": errs[-1] <= 0.02}}
+
+
+def run_gpu(args, dist):
+    import mithra_gb300 as mg
+    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
+    setup = mg.Setup.from_job(jobpath)
+    meta = setup.meta()
+    g = setup.grid()
+    interior = (g.N0 - 2) * (g.N1 - 2) * (g.N2 - 2)
+    n_part = setup.particles().shape[0]
+    nodes, pushes, nsub = units_per_step(meta, n_part)
+    units = nodes + pushes
+    main = measure_form(mg, setup, args.precision, args, dist, units, interior)
+    ms_max = main["ms_total"]
+    value = main["value"]
+
+    # The FP64 form is bound by GB300's FP64 pipe, not by HBM: its dominant kernel is also placed
+    # against the FP64 rate measured on this device (FLOPs per unit counted by ncu on the
+    # profiling case, FMA = 2).
+    fp64_pipe = None
+    dominant, dom_ms, unit_count = main["dominant"]
+    flop = traffic_table().get("fp64_flop_per_unit", {}).get(dominant) if args.precision == "fp64" else None
+    if flop:
+        peak = mg.probe_fp64_tflops(dist.local)
+        tflops = flop * unit_count / (dom_ms / 1e3) / 1e12
+        fp64_pipe = {"kernel": dominant, "flop_per_unit": flop, "achieved": tflops, "peak": peak,
+                     "unit": "TFLOP/s", "frac": tflops / peak,
+                     "peak_source": "measured in this run (mithra_probe_fp64_tflops: independent DFMA chains on "
+                                    "every SM); nominal %.2f" % FP64_NOMINAL_TFLOPS}
+
+    # "FP32 vs FP64": the mixed form on the same workload and step count, measured the same way.
     fp32_form = None
     if args.precision == "fp64" and not args.no_fp32_compare:
-        c32 = mg.Context.from_setup(setup, mg.FP32, device=dist.local)
-        c32.run_prelude()
-        c32.run(args.warmup)
-        c32.synchronize()
-        dist.barrier()
-        ms32 = dist.max(c32.run_timed(args.steps))
-        c32.close()
-        v32 = dist.world * units * args.steps / (ms32 / 1e3)
-        fp32_form = {"value": v32, "unit": METRIC, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value}
+        f = measure_form(mg, setup, "fp32", args, dist, units, interior)
+        fp32_form = {"value": f["value"], "unit": METRIC, "ms_per_step": f["ms_per_step"],
+                     "speedup_vs_fp64": f["value"] / value, "roofline": f["roofline"], "kernels": f["kernels"],
+                     "e2e": f["e2e"], "clocks": f["clocks"], "gpu_launches": f["launches"]}
+
+    runs = None
+    if args.workload == "fel-130x130x2050" and args.sweep_leg_designs > 0:
+        runs = sweep_leg(args, dist)
 
     if dist.rank != 0:
         return
@@ -373,18 +482,17 @@ def run_gpu(args, dist):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
         "data": "synthetic (seeded Halton bunch of the job file)",
-        "config": {"workload": args.workload, "nodes": nodes, "particles": n_part, "substeps": nsub,
-                   "precision": args.precision, "parallelism": "replicas" if dist.world > 1 else "single-gpu",
-                   "l2": "inputs larger than L2 (%.1f GB of field state)" % (nodes * 3 * 3 * 8 / 1e9)},
+        "config": run_config(args.workload, nodes, n_part, nsub, args.precision, dist.world),
         "cell_updates_per_s": dist.world * nodes * args.steps / (ms_max / 1e3),
         "particle_pushes_per_s": dist.world * pushes * args.steps / (ms_max / 1e3),
-        "roofline": roof,
+        "roofline": main["roofline"],
         "fp64_pipe": fp64_pipe,
         "fp32_form": fp32_form,
-        "kernels": kernels,
-        "gpu_launches": launches,
-        "clocks": clk.summary(),
-        "e2e": e2e,
+        "fel_runs_per_hour": runs,
+        "kernels": main["kernels"],
+        "gpu_launches": main["launches"],
+        "clocks": main["clocks"],
+        "e2e": main["e2e"],
         "cpu_baseline": cpu,
     }
     print(json.dumps(out), flush=True)

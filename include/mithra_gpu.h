@@ -216,9 +216,10 @@ int mithra_gpu_power_sample(mithra_ctx* ctx);
  * The per-block partial sums go to one fixed 1 MiB array per device (131072 doubles, shared by
  * every context on the device and needing no zeroing); an output that needs more
  * (planes x blocks per plane x frequencies) is refused with MITHRA_ERR_CAPACITY, and so is a
- * call when the row log is full (drain it with mithra_gpu_power_rows).  The first call on a
- * device looks up the array's address and may load the module: make one call before any
- * stream capture.  Calls that overlap in time on one device race on the shared array. */
+ * call when the row log is full (drain it with mithra_gpu_power_rows).  Each call looks up the
+ * array's address on the context's device; the first call on a device may load the module, so
+ * make one call before any stream capture.  Calls that overlap in time on one device race on
+ * the shared array. */
 int mithra_gpu_power_sample_noalloc(mithra_ctx* ctx);
 /* FdTd::fieldShift (src/fdtd.cpp:806-812). */
 int mithra_gpu_field_shift(mithra_ctx* ctx);
@@ -255,6 +256,11 @@ int mithra_gpu_enable_timing(mithra_ctx* ctx, int on);
 int mithra_host_alloc(size_t bytes, void** p);
 int mithra_host_free(void* p);
 
+/* Measured FP64 fused multiply-add rate of `device` in TFLOP/s (an FMA counts two), from a short
+ * kernel of independent FMA chains on every SM (no counterpart in the reference).  The FP64 form
+ * of the loop is bound by this rate on GB300; the bench reports its kernels against it. */
+int mithra_probe_fp64_tflops(int device, double* tflops);
+
 /* ---- job-file level entry points (host initialisation of the reference, then a context) --- */
 
 /* Parses a MITHRA job file (src/readdata.cpp:10-53, src/datainput.cpp:18-751) and runs the
@@ -275,6 +281,13 @@ int mithra_gpu_get_tuning(const mithra_ctx* ctx, mithra_tuning* t);
 /* Times every candidate shape on `steps_per_trial` real field steps of the march (the steps are
  * part of the simulation) and keeps the fastest; writes the chosen shape and its ms per step. */
 int mithra_gpu_autotune(mithra_ctx* ctx, int steps_per_trial, mithra_tuning* chosen, double* ms_per_step);
+/* Attempts of each bounded barrier wait in the mixed form's bulk-tensor stencil before it gives
+ * up (no counterpart in the reference; a negative value restores the default of 2e7, 0 makes
+ * every wait give up at once).  A CTA whose wait gives up waits, with the default limit, for the
+ * copies it issued, leaves its planes unwritten, and the next call that checks the device state
+ * returns MITHRA_ERR_STATE; the error stays set for the context.  Small values exist to
+ * exercise that path. */
+int mithra_gpu_set_wait_limit(mithra_ctx* ctx, int64_t iterations);
 
 /* ---- batched instances ---------------------------------------------------------------------- */
 
@@ -298,6 +311,11 @@ int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, i
 int mithra_setup_seed(const mithra_setup* s, mithra_seed_desc* seed);
 int mithra_setup_external_fields(const mithra_setup* s, mithra_beam_desc* fields, int cap, int* n);
 int mithra_setup_time(const mithra_setup* s, mithra_time_state* t);
+/* The o-th radiation-power output as mithra_gpu_set_power takes it (Solver::initializePowerSample,
+ * src/radiation.cpp:18-121: planes, frequencies, DFT length, power constant, boosted plane
+ * positions, twiddles); the arrays belong to the setup.  *n returns the number of outputs, and
+ * out = NULL asks for that number only. */
+int mithra_setup_power(const mithra_setup* s, int o, mithra_power_desc* out, int* n);
 int mithra_setup_particles(const mithra_setup* s, double* rec, size_t cap, size_t* n);
 int mithra_setup_fields(const mithra_setup* s, double* anp1, double* an, double* anm1);
 int mithra_setup_total_time(const mithra_setup* s, double* total_time);

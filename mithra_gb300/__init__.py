@@ -125,6 +125,7 @@ _SIGS = {
     "mithra_gpu_power_sample_noalloc": [_vp],
     "mithra_gpu_bunch_sample": [_vp, _dp],
     "mithra_gpu_set_tuning": [_vp, _P(Tuning)],
+    "mithra_gpu_set_wait_limit": [_vp, C.c_int64],
     "mithra_gpu_get_tuning": [_vp, _P(Tuning)],
     "mithra_gpu_autotune": [_vp, C.c_int, _P(Tuning), _dp],
     "mithra_batch_create": [_P(_vp), C.c_int, _P(_vp)],
@@ -145,6 +146,7 @@ _SIGS = {
     "mithra_gpu_launches_per_step": [_vp, _P(C.c_int)],
     "mithra_host_alloc": [C.c_size_t, _P(_vp)],
     "mithra_host_free": [_vp],
+    "mithra_probe_fp64_tflops": [C.c_int, _dp],
     "mithra_gpu_power_rows": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
     "mithra_gpu_kernel_times": [_vp, C.c_char_p, C.c_size_t, _dp, C.c_int, _P(C.c_int)],
     "mithra_gpu_enable_timing": [_vp, C.c_int],
@@ -156,6 +158,7 @@ _SIGS = {
     "mithra_setup_seed": [_vp, _P(SeedDesc)],
     "mithra_setup_external_fields": [_vp, _P(BeamDesc), C.c_int, _P(C.c_int)],
     "mithra_setup_time": [_vp, _P(TimeState)],
+    "mithra_setup_power": [_vp, C.c_int, _P(PowerDesc), _P(C.c_int)],
     "mithra_setup_particles": [_vp, _dp, C.c_size_t, _P(C.c_size_t)],
     "mithra_setup_fields": [_vp, _dp, _dp, _dp],
     "mithra_setup_total_time": [_vp, _dp],
@@ -203,6 +206,15 @@ def fptr(a):
         return None
     assert a.dtype == np.float32 and a.flags.c_contiguous, "float32 C-contiguous array expected"
     return a.ctypes.data_as(_fp)
+
+
+def probe_fp64_tflops(device: int = 0) -> float:
+    """The device's measured FP64 FMA rate in TFLOP/s (mithra_probe_fp64_tflops)."""
+    out = np.zeros(1)
+    r = lib().mithra_probe_fp64_tflops(int(device), dptr(out))
+    if r != 0:
+        raise MithraError("mithra_probe_fp64_tflops: status %d" % r)
+    return float(out[0])
 
 
 class PinnedArray:
@@ -285,6 +297,22 @@ class Setup:
         t = TimeState()
         lib().mithra_setup_time(self._h, C.byref(t))
         return t
+
+    def power_outputs(self) -> list:
+        """The radiation-power outputs as mithra_gpu_set_power takes them: dicts of N, Nl, Nf, pc
+        and copies of the plane positions z and the twiddles re, im (Nl * Nf each)."""
+        n = C.c_int()
+        lib().mithra_setup_power(self._h, 0, None, C.byref(n))
+        out = []
+        for o in range(n.value):
+            d = PowerDesc()
+            lib().mithra_setup_power(self._h, o, C.byref(d), C.byref(n))
+            k = d.Nl * d.Nf
+            out.append({"N": d.N, "Nl": d.Nl, "Nf": d.Nf, "pc": d.pc,
+                        "z": np.ctypeslib.as_array(d.z, (d.N,)).copy() if d.N else np.zeros(0),
+                        "re": np.ctypeslib.as_array(d.twiddle_re, (k,)).copy() if k else np.zeros(0),
+                        "im": np.ctypeslib.as_array(d.twiddle_im, (k,)).copy() if k else np.zeros(0)})
+        return out
 
     def total_time(self) -> float:
         v = C.c_double()
@@ -685,6 +713,11 @@ class Context:
 
     def set_tuning(self, blocks_per_sm: int = 16, slab_planes: int = 64):
         self.call("mithra_gpu_set_tuning", C.byref(Tuning(blocks_per_sm, slab_planes)))
+
+    def set_wait_limit(self, iterations: int = -1):
+        """Attempts of each bounded barrier wait in the mixed form's stencil (negative: default;
+        0: every wait gives up at once)."""
+        self.call("mithra_gpu_set_wait_limit", int(iterations))
 
     def tuning(self) -> Tuning:
         t = Tuning()

@@ -159,6 +159,16 @@ int mithra_gpu_set_tuning(mithra_ctx* ctx, const mithra_tuning* t) {
   return MITHRA_OK;
 }
 
+int mithra_gpu_set_wait_limit(mithra_ctx* ctx, int64_t iterations) {
+  if (!ctx || iterations > 4000000000LL) return MITHRA_ERR_ARG;
+  if (iterations < 0) iterations = -1;
+  if (iterations != ctx->wait_limit) {
+    ctx->wait_limit = iterations;
+    invalidate_graphs(ctx);  // the limit is a launch argument baked into captured steps
+  }
+  return MITHRA_OK;
+}
+
 int mithra_gpu_get_tuning(const mithra_ctx* ctx, mithra_tuning* t) {
   if (!ctx || !t) return MITHRA_ERR_ARG;
   *t = ctx->tune;

@@ -94,6 +94,7 @@ struct mithra_ctx {
   int sm_count = 152;
   unsigned graph_generation = 0;  // incremented whenever the captured step graphs are dropped
   mithra_tuning tune{16, 64};     // launch shapes (mithra_gpu_set_tuning / mithra_gpu_autotune)
+  long long wait_limit = -1;      // attempts of a device barrier wait (negative: the kernels' default)
   int launches_per_step = 0;
   int launch_counter = 0;
   void* diag_partial = nullptr;  // bunch diagnostics: per-block compensated sums (allocated on first use)

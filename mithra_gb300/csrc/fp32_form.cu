@@ -80,6 +80,7 @@ int run_interior_tma(mithra_ctx* ctx, const PotentialArgs<float>& p) {
   a.a0 = p.k.a0; a.a1 = p.k.a1; a.a2 = p.k.a2; a.a3 = p.k.a3; a.asrc = p.asrc; a.al = p.k.al; a.be = p.k.be;
   a.error = f.tma_error;
   a.ks = ctx->tune.slab_planes;
+  a.spin_limit = ctx->wait_limit < 0 ? TMA_SPIN_LIMIT : (unsigned)ctx->wait_limit;
   const int nslab = (g.N2 - 2 + a.ks - 1) / a.ks;
   dim3 grd((g.N1 - 2 + TMA_TJ - 1) / TMA_TJ, (g.N0 - 2 + TMA_TI - 1) / TMA_TI, 3 * nslab);
   const CUtensorMap* an = (const CUtensorMap*)f.map_an[ctx->idx[1]];

@@ -142,6 +142,18 @@ int mithra_setup_undulators(const mithra_setup* s, mithra_undulator_desc* und, i
   return MITHRA_OK;
 }
 
+int mithra_setup_power(const mithra_setup* s, int o, mithra_power_desc* out, int* n) {
+  if (!s || !n) return MITHRA_ERR_ARG;
+  const auto& P = s->s.power;
+  *n = (int)P.size();
+  if (!out) return MITHRA_OK;
+  if (o < 0 || o >= (int)P.size()) return MITHRA_ERR_ARG;
+  const auto& pc = P[(size_t)o];
+  out->N = pc.N; out->Nl = pc.Nl; out->Nf = pc.Nf; out->pc = pc.pc;
+  out->z = pc.z.data(); out->twiddle_re = pc.tw_re.data(); out->twiddle_im = pc.tw_im.data();
+  return MITHRA_OK;
+}
+
 int mithra_setup_time(const mithra_setup* s, mithra_time_state* t) {
   if (!s || !t) return MITHRA_ERR_ARG;
   t->time = s->s.time;
@@ -301,12 +313,10 @@ int mithra_gpu_create_from_setup(const mithra_setup* s, int precision, int devic
   if (nx > MITHRA_MAX_EXT_FIELDS)
     return bail(MITHRA_ERR_ARG);
   if ((r = mithra_gpu_set_external_fields(ctx, ext.data(), nx))) return bail(r);
-  std::vector<mithra_power_desc> pw;
-  for (const auto& pc : S.power) {
-    mithra_power_desc d;
-    d.N = pc.N; d.Nl = pc.Nl; d.Nf = pc.Nf; d.pc = pc.pc;
-    d.z = pc.z.data(); d.twiddle_re = pc.tw_re.data(); d.twiddle_im = pc.tw_im.data();
-    pw.push_back(d);
+  std::vector<mithra_power_desc> pw(S.power.size());
+  for (size_t o = 0; o < pw.size(); o++) {
+    int np = 0;
+    if ((r = mithra_setup_power(s, (int)o, &pw[o], &np))) return bail(r);
   }
   if ((r = mithra_gpu_set_power(ctx, pw.data(), (int)pw.size()))) return bail(r);
   const size_t nf = (size_t)S.N1N0 * S.np * 3;

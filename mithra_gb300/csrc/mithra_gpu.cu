@@ -11,7 +11,6 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
@@ -198,20 +197,24 @@ int stage_erase(mithra_ctx* ctx) {
   });
 }
 
-int stage_power(mithra_ctx* ctx) {
+// Solver::powerSample for every output.  `partial` (optional) replaces each output's own buffer
+// of per-block partial sums: the sample kernel writes every slot the finish kernel reads within
+// the same output, so one scratch array can serve all outputs in turn.
+int stage_power(mithra_ctx* ctx, double* partial = nullptr) {
   for (size_t o = 0; o < ctx->power.size(); o++) {
-    PowerOut& po = ctx->power[o];
-    const int blocks = po.dev.N * po.dev.blocks_per_plane;
-    const size_t shm = (size_t)kPowerBlock * po.dev.Nl * sizeof(double);
+    PowerDev pw = ctx->power[o].dev;
+    if (partial) pw.partial = partial;
+    const int blocks = pw.N * pw.blocks_per_plane;
+    const size_t shm = (size_t)kPowerBlock * pw.Nl * sizeof(double);
     int r = timed(ctx, "power_sample", [&] {
       if (ctx->precision == MITHRA_PRECISION_FP64)
-        k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E64, ctx->B64, ctx->st);
+        k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E64, ctx->B64, ctx->st);
       else
-        k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, po.dev, ctx->E, ctx->B, ctx->st);
+        k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E, ctx->B, ctx->st);
     });
     if (r) return r;
     const int last = (o + 1 == ctx->power.size());
-    r = timed(ctx, "power_finish", [&] { k_power_finish<<<1, 256, 0, ctx->stream>>>(po.dev, ctx->st, last); });
+    r = timed(ctx, "power_finish", [&] { k_power_finish<<<1, 256, 0, ctx->stream>>>(pw, ctx->st, last); });
     if (r) return r;
   }
   return MITHRA_OK;
@@ -993,8 +996,9 @@ int mithra_gpu_power_sample(mithra_ctx* ctx) {
   if (!ctx) return MITHRA_ERR_ARG;
   int r = ensure_rows(ctx, 1);
   if (r) return r;
-  if (!ctx->power.empty()) ctx->rows_pending += 1;
-  return stage_power(ctx);
+  if ((r = stage_power(ctx))) return r;
+  if (!ctx->power.empty()) ctx->rows_pending += 1;  // counted once the row's kernels are queued
+  return MITHRA_OK;
 }
 
 int mithra_gpu_field_shift(mithra_ctx* ctx) {
@@ -1353,29 +1357,21 @@ namespace {
 constexpr long long kStaticPartialMax = 1LL << 17;  // 131072 doubles = 1 MiB
 static __device__ __align__(256) double g_static_partial[kStaticPartialMax];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_static_partial_mu;
-double* g_static_partial_addr[kMaxDevices] = {};
-
-// Device address of g_static_partial on `device`, looked up once per device with that device
-// current.  The first lookup on a device does set-up work in the runtime (it may load the
-// module), so callers should make one call before they start any stream capture.
+// Device address of g_static_partial on the context's device, looked up with that device current.
+// The host-side name g_static_partial is only a stand-in for the symbol, not a device address.
+// The address is looked up on every call rather than cached, so it stays right after the device
+// is reset or the module reloaded.  The first lookup on a device does set-up work in the runtime
+// (it may load the module), so callers should make their first call before any stream capture.
 int static_partial_address(mithra_ctx* ctx, double** out) {
-  const int device = ctx->device;
-  if (device < 0 || device >= kMaxDevices) return fail(ctx, MITHRA_ERR_ARG, "device %d out of range", device);
-  std::lock_guard<std::mutex> lock(g_static_partial_mu);
-  if (!g_static_partial_addr[device]) {
-    int prev = -1;
-    CK(cudaGetDevice(&prev));
-    if (prev != device) CK(cudaSetDevice(device));
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partial);
-    if (prev != device) CK(cudaSetDevice(prev));
-    if (e != cudaSuccess || !p)
-      return fail(ctx, MITHRA_ERR_CUDA, "cudaGetSymbolAddress(g_static_partial): %s", cudaGetErrorString(e));
-    g_static_partial_addr[device] = static_cast<double*>(p);
-  }
-  *out = g_static_partial_addr[device];
+  int prev = -1;
+  CK(cudaGetDevice(&prev));
+  if (prev != ctx->device) CK(cudaSetDevice(ctx->device));
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_static_partial);
+  if (prev != ctx->device) CK(cudaSetDevice(prev));
+  if (e != cudaSuccess || !p)
+    return fail(ctx, MITHRA_ERR_CUDA, "cudaGetSymbolAddress(g_static_partial): %s", cudaGetErrorString(e));
+  *out = static_cast<double*>(p);
   return MITHRA_OK;
 }
 
@@ -1399,21 +1395,8 @@ extern "C" int mithra_gpu_power_sample_noalloc(mithra_ctx* ctx) {
   double* partial = nullptr;
   int r = static_partial_address(ctx, &partial);
   if (r) return r;
-  ctx->rows_pending += 1;
-  for (size_t o = 0; o < ctx->power.size(); o++) {
-    PowerDev pw = ctx->power[o].dev;  // same output, partial sums redirected to the fixed array
-    pw.partial = partial;
-    const int blocks = pw.N * pw.blocks_per_plane;
-    const size_t shm = (size_t)kPowerBlock * pw.Nl * sizeof(double);
-    if (ctx->precision == MITHRA_PRECISION_FP64)
-      k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E64, ctx->B64, ctx->st);
-    else
-      k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E, ctx->B, ctx->st);
-    const int last = (o + 1 == ctx->power.size());
-    k_power_finish<<<1, 256, 0, ctx->stream>>>(pw, ctx->st, last);
-    ctx->launch_counter += 2;
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return fail(ctx, MITHRA_ERR_CUDA, "launch power_sample (fixed scratch): %s", cudaGetErrorString(e));
-  }
+  // The same launches as mithra_gpu_power_sample, partial sums redirected to the fixed array.
+  if ((r = stage_power(ctx, partial))) return r;
+  ctx->rows_pending += 1;  // counted once the row's kernels are queued
   return MITHRA_OK;
 }

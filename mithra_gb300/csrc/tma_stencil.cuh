@@ -2,14 +2,16 @@
 //
 // Each CTA owns a TJ x TI tile of (j, i) for one component and marches along k over a slab of
 // KS planes.  Planes of A^n (with a one-node halo), A^{n-1} and J are brought into shared memory
-// by cp.async.bulk.tensor under mbarriers: a ring of four A^n planes (k-1, k, k+1 in use, k+2 in
-// flight) and two of A^{n-1} and J.  One thread per tile column computes A^{n+1} for the plane
+// by cp.async.bulk.tensor under mbarriers: a ring of six A^n planes (k-1, k, k+1 in use, three
+// ahead in flight) and four of A^{n-1} and J.  One thread per tile column computes A^{n+1} for the plane
 // from shared memory (FD: 7 points; NSFD: the 15-point stencil of src/database.cpp:44-72) and
 // stores it with coalesced row writes.  Every byte of A^n, A^{n-1}, J is read from HBM once per
 // slab (plus the thin halos), which is what the 48 B/node roofline assumes.
 //
 // Waits are bounded: a CTA whose barrier does not complete within the iteration limit records
 // the failure in an error word and leaves after a bounded drain, instead of spinning forever.
+// The drain waits, with the default limit, for every copy group the CTA issued and has not seen
+// complete, so no bulk copy is still landing in shared memory when the CTA exits.
 #pragma once
 #include <cuda.h>
 
@@ -30,7 +32,8 @@ struct TmaStencilArgs {
   long long plane, cstride;
   float a0, a1, a2, a3, asrc, al, be;
   int ks;            // planes per slab (the z extent of a CTA's tile)
-  int* error;        // set to 1 when a barrier wait gives up
+  unsigned spin_limit;  // iterations of one barrier wait before it gives up (TMA_SPIN_LIMIT)
+  int* error;        // set to 1 when a barrier wait gives up, 2 for an unaligned slot
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void* p) {
@@ -103,52 +106,60 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
   const int j = jb + 1 + tx, i = ib + 1 + ty;
   const unsigned bytes_an = TMA_BW * TMA_BH * 4, bytes_c = TMA_BW * TMA_TI * 4;
 
-  // Issues a copy only into a 128-byte aligned slot; anything else is recorded as an error and
-  // skipped (the wait on its barrier then times out and the CTA leaves).
+  // The parity of the wait for plane kk's group on its barrier kk % RC: the planes of a slab use
+  // the barriers in turn, so barrier g completes its n-th phase for the n-th plane that maps to it.
+  auto group_parity = [&](int kk) { return (unsigned)(((kk - k_first) / TMA_RC) & 1); };
   auto aligned = [&](const void* d) { return (smem_addr(d) & 127u) == 0u; };
   auto issue_group = [&](int kk) {  // A^n(kk+1), A^{n-1}(kk), J(kk) on barrier kk % RC
     unsigned long long* b = &bar[kk % TMA_RC];
-    float* d0 = &an_slot((kk + 1) % TMA_RAN)[0][0];
-    float* d1 = &am_slot(kk % TMA_RC)[0][0];
-    float* d2 = &j_slot(kk % TMA_RC)[0][0];
-    if (!(aligned(d0) && aligned(d1) && aligned(d2))) {
-      atomicExch(a.error, 2);
-      s_abort = 1;
-      return;
-    }
     mbar_expect_tx(b, bytes_an + 2 * bytes_c);
-    tma_load_4d(d0, &map_an, jb, ib, kk + 1, comp, b);
-    tma_load_4d(d1, &map_anm1, jb, ib + 1, kk, comp, b);
-    tma_load_4d(d2, &map_j, jb, ib + 1, kk, comp, b);
+    tma_load_4d(&an_slot((kk + 1) % TMA_RAN)[0][0], &map_an, jb, ib, kk + 1, comp, b);
+    tma_load_4d(&am_slot(kk % TMA_RC)[0][0], &map_anm1, jb, ib + 1, kk, comp, b);
+    tma_load_4d(&j_slot(kk % TMA_RC)[0][0], &map_j, jb, ib + 1, kk, comp, b);
   };
 
+  // Thread 0's record of the copy groups: the last plane whose group it issued and the last one
+  // whose wait it saw complete (the drain waits for the groups in between).
+  int issued = k_first - 1, completed = k_first - 1;
   if (threadIdx.x == 0) {
     for (int b = 0; b <= TMA_RC; b++) mbar_init(&bar[b], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     s_abort = 0;
-    float* p0 = &an_slot((k_first - 1) % TMA_RAN)[0][0];
-    float* p1 = &an_slot(k_first % TMA_RAN)[0][0];
-    if (aligned(p0) && aligned(p1)) {
+    // Every slot a copy may target is checked once, before any copy is issued: a copy only goes
+    // to a 128-byte aligned slot, and an unaligned layout is recorded as an error with nothing
+    // in flight.
+    bool ok = true;
+    for (int r = 0; r < TMA_RAN; r++) ok = ok && aligned(&an_slot(r)[0][0]);
+    for (int r = 0; r < TMA_RC; r++) ok = ok && aligned(&am_slot(r)[0][0]) && aligned(&j_slot(r)[0][0]);
+    if (ok) {
       mbar_expect_tx(&bar[TMA_RC], 2 * bytes_an);
-      tma_load_4d(p0, &map_an, jb, ib, k_first - 1, comp, &bar[TMA_RC]);
-      tma_load_4d(p1, &map_an, jb, ib, k_first, comp, &bar[TMA_RC]);
-      for (int kk = k_first; kk < k_first + TMA_D && kk <= k_last && !s_abort; kk++) issue_group(kk);
+      tma_load_4d(&an_slot((k_first - 1) % TMA_RAN)[0][0], &map_an, jb, ib, k_first - 1, comp, &bar[TMA_RC]);
+      tma_load_4d(&an_slot(k_first % TMA_RAN)[0][0], &map_an, jb, ib, k_first, comp, &bar[TMA_RC]);
+      for (int kk = k_first; kk < k_first + TMA_D && kk <= k_last; kk++) {
+        issue_group(kk);
+        issued = kk;
+      }
     } else {
       atomicExch(a.error, 2);
       s_abort = 1;
     }
   }
   __syncthreads();
-  if (s_abort) return;  // nothing was issued, or copies are in flight only for earlier slots
-  unsigned phases = 0u;  // bit b: parity of the next wait on bar[b]
-  if (!mbar_wait(&bar[TMA_RC], 0, TMA_SPIN_LIMIT)) s_abort = 1;
+  if (s_abort) return;  // nothing was issued
+  const bool prologue_done = mbar_wait(&bar[TMA_RC], 0, a.spin_limit);
+  if (!prologue_done) s_abort = 1;
 
   float* out = a.np1 + (long long)comp * a.cstride;
   for (int k = k_first; k <= k_last; k++) {
     const int g = k % TMA_RC;
-    if (threadIdx.x == 0 && k + TMA_D <= k_last && !s_abort) issue_group(k + TMA_D);  // reuses the slots of plane k-1
-    if (!mbar_wait(&bar[g], (phases >> g) & 1u, TMA_SPIN_LIMIT)) s_abort = 1;
-    phases ^= 1u << g;
+    if (threadIdx.x == 0 && k + TMA_D <= k_last && !s_abort) {  // reuses the slots of planes k-1, k-2
+      issue_group(k + TMA_D);
+      issued = k + TMA_D;
+    }
+    if (!mbar_wait(&bar[g], group_parity(k), a.spin_limit))
+      s_abort = 1;
+    else if (threadIdx.x == 0)
+      completed = k;
     __syncthreads();
     if (s_abort) break;
     if (i <= a.N0 - 2 && j <= a.N1 - 2) {
@@ -176,8 +187,11 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
   if (s_abort) {
     if (threadIdx.x == 0) {
       atomicExch(a.error, 1);
-      // Bounded drain of copies still in flight into this CTA's shared memory.
-      for (int b = 0; b < TMA_RC; b++) mbar_wait(&bar[b], (phases >> b) & 1u, TMA_SPIN_LIMIT);
+      // Bounded drain of the copies that may still be in flight into this CTA's shared memory:
+      // the prologue's, and every group issued after the last completed wait (a phase that has
+      // completed already passes at once).
+      if (!prologue_done) mbar_wait(&bar[TMA_RC], 0, TMA_SPIN_LIMIT);
+      for (int kk = completed + 1; kk <= issued; kk++) mbar_wait(&bar[kk % TMA_RC], group_parity(kk), TMA_SPIN_LIMIT);
     }
     __syncthreads();
   }

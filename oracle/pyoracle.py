@@ -40,14 +40,26 @@ def build_oracle(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_reference(ref_src: str = "/root/reference/src", jobs: int = 8) -> str | None:
-    """Build oracle/_ref/ref_harness from the reference sources when they are present."""
-    if not os.path.isdir(ref_src):
+def reference_src() -> str | None:
+    """The reference's src/ directory: $MITHRA_REFERENCE_SRC, or None when it is not set."""
+    return os.environ.get("MITHRA_REFERENCE_SRC") or None
+
+
+def build_reference(ref_src: str | None = None, jobs: int = 8) -> str | None:
+    """Build oracle/_ref/ref_harness from the reference sources (`ref_src`, else
+    $MITHRA_REFERENCE_SRC, else the default of oracle/Makefile.ref) when they are present;
+    returns its path, or None when no reference tree was found."""
+    ref_src = ref_src or reference_src()
+    if ref_src and not os.path.isdir(ref_src):
         return None
     repo = os.path.dirname(HERE)
-    subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "REF_SRC=" + ref_src,
-                    "-j%d" % jobs], cwd=repo, check=True)
-    return os.path.join(HERE, "_ref", "ref_harness")
+    # without REF_SRC the recipe's own default applies (and it builds nothing where that is absent)
+    cmd = ["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "-j%d" % jobs]
+    if ref_src:
+        cmd.append("REF_SRC=" + ref_src)
+    subprocess.run(cmd, cwd=repo, check=True)
+    harness = os.path.join(HERE, "_ref", "ref_harness")
+    return harness if os.path.exists(harness) else None
 
 
 MO_MAX_EXT = 16

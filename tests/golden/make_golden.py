@@ -7,6 +7,8 @@ reference tree:
 
     python tests/golden/make_golden.py [REF_SRC] [--only=screen|--only=vtk|--only=ragged]
 
+REF_SRC defaults to $MITHRA_REFERENCE_SRC.
+
 Seeded random inputs (numpy default_rng) make every fixture reproducible.
 """
 import os
@@ -210,7 +212,9 @@ def fixtures_for(harness, jobname, tag, with_kats=True):
 def main():
     args = [a for a in sys.argv[1:] if not a.startswith("--only=")]
     only = [a.split("=", 1)[1] for a in sys.argv[1:] if a.startswith("--only=")]
-    ref_src = args[0] if args else "/root/reference/src"
+    ref_src = args[0] if args else pyoracle.reference_src()
+    if not ref_src:
+        sys.exit("give the reference's src/ directory as the first argument or in $MITHRA_REFERENCE_SRC")
     harness = pyoracle.build_reference(ref_src)
     if harness is None:
         sys.exit("reference sources not found at %s" % ref_src)

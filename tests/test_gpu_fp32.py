@@ -16,7 +16,14 @@ pytestmark = pytest.mark.gpu
 FIELD_STAGE_RTOL = 2e-6   # one field update in FP32, relative to max |A|
 PUSH_RTOL = 2e-5          # one push: E = (A^n - A^{n+1})/dt loses digits to cancellation in FP32
 DEPOSIT_RTOL = 5e-6       # relative L2 of J
-PSAT_RTOL = 0.01          # saturated (peak) radiated power of a full march vs the FP64 form
+# Full-march bounds against the FP64 form: about ten times the largest errors measured on the
+# 48x48x384 job (P_sat 4.1e-5 .. 2.5e-4 over repeated runs, whose atomic order differs; P(z)
+# curve 2.3e-4; spectrum 6.5e-5; bunching factor 4.2e-6), so that a regression shows; the
+# target itself is 1 % on P_sat.
+PSAT_RTOL = 2.5e-3        # saturated (peak) radiated power
+CURVE_RTOL = 2.5e-3       # largest P(z) difference / peak power
+SPECTRUM_RTOL = 1e-3      # final spectrum, relative L2
+BUNCHING_RTOL = 5e-5      # bunching factor at the ponderomotive wavenumber
 BEAM_MARCH_RTOL = 2e-4    # A after 12 steps with seed / laser fields, relative L2 vs the reference
 
 
@@ -149,7 +156,7 @@ def test_fp32_error_statement_p_spectrum_bunching(gpu_available):
     print("mixed vs FP64 form: P_sat %.2e, P(z) curve %.2e (max abs diff / max P), final spectrum %.2e "
           "(relative L2), bunching factor %.2e (%.4g vs %.4g)" % (psat, curve, spec, bunch, b32, b64))
     assert psat <= PSAT_RTOL
-    assert curve <= 0.05 and spec <= 0.05 and bunch <= 0.05
+    assert curve <= CURVE_RTOL and spec <= SPECTRUM_RTOL and bunch <= BUNCHING_RTOL
 
 
 def test_fp32_space_charge_march(gpu_available):
