@@ -220,6 +220,27 @@ def solve_designs(ps: list[dict], spectrum_points: int, workdir: str, device: in
     return curves, spectra, psat, host, wall
 
 
+def noise_floor(ps: list[dict], n_perturb: int, spectrum_points: int, workdir: str, device: int = 0):
+    """The full solver's own repeatability of P_sat: every design solved `n_perturb` times with
+    the macro-particle count moved by whole beamlet groups (4 particles: +0, +4, ..., the
+    bunch, undulator and mesh unchanged), which changes only the sampling noise that seeds the
+    radiation.  Returns (P_sat [n_designs x n_perturb], the spread per design: relative standard
+    deviation and median relative deviation from the design's mean)."""
+    runs = []
+    for p in ps:
+        for j in range(n_perturb):
+            q = dict(p)
+            q["particles"] = int(p["particles"]) + 4 * j
+            q["index"] = len(runs)
+            runs.append(q)
+    _, _, psat, _, _ = solve_designs(runs, spectrum_points, workdir, device)
+    P = psat.reshape(len(ps), n_perturb)
+    mean = P.mean(axis=1, keepdims=True)
+    rel_sd = P.std(axis=1) / mean[:, 0]
+    rel_dev = np.median(np.abs(P - mean) / mean, axis=1)
+    return P, rel_sd, rel_dev
+
+
 def to_log(x: np.ndarray, scale: float) -> np.ndarray:
     return np.log10(np.maximum(x, FLOOR * scale))
 
@@ -344,10 +365,21 @@ def main(argv=None):
     ap.add_argument("--save", default="", help="npz file for the dataset")
     ap.add_argument("--load", default="", help="npz dataset written by --save (no solves)")
     ap.add_argument("--gemm-bench", action="store_true", help="time mithra_tc_gemm and exit")
+    ap.add_argument("--noise-floor", type=int, default=0, metavar="N",
+                    help="measure the solver's P_sat repeatability on N designs and exit")
+    ap.add_argument("--perturb", type=int, default=8, help="--noise-floor: solves per design")
     a = ap.parse_args(argv)
 
     if a.gemm_bench:
         print(json.dumps(gemm_bench()))
+        return
+    if a.noise_floor:
+        ps = design_parameters(a.noise_floor, a.seed, small=a.small, seeded=a.seeded)
+        P, sd, dev = noise_floor(ps, a.perturb, a.spectrum, tempfile.mkdtemp(prefix="mithra-floor-"))
+        print(json.dumps(dict(designs=a.noise_floor, perturb=a.perturb, small=a.small, seeded=a.seeded,
+                              median_rel_sd=float(np.median(sd)), p90_rel_sd=float(np.quantile(sd, 0.9)),
+                              median_rel_dev=float(np.median(dev)), p90_rel_dev=float(np.quantile(dev, 0.9)),
+                              rel_sd=[float(x) for x in sd], psat=P.tolist())))
         return
     if a.load:
         d = np.load(a.load)
