@@ -421,15 +421,21 @@ def sweep_leg(args, dist):
         d, _, _ = sweep.run_queue(sub, tempfile.mkdtemp(prefix="mithra-chk-"), slots=len(sub), precision=prec,
                                   device=dist.local)
         psat[prec] = {i: float(r.reshape(-1, 2)[:, 1].max()) for i, r in d.items()}
-    errs = sorted(abs(psat[mg.FP32][i] - psat[mg.FP64][i]) / psat[mg.FP64][i] for i in psat[mg.FP64])
+    ok = [i for i in psat[mg.FP64] if np.isfinite(psat[mg.FP64][i]) and psat[mg.FP64][i] > 0.0]
+    errs = sorted(abs(psat[mg.FP32][i] - psat[mg.FP64][i]) / psat[mg.FP64][i] for i in ok) or [float("nan")]
     return {"value": runs_h, "unit": "FEL runs/h", "designs": len(done), "slots": args.sweep_leg_slots,
             "wall_s": wall, "batch_rebuilds": rebuilds, "precision": "fp32",
             "how": "designs of the sweep family (gamma 80-400, K 0.8-2, lambda_u 1.5-3 cm, 50-500 pC, "
                    "32-96 x 32-96 x 128-768 cells, 5e4-1e6 particles) marched to their undulator exits "
                    "through a queue of slots refilled as designs exit; device set-up, prelude and batch "
                    "rebuilds inside the clock",
-            "psat_error_vs_fp64": {"designs": len(errs), "max": errs[-1], "median": errs[len(errs) // 2],
-                                   "bound": 0.02, "within_bound": errs[-1] <= 0.02}}
+            "psat_error_vs_fp64": {"designs": len(ok), "max": errs[-1], "median": errs[len(errs) // 2],
+                                   "bound": 0.02, "within_bound": bool(errs[-1] <= 0.02),
+                                   "excluded": {"no_power": sum(1 for i in psat[mg.FP64] if psat[mg.FP64][i] == 0.0),
+                                                "non_finite": sum(1 for i in psat[mg.FP64]
+                                                                  if not np.isfinite(psat[mg.FP64][i]))},
+                                   "psat_fp64": [psat[mg.FP64][i] for i in sorted(psat[mg.FP64])],
+                                   "psat_fp32": [psat[mg.FP32][i] for i in sorted(psat[mg.FP32])]}}
 
 
 def run_gpu(args, dist):

@@ -76,6 +76,8 @@ struct mithra_ctx {
   double* E64 = nullptr;  // FP64 form: E and B as doubles holding float-rounded values
   double* B64 = nullptr;
   uint8_t* plane_needed = nullptr;  // N2 flags: planes read by a power sample
+  int* eb_planes = nullptr;         // the interior planes whose E/B those flags require (mixed form)
+  int n_eb_planes = 0;
   void* und_table = nullptr;        // mixed form: per-plane undulator lz and phase
   int idx[3] = {0, 1, 2};  // buffer index of np1, n, nm1
   size_t capacity = 0;

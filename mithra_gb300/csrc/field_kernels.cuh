@@ -42,6 +42,9 @@ struct PotentialArgs {
   // deposit, J_c(node) = Je_c(node) + Je_c(node - unit step along c), instead of np1.
   const T* jedge = nullptr;
   StateDev* st = nullptr;
+  // The y faces (j = 0 and N1-1) were updated by the interior kernel already (the mixed form's
+  // bulk-tensor stencil, when no seed is injected): the face kernel leaves them out.
+  int yfaces_done = 0;
 };
 
 // Interior update, AdvanceField::advanceMagneticPotentialFD/NSFD and the scalar variants
@@ -96,7 +99,7 @@ __device__ __forceinline__ T face_value(const T* B, const T* np1, const T* n, co
 template <typename T>
 __global__ void __launch_bounds__(256) k_potential_faces(GridDev g, PotentialArgs<T> p) {
   const long long nx = (long long)(g.N1 - 2) * (g.N2 - 2);
-  const long long ny = (long long)(g.N0 - 2) * (g.N2 - 2);
+  const long long ny = p.yfaces_done ? 0 : (long long)(g.N0 - 2) * (g.N2 - 2);
   const long long nz = (long long)(g.N0 - 2) * (g.N1 - 2);
   const long long total = 2 * (nx + ny + nz);
   const long long sI = g.P1, sK = g.plane;

@@ -5,6 +5,7 @@
 #include "field_kernels.cuh"
 #include "fp32_kernels.cuh"
 #include "sort_kernels.cuh"
+#include "eb_tma.cuh"
 #include "tma_stencil.cuh"
 
 namespace mithra {
@@ -68,6 +69,7 @@ int make_tma_maps(mithra_ctx* ctx) {
   CK(cudaMemsetAsync(f.tma_error, 0, sizeof(int), ctx->stream));
   CK(cudaFuncSetAttribute(k_potential_interior_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaStencilSmem));
   CK(cudaFuncSetAttribute(k_potential_interior_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaStencilSmem));
+  CK(cudaFuncSetAttribute(k_eval_eb_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEbTmaSmem));
   f.tma_ready = true;
   return MITHRA_OK;
 }
@@ -81,6 +83,8 @@ int run_interior_tma(mithra_ctx* ctx, const PotentialArgs<float>& p) {
   a.error = f.tma_error;
   a.ks = ctx->tune.slab_planes;
   a.spin_limit = ctx->wait_limit < 0 ? TMA_SPIN_LIMIT : (unsigned)ctx->wait_limit;
+  a.yfaces = p.yfaces_done;
+  for (int q = 0; q < 5; q++) a.cB[q] = p.k.cB[q];
   const int nslab = (g.N2 - 2 + a.ks - 1) / a.ks;
   dim3 grd((g.N1 - 2 + TMA_TJ - 1) / TMA_TJ, (g.N0 - 2 + TMA_TI - 1) / TMA_TI, 3 * nslab);
   const CUtensorMap* an = (const CUtensorMap*)f.map_an[ctx->idx[1]];
@@ -102,6 +106,8 @@ int run_potential_f32(mithra_ctx* ctx, PotentialArgs<float> p, bool vector) {
                                   (long long)(g.N0 - 2) * (g.N1 - 2));
   const long long nedges = 4LL * ((g.N2 - 2) + (g.N0 - 2) + (g.N1 - 2));
   int r;
+  // the bulk-tensor stencil also updates the y faces when no seed injection comes in between
+  if (vector && ctx->f32.tma_ready) p.yfaces_done = ctx->seed_active ? 0 : 1;
   if (vector && ctx->f32.tma_ready)
     r = run_interior_tma(ctx, p);
   else if (g.solver == 1)
@@ -239,6 +245,37 @@ int fp32_soa_to_records(mithra_ctx* ctx, double* staging, long long slots, long 
 
 int fp32_eval_eb(mithra_ctx* ctx, bool full) {
   const GridDev& g = ctx->g;
+  const EBConstF32 c{(float)(1.0 / g.dt), (float)(0.5 / (2.0 * g.dx)), (float)(0.5 / (2.0 * g.dy)),
+                     (float)(0.5 / (2.0 * g.dz))};
+  Fp32State& f = ctx->f32;
+  if (!g.space_charge && f.tma_ready) {
+    // Bulk-tensor z-slabs over the planes the particles occupy (every plane when `full`), then
+    // the power-sampling planes outside them.
+    EbTmaArgs a;
+    a.E = ctx->E; a.B = ctx->B;
+    a.N0 = g.N0; a.N1 = g.N1; a.N2 = g.N2; a.P1 = g.P1; a.plane = g.plane; a.cstride = g.cstride;
+    a.rdt = c.rdt; a.hx = c.hx; a.hy = c.hy; a.hz = c.hz;
+    a.ks = ctx->tune.slab_planes;
+    a.st = full ? nullptr : ctx->st;
+    a.spin_limit = ctx->wait_limit < 0 ? TMA_SPIN_LIMIT : (unsigned)ctx->wait_limit;
+    a.error = f.tma_error;
+    const int nslab = (g.N2 - 2 + a.ks - 1) / a.ks;
+    dim3 grd((g.N1 - 2 + TMA_TJ - 1) / TMA_TJ, (g.N0 - 2 + TMA_TI - 1) / TMA_TI, nslab);
+    const CUtensorMap* a0 = (const CUtensorMap*)f.map_an[ctx->idx[1]];
+    const CUtensorMap* a1 = (const CUtensorMap*)f.map_an[ctx->idx[0]];
+    int r = timed(ctx, "eval_eb", [&] {
+      k_eval_eb_tma<<<grd, TMA_TJ * TMA_TI, kEbTmaSmem, ctx->stream>>>(*a0, *a1, a);
+    });
+    if (r || full || ctx->n_eb_planes == 0) return r;
+    int bx = 32;
+    while (bx < 128 && bx < g.N1 - 2) bx *= 2;
+    const int by = 256 / bx;
+    dim3 pblk(bx, by), pgrd((g.N1 - 2 + bx - 1) / bx, (g.N0 - 2 + by - 1) / by, ctx->n_eb_planes);
+    return timed(ctx, "eval_eb_planes", [&] {
+      k_eval_eb_planes_f32<<<pgrd, pblk, 0, ctx->stream>>>(g, c, f.A[ctx->idx[0]], f.A[ctx->idx[1]], ctx->E, ctx->B,
+                                                          ctx->eb_planes);
+    });
+  }
   const float* fn = g.space_charge ? ctx->f32.F[ctx->idx[1]] : nullptr;
   // Blocks of 256 threads whose rows span as much of a j row as possible (up to 128 nodes): on a
   // 128-node row, 128 x 2 blocks evaluate in 0.291 ms where 32 x 8 take 0.316 (128x128x2048).
@@ -247,8 +284,6 @@ int fp32_eval_eb(mithra_ctx* ctx, bool full) {
   const int by = 256 / bx;
   dim3 blk(bx, by), grd((g.N1 - 2 + bx - 1) / bx, (g.N0 - 2 + by - 1) / by, g.N2 - 2);
   return timed(ctx, "eval_eb", [&] {
-    const EBConstF32 c{(float)(1.0 / g.dt), (float)(0.5 / (2.0 * g.dx)), (float)(0.5 / (2.0 * g.dy)),
-                       (float)(0.5 / (2.0 * g.dz))};
     k_eval_eb_f32<<<grd, blk, 0, ctx->stream>>>(g, c, ctx->f32.A[ctx->idx[0]], ctx->f32.A[ctx->idx[1]], fn, ctx->E,
                                                  ctx->B, 1, g.N2 - 2, full ? nullptr : ctx->st, ctx->plane_needed);
   });

@@ -17,16 +17,12 @@ struct EBConstF32 {
   float rdt, hx, hy, hz;  // 1/dt and 0.5/(2 d) per axis
 };
 
-__global__ void __launch_bounds__(256) k_eval_eb_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
-                                                     const float* __restrict__ A0,
-                                                     const float* __restrict__ fn, float* __restrict__ E,
-                                                     float* __restrict__ B, int k_lo, int k_hi, const StateDev* st,
-                                                     const uint8_t* plane_needed) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int k = blockIdx.z + k_lo;
-  if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
-  if (!eb_plane_wanted(k, st, plane_needed, g.N2)) return;
+// E and B of one interior node (FdTd::fieldEvaluate, src/fdtd.cpp:818-845; SC src/fdtdSC.cpp:1110-1140)
+// from A^{n+1} (A1), A^n (A0) and phi^n (fn, space charge only), with the copies of planes 1 and
+// N2-2 into the boundary planes (src/fdtd.cpp:755-772).
+__device__ __forceinline__ void eval_eb_node_f32(const GridDev& g, const EBConstF32& c, const float* __restrict__ A1,
+                                                 const float* __restrict__ A0, const float* __restrict__ fn,
+                                                 float* __restrict__ E, float* __restrict__ B, int k, int i, int j) {
   const long long m = node_index(g, k, i, j);
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
   const float rdt = c.rdt, hx = c.hx, hy = c.hy, hz = c.hz;
@@ -55,6 +51,29 @@ __global__ void __launch_bounds__(256) k_eval_eb_f32(GridDev g, EBConstF32 c, co
     E[m + sK] = e0; E[cs + m + sK] = e1; E[2 * cs + m + sK] = e2;
     B[m + sK] = b0; B[cs + m + sK] = b1; B[2 * cs + m + sK] = b2;
   }
+}
+
+__global__ void __launch_bounds__(256) k_eval_eb_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
+                                                     const float* __restrict__ A0,
+                                                     const float* __restrict__ fn, float* __restrict__ E,
+                                                     float* __restrict__ B, int k_lo, int k_hi, const StateDev* st,
+                                                     const uint8_t* plane_needed) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z + k_lo;
+  if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
+  if (!eb_plane_wanted(k, st, plane_needed, g.N2)) return;
+  eval_eb_node_f32(g, c, A1, A0, fn, E, B, k, i, j);
+}
+
+// E and B on the planes of a list (the power-sampling planes outside the particle slab).
+__global__ void __launch_bounds__(256) k_eval_eb_planes_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
+                                                            const float* __restrict__ A0, float* __restrict__ E,
+                                                            float* __restrict__ B, const int* __restrict__ planes) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.N1 - 2 || i > g.N0 - 2) return;
+  eval_eb_node_f32(g, c, A1, A0, nullptr, E, B, planes[blockIdx.z], i, j);
 }
 
 // Per-launch constants of the mixed-precision push, prepared on the host from GridDev/PushDev.

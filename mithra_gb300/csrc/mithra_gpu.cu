@@ -542,6 +542,7 @@ int mithra_gpu_destroy(mithra_ctx* ctx) {
   fp32_free(ctx);
   cudaFree(ctx->staging);
   cudaFree(ctx->E64); cudaFree(ctx->B64); cudaFree(ctx->plane_needed); cudaFree(ctx->und_table);
+  cudaFree(ctx->eb_planes);
   cudaFree(ctx->E); cudaFree(ctx->B); cudaFree(ctx->st); cudaFree(ctx->und_dev); cudaFree(ctx->beams_dev); cudaFree(ctx->Jedge);
   cudaFree(ctx->diag_partial); cudaFree(ctx->diag_out);
   cudaFree(ctx->screen_lz); cudaFree(ctx->screen_rec); cudaFree(ctx->screen_key); cudaFree(ctx->screen_count);
@@ -710,6 +711,20 @@ int mithra_gpu_set_power(mithra_ctx* ctx, const mithra_power_desc* outs, int n) 
           if (kc + 1 >= 0 && kc + 1 < g.N2) flags[kc + 1] = 1;
         }
     CK(cudaMemcpyAsync(ctx->plane_needed, flags.data(), flags.size(), cudaMemcpyHostToDevice, ctx->stream));
+    // the same as a list of interior planes (planes 0 and N2-1 are copies of 1 and N2-2)
+    std::vector<int> list;
+    for (int k = 0; k < g.N2; k++)
+      if (flags[(size_t)k]) {
+        const int kk = std::min(std::max(k, 1), g.N2 - 2);
+        if (std::find(list.begin(), list.end(), kk) == list.end()) list.push_back(kk);
+      }
+    cudaFree(ctx->eb_planes);
+    ctx->eb_planes = nullptr;
+    ctx->n_eb_planes = (int)list.size();
+    if (!list.empty()) {
+      CK(dalloc(&ctx->eb_planes, list.size()));
+      CK(cudaMemcpyAsync(ctx->eb_planes, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    }
   }
   // Reset the row log.
   CK(cudaMemcpyAsync(ctx->st_host, ctx->st, sizeof(StateDev), cudaMemcpyDeviceToHost, ctx->stream));

@@ -32,6 +32,10 @@ struct TmaStencilArgs {
   long long plane, cstride;
   float a0, a1, a2, a3, asrc, al, be;
   int ks;            // planes per slab (the z extent of a CTA's tile)
+  int yfaces;        // also the Mur faces j = 0 and N1-1 (AdvanceField::advanceBoundaryF with the
+                     // face pattern of src/fdtd.cpp:377-472): only when nothing changes A^{n+1} at
+                     // j = 1 or N1-2 between the interior update and the faces (no seed injection)
+  float cB[5];       // the y-face coefficients
   unsigned spin_limit;  // iterations of one barrier wait before it gives up (TMA_SPIN_LIMIT)
   int* error;        // set to 1 when a barrier wait gives up, 2 for an unaligned slot
 };
@@ -83,7 +87,7 @@ constexpr int TMA_OFF_J = TMA_OFF_AM + TMA_RC * TMA_SLOT_C;
 constexpr int TMA_SMEM_USED = TMA_OFF_J + TMA_RC * TMA_SLOT_C;
 
 template <bool NSFD>
-__global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
+__global__ void __launch_bounds__(TMA_TJ * TMA_TI, 4) k_potential_interior_tma(
     const __grid_constant__ CUtensorMap map_an,    // A^n, box TMA_BW x TMA_BH
     const __grid_constant__ CUtensorMap map_anm1,  // A^{n-1}, box TMA_BW x TMA_TI
     const __grid_constant__ CUtensorMap map_j,     // J (the A^{n+1} buffer), box TMA_BW x TMA_TI
@@ -180,7 +184,20 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_potential_interior_tma(
         r = a.a0 * v - am[ty][x] + a.a1 * (c[y + 1][x] + c[y - 1][x]) + a.a2 * (c[y][x + 1] + c[y][x - 1]) +
             a.a3 * (p[y][x] + m[y][x]) + a.asrc * jj[ty][x];
       }
-      out[(long long)k * a.plane + (long long)i * a.P1 + j] = r;
+      const long long row = (long long)k * a.plane + (long long)i * a.P1;
+      out[row + j] = r;
+      if (a.yfaces && (j == 1 || j == a.N1 - 2)) {
+        // face node f next to this node (f = x - 1 for j = 0, x + 1 for j = N1 - 1); the terms of
+        // face_value in its order: cB0 (nm1 face + np1 inner) + cB1 nm1 inner + cB2 (n face + n
+        // inner) + cB3 (n inner and face at i +- 1) + cB4 (n inner and face at k +- 1)
+        auto face = [&](int f) {
+          return a.cB[0] * (am[ty][f] + r) + a.cB[1] * am[ty][x] + a.cB[2] * (c[y][f] + c[y][x]) +
+                 a.cB[3] * (c[y + 1][x] + c[y - 1][x] + c[y + 1][f] + c[y - 1][f]) +
+                 a.cB[4] * (p[y][x] + m[y][x] + p[y][f] + m[y][f]);
+        };
+        if (j == 1) out[row] = face(x - 1);
+        if (j == a.N1 - 2) out[row + a.N1 - 1] = face(x + 1);
+      }
     }
     __syncthreads();
   }

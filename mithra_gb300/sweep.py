@@ -46,14 +46,22 @@ def sweep_parameters(n: int = 192, seed: int = 20261204) -> list[dict]:
 def job_text(p: dict, spectrum_points: int = 0) -> str:
     """Job file of one sweep instance (the 48x48x384 FEL job with the instance's parameters).
     p may set "periods" (default 30), "sigma_r" (transverse rms size in um, default 200),
-    "lz" (mesh length along z in um, default 180; the bunch's rms length is lz / 6, truncated at
-    lz / 3, and the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD);
+    "lz" (mesh length along z in um; the bunch's rms length is lz / 6, truncated at lz / 3, and
+    the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD).  The default
+    lz follows the radiation as the 48x48x384 FEL job does (80 resonant wavelengths on 384 cells):
+    4.8 cells per resonant wavelength lambda_u (1 + K^2 / 2) / (2 gamma^2) along z, so that every
+    design resolves its own radiation; a fixed lz leaves the radiation of high-gamma designs
+    below one cell per wavelength, and such marches diverge;
     spectrum_points > 0 samples the power at that many normalized frequencies in 0.9 .. 1.1
     instead of at 1.0 only.  p["seed_a0"] > 0 adds a continuous gaussian-beam seed at the
     resonant wavelength lambda_u (1 + K^2/2) / (2 gamma^2), polarised along y, focused at the
     undulator start with a waist of 2 sigma_r and that strength parameter."""
-    lx, lz = 2400.0, float(p.get("lz", 180.0))
+    lam = p["lambda_u"] * (1.0 + 0.5 * p["K"] ** 2) / (2.0 * p["gamma"] ** 2)
+    lx, lz = 2400.0, float(p.get("lz", p["n_longitudinal"] / 4.8 * lam))
     dx, dz = lx / p["n_transverse"], lz / p["n_longitudinal"]
+    # the reference counts cells as int(L / d) + 1 (src/solver.cpp:610-612): a length a hair above
+    # the whole number of cells keeps that count from losing one to rounding
+    lz = dz * p["n_longitudinal"] * (1.0 + 1e-12)
     periods = int(p.get("periods", PERIODS))
     sr = float(p.get("sigma_r", 200.0))
     solver = p.get("solver", "FD")
