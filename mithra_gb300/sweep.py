@@ -7,6 +7,9 @@ drawn from fixed ranges with a seeded generator:
     charge 50 .. 500 pC, relative energy spread 1e-5 .. 1e-3,
     transverse cells 32 .. 96, longitudinal cells 128 .. 768, macro-particles 5e4 .. 1e6.
 
+The mesh length along z follows each design's resonant wavelength (4.8 cells per wavelength, as
+in the 48x48x384 job) and the solver is NSFD, which may widen the transverse cells.
+
 The jobs are ordinary job files (written to a work directory), set up on the host in parallel
 and stepped together on one device by `mithra_gb300.Batch`.
 """
@@ -39,6 +42,7 @@ def sweep_parameters(n: int = 192, seed: int = 20261204) -> list[dict]:
             n_transverse=int(rng.integers(32, 97)),
             n_longitudinal=int(rng.integers(128, 769)),
             particles=int(rng.integers(50_000, 1_000_001)),
+            solver="NSFD",
         ))
     return out
 
@@ -47,7 +51,9 @@ def job_text(p: dict, spectrum_points: int = 0) -> str:
     """Job file of one sweep instance (the 48x48x384 FEL job with the instance's parameters).
     p may set "periods" (default 30), "sigma_r" (transverse rms size in um, default 200),
     "lz" (mesh length along z in um; the bunch's rms length is lz / 6, truncated at lz / 3, and
-    the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD).  The default
+    the power is sampled at z = lz / 3) and "solver" ("FD" or "NSFD", default FD; the sweep family
+    uses NSFD, the reference's solver for FEL runs: with FD, low-gamma designs of the family can
+    diverge in both precision forms).  The default
     lz follows the radiation as the 48x48x384 FEL job does (80 resonant wavelengths on 384 cells):
     4.8 cells per resonant wavelength lambda_u (1 + K^2 / 2) / (2 gamma^2) along z, so that every
     design resolves its own radiation; a fixed lz leaves the radiation of high-gamma designs
