@@ -533,6 +533,13 @@ def run_sweep(args, dist):
     # until its longest design ends; refilled: finished slots take new designs at once.
     runs_lockstep = dist.world * len(ctxs) * 3600.0 / (max(steps_to_end) * step_s)
     runs_refill = dist.world * len(ctxs) * 3600.0 / (float(np.mean(steps_to_end)) * step_s)
+    # The same instances and step count one at a time, each from its own captured step graphs (a
+    # queue of single-instance launches with nothing overlapping), against the batch's one launch.
+    for c in ctxs:
+        c.run(6)  # one cycle of step phases: every step graph of the instance captured
+    ms_seq = sum(c.run_timed(args.steps) for c in ctxs)
+    sequential = {"ms_per_step": ms_seq / args.steps, "batch_speedup": ms_seq / ms_max,
+                  "how": "each instance's own step graphs launched alone, instance after instance"}
     batch.close()
     for c in ctxs:
         c.close()
@@ -558,6 +565,7 @@ def run_sweep(args, dist):
         "fel_runs_per_hour": {"lockstep": runs_lockstep, "refilled": runs_refill, "measured_queue": measured,
                               "steps_to_exit": {"min": min(steps_to_end), "mean": float(np.mean(steps_to_end)),
                                                 "max": max(steps_to_end)}},
+        "sequential": sequential,
         "tuning": [[t.blocks_per_sm, t.slab_planes, ms] for t, ms in tuned][:8],
         "clocks": clk.summary(),
     }

@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI, 4) k_potential_interior_tma(
   auto j_slot = [&](int r) { return reinterpret_cast<float(*)[TMA_BW]>(s_base + TMA_OFF_J + r * TMA_SLOT_C); };
   __shared__ __align__(8) unsigned long long bar[TMA_RC + 1];  // one per group slot; last: prologue
   __shared__ int s_abort;
+  __shared__ float s_face[2][TMA_TI];
 
   const int tx = threadIdx.x % TMA_TJ, ty = threadIdx.x / TMA_TJ;
   const int nslab = (a.N2 - 2 + a.ks - 1) / a.ks;
@@ -108,6 +109,8 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI, 4) k_potential_interior_tma(
   const int k_first = 1 + slab * a.ks;
   const int k_last = min(a.N2 - 2, k_first + a.ks - 1);
   const int j = jb + 1 + tx, i = ib + 1 + ty;
+  const bool last_cta = (int)blockIdx.x == (a.N1 - 3) / TMA_TJ;  // holds j = N1 - 2
+  const bool face_cta = a.yfaces && (jb == 0 || last_cta);
   const unsigned bytes_an = TMA_BW * TMA_BH * 4, bytes_c = TMA_BW * TMA_TI * 4;
 
   // The parity of the wait for plane kk's group on its barrier kk % RC: the planes of a slab use
@@ -154,16 +157,19 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI, 4) k_potential_interior_tma(
   if (!prologue_done) s_abort = 1;
 
   float* out = a.np1 + (long long)comp * a.cstride;
+  unsigned phases = 0u;  // bit b: parity of the next wait on bar[b] (flipped only by a completed wait)
   for (int k = k_first; k <= k_last; k++) {
     const int g = k % TMA_RC;
     if (threadIdx.x == 0 && k + TMA_D <= k_last && !s_abort) {  // reuses the slots of planes k-1, k-2
       issue_group(k + TMA_D);
       issued = k + TMA_D;
     }
-    if (!mbar_wait(&bar[g], group_parity(k), a.spin_limit))
+    if (!mbar_wait(&bar[g], (phases >> g) & 1u, a.spin_limit)) {
       s_abort = 1;
-    else if (threadIdx.x == 0)
-      completed = k;
+    } else {
+      phases ^= 1u << g;
+      if (threadIdx.x == 0) completed = k;
+    }
     __syncthreads();
     if (s_abort) break;
     if (i <= a.N0 - 2 && j <= a.N1 - 2) {
@@ -186,17 +192,28 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI, 4) k_potential_interior_tma(
       }
       const long long row = (long long)k * a.plane + (long long)i * a.P1;
       out[row + j] = r;
-      if (a.yfaces && (j == 1 || j == a.N1 - 2)) {
-        // face node f next to this node (f = x - 1 for j = 0, x + 1 for j = N1 - 1); the terms of
-        // face_value in its order: cB0 (nm1 face + np1 inner) + cB1 nm1 inner + cB2 (n face + n
-        // inner) + cB3 (n inner and face at i +- 1) + cB4 (n inner and face at k +- 1)
-        auto face = [&](int f) {
-          return a.cB[0] * (am[ty][f] + r) + a.cB[1] * am[ty][x] + a.cB[2] * (c[y][f] + c[y][x]) +
-                 a.cB[3] * (c[y + 1][x] + c[y - 1][x] + c[y + 1][f] + c[y - 1][f]) +
-                 a.cB[4] * (p[y][x] + m[y][x] + p[y][f] + m[y][f]);
-        };
-        if (j == 1) out[row] = face(x - 1);
-        if (j == a.N1 - 2) out[row + a.N1 - 1] = face(x + 1);
+      if (j == 1) s_face[0][ty] = r;          // A^{n+1} next to the y faces, for the face update below
+      if (j == a.N1 - 2) s_face[1][ty] = r;
+    }
+    if (face_cta) {
+      // The y-face nodes of this tile's rows (j = 0 in the first tile column, j = N1-1 in the last),
+      // one per lane of warps 0 and 1, from the planes still in shared memory: the terms of
+      // face_value in its order, cB0 (nm1 face + np1 inner) + cB1 nm1 inner + cB2 (n face + n
+      // inner) + cB3 (n inner and face at i +- 1) + cB4 (n inner and face at k +- 1).
+      __syncthreads();
+      const int side = threadIdx.x >> 5, l = threadIdx.x & 31;
+      const int fi = ib + 1 + l;
+      if (side < 2 && l < TMA_TI && fi <= a.N0 - 2 && ((side == 0 && jb == 0) || (side == 1 && last_cta))) {
+        const int xi = side == 0 ? 1 : a.N1 - 2 - jb, f = side == 0 ? 0 : xi + 1, fy = l + 1;
+        const float(*c)[TMA_BW] = an_slot(k % TMA_RAN);
+        const float(*m)[TMA_BW] = an_slot((k - 1) % TMA_RAN);
+        const float(*p)[TMA_BW] = an_slot((k + 1) % TMA_RAN);
+        const float(*am)[TMA_BW] = am_slot(g);
+        const float rr = s_face[side][l];
+        const float v = a.cB[0] * (am[l][f] + rr) + a.cB[1] * am[l][xi] + a.cB[2] * (c[fy][f] + c[fy][xi]) +
+                        a.cB[3] * (c[fy + 1][xi] + c[fy - 1][xi] + c[fy + 1][f] + c[fy - 1][f]) +
+                        a.cB[4] * (p[fy][xi] + m[fy][xi] + p[fy][f] + m[fy][f]);
+        out[(long long)k * a.plane + (long long)fi * a.P1 + (side == 0 ? 0 : a.N1 - 1)] = v;
       }
     }
     __syncthreads();

@@ -220,17 +220,24 @@ def solve_designs(ps: list[dict], spectrum_points: int, workdir: str, device: in
     return curves, spectra, psat, host, wall
 
 
-def noise_floor(ps: list[dict], n_perturb: int, spectrum_points: int, workdir: str, device: int = 0):
+def noise_floor(ps: list[dict], n_perturb: int, spectrum_points: int, workdir: str, device: int = 0,
+                step: float = 4):
     """The full solver's own repeatability of P_sat: every design solved `n_perturb` times with
-    the macro-particle count moved by whole beamlet groups (4 particles: +0, +4, ..., the
-    bunch, undulator and mesh unchanged), which changes only the sampling noise that seeds the
-    radiation.  Returns (P_sat [n_designs x n_perturb], the spread per design: relative standard
+    only the macro-particle count changed (the bunch's charge, size and energy, the undulator and
+    the mesh unchanged), which changes only the sampling noise that seeds the radiation.  step >= 1:
+    the count moves by that many particles per solve (4 = one beamlet group: the quasi-random
+    sequence keeps its points and gains one group); step < 1: by that fraction per solve, rounded
+    to whole groups (the sequence is then truncated elsewhere, a different sampling of the same
+    bunch).  Returns (P_sat [n_designs x n_perturb], the spread per design: relative standard
     deviation and median relative deviation from the design's mean)."""
     runs = []
     for p in ps:
         for j in range(n_perturb):
             q = dict(p)
-            q["particles"] = int(p["particles"]) + 4 * j
+            if step >= 1:
+                q["particles"] = int(p["particles"]) + int(step) * j
+            else:
+                q["particles"] = 4 * int(round(int(p["particles"]) * (1.0 + step * j) / 4.0))
             q["index"] = len(runs)
             runs.append(q)
     _, _, psat, _, _ = solve_designs(runs, spectrum_points, workdir, device)
@@ -368,6 +375,8 @@ def main(argv=None):
     ap.add_argument("--noise-floor", type=int, default=0, metavar="N",
                     help="measure the solver's P_sat repeatability on N designs and exit")
     ap.add_argument("--perturb", type=int, default=8, help="--noise-floor: solves per design")
+    ap.add_argument("--perturb-step", type=float, default=4,
+                    help="--noise-floor: particles added per solve (>= 1) or fraction of the count (< 1)")
     a = ap.parse_args(argv)
 
     if a.gemm_bench:
@@ -375,8 +384,10 @@ def main(argv=None):
         return
     if a.noise_floor:
         ps = design_parameters(a.noise_floor, a.seed, small=a.small, seeded=a.seeded)
-        P, sd, dev = noise_floor(ps, a.perturb, a.spectrum, tempfile.mkdtemp(prefix="mithra-floor-"))
-        print(json.dumps(dict(designs=a.noise_floor, perturb=a.perturb, small=a.small, seeded=a.seeded,
+        P, sd, dev = noise_floor(ps, a.perturb, a.spectrum, tempfile.mkdtemp(prefix="mithra-floor-"),
+                                 step=a.perturb_step)
+        print(json.dumps(dict(designs=a.noise_floor, perturb=a.perturb, step=a.perturb_step, small=a.small,
+                              seeded=a.seeded,
                               median_rel_sd=float(np.median(sd)), p90_rel_sd=float(np.quantile(sd, 0.9)),
                               median_rel_dev=float(np.median(dev)), p90_rel_dev=float(np.quantile(dev, 0.9)),
                               rel_sd=[float(x) for x in sd], psat=P.tolist())))
