@@ -126,6 +126,10 @@ __device__ __noinline__ double lab_z_outside(double zmin, double dzd, double gam
   return gamma * (zmin + ((double)k + (double)fz) * dzd + tshift);
 }
 
+// The same lab z rounded to float, out of line like lab_z_outside: GB300 converts double to float
+// on its FP64 pipe, and only particles outside the mesh's z range need the conversion.
+__device__ __noinline__ float to_float_outside(double v) { return (float)v; }
+
 // Undulator lz and phase ku*lz reduced modulo 2 pi, from the FP64 lab z (particles outside the mesh).
 __device__ __noinline__ float2 undulator_phase_outside(double labz, double rb, double ku) {
   const double lzd = labz - rb;
@@ -240,7 +244,6 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
       int i, j, k;
       unpack_cell(cell, i, j, k);
       const int Lk = C.N2 - 1;
-      const int kw = ((k % Lk) + Lk) % Lk;  // wrapped cell of pmod(z - zmin, Lz)
       float fx = cur.fx, fy = cur.fy, fz = cur.fz;
       if (save_rnm) { pt.mcell[p] = cell; pt.mfx[p] = fx; pt.mfy[p] = fy; pt.mfz[p] = fz; }
       const float x = C.xmin + ((float)i + fx) * C.dx, y = C.ymin + ((float)j + fy) * C.dy;
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
         // src/solver.cpp:184-185, so it is the first table entry's lz.
         float lz;
         if (k_in) lz = fmaf(C.gdz, fz, table[k].lz + C.rb0_f);
-        else lz = (float)labz_outside;
+        else lz = to_float_outside(labz_outside);
         e = (lz > -C.und0_dist_f) ? 1 : 0;
         pt.e[p] = e;
       } else {
@@ -323,7 +326,11 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
         pt.status[p] = cur.status | 1;
         atomicAdd(&st->nonfinite, 1);
       }
-      // z-face crossing of the wrapped position (src/solver.cpp:1544-1548), in cells.
+      // z-face crossing of the wrapped position (src/solver.cpp:1544-1548), in cells: kw is the
+      // cell of pmod(z - zmin, Lz) before the drift, the particle's own cell inside the mesh (the
+      // integer modulo, tens of instructions, only outside it).
+      const int ko = k - (int)iz;
+      const int kw = (ko >= 0 && ko < Lk) ? ko : ((ko % Lk) + Lk) % Lk;
       const int kwn = kw + (int)iz;
       if (kwn < 0) cross = 1;
       else if (kwn >= Lk) cross = 2;
