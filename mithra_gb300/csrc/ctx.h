@@ -40,6 +40,8 @@ struct Fp32State {
   int* key = nullptr;
   int* rank = nullptr;
   int* block_sums = nullptr;  // 1024 block totals of the bin scan + grand total
+  int* work = nullptr;        // occupied tiles of the last sort (the deposit's work list)
+  int* work_count = nullptr;  // [heavy, light] entries of the list, then the deposit's next entry
   TileGridHost tiles;
   // TMA descriptors of the three A buffers (4D: j, i, k, component): box with halo rows for
   // A^n, box of the tile rows for A^{n-1} and J.

@@ -94,21 +94,27 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_eval_eb_tma(const __grid_co
   __syncthreads();
   if (s_abort) return;  // nothing was issued
   // planes p0 and p0 + 1 (= k_first - 1, k_first) before the first plane computed
+  bool pro_ok = true;  // this thread saw planes p0 and p0 + 1 land
   for (int p = p0; p <= p0 + 1; p++) {
-    if (!mbar_wait(&bar[p % EB_R], parity(p), a.spin_limit)) s_abort = 1;
-    else if (threadIdx.x == 0 && completed == p - 1) completed = p;  // contiguous only
+    if (!mbar_wait(&bar[p % EB_R], parity(p), a.spin_limit)) {
+      s_abort = 1;
+      pro_ok = false;
+    } else if (threadIdx.x == 0 && completed == p - 1) {
+      completed = p;  // contiguous only
+    }
   }
   const float rdt = a.rdt, hx = a.hx, hy = a.hy, hz = a.hz;
   const bool in = i <= a.N0 - 2 && j <= a.N1 - 2;
   const int y = ty + 1, x = tx + 1;  // the node in the boxes
   for (int k = k_first; k <= k_last; k++) {
-    if (!mbar_wait(&bar[(k + 1) % EB_R], parity(k + 1), a.spin_limit))
+    // No barrier after the wait: a thread whose wait gives up skips the plane, and the abort is
+    // seen by all after the end-of-plane barrier.
+    const bool ok = mbar_wait(&bar[(k + 1) % EB_R], parity(k + 1), a.spin_limit);
+    if (!ok)
       s_abort = 1;
     else if (threadIdx.x == 0 && completed == k)
       completed = k + 1;
-    __syncthreads();
-    if (s_abort) break;
-    if (in) {
+    if (ok && pro_ok && in) {
       const int rc = k % EB_R, rm = (k - 1) % EB_R, rp = (k + 1) % EB_R;
       const float(*X0)[TMA_BW] = box(rc, 0);
       const float(*Y0)[TMA_BW] = box(rc, 1);
@@ -142,7 +148,8 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_eval_eb_tma(const __grid_co
       }
     }
     __syncthreads();  // slot of plane k-1 free: the next group may overwrite it
-    if (threadIdx.x == 0 && k + 1 + EB_D + 1 <= p_end && !s_abort) {
+    if (s_abort) break;
+    if (threadIdx.x == 0 && k + 1 + EB_D + 1 <= p_end) {
       issue(k + EB_D + 2);  // slot (k + EB_D + 2) % EB_R = (k - 1) % EB_R
       issued = k + EB_D + 2;
     }

@@ -189,6 +189,9 @@ int fp32_alloc(mithra_ctx* ctx) {
   CK(dalloc(&f.offsets, (size_t)t.n_bins + 1));
   if ((t.n_bins + 1023) / 1024 > 1024) return fail(ctx, MITHRA_ERR_ARG, "mesh too large for the tile sort (%d tiles)", t.n_tiles);
   CK(dalloc(&f.block_sums, 1025));
+  CK(dalloc(&f.work, (size_t)t.n_tiles));
+  CK(dalloc(&f.work_count, 3));
+  CK(cudaMemsetAsync(f.work_count, 0, 3 * sizeof(int), ctx->stream));
   CK(dalloc(&f.key, ctx->capacity));
   CK(dalloc(&f.rank, ctx->capacity));
   CK(cudaFuncSetAttribute(k_deposit_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -208,6 +211,8 @@ void fp32_free(mithra_ctx* ctx) {
   free_particles(f.alt);
   cudaFree(f.counts); cudaFree(f.offsets); cudaFree(f.key); cudaFree(f.rank); cudaFree(f.tma_error);
   cudaFree(f.block_sums);
+  cudaFree(f.work); cudaFree(f.work_count);
+  f.work = f.work_count = nullptr;
   f.counts = f.offsets = f.key = f.rank = f.tma_error = f.block_sums = nullptr;
   f.tma_ready = false;
 }
@@ -358,9 +363,10 @@ int fp32_current(mithra_ctx* ctx) {
     const int r = fp32_sort(ctx);
     if (r) return r;
   }
+  CK(cudaMemsetAsync(f.work_count + 2, 0, sizeof(int), ctx->stream));  // the deposit's next list entry
   return timed(ctx, "deposit", [&] {
-    k_deposit_tiled<<<T.n_tiles + kOutsideBlocks, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
-        D, T, f.pt, f.offsets, ctx->st, J, rho, g.cstride, g.plane, g.P1);
+    k_deposit_tiled<<<ctx->sm_count * kDepositBlocksPerSM, kDepositBlock, 3 * TILE_NODES * sizeof(float), ctx->stream>>>(
+        D, T, f.pt, f.offsets, f.work, f.work_count, f.work_count + 2, ctx->st, J, rho, g.cstride, g.plane, g.P1);
   });
 }
 
@@ -374,7 +380,7 @@ bool fp32_sorts_this_step(const mithra_ctx* ctx) { return ctx->idx[0] == 0; }
 int fp32_unsorted(mithra_ctx* ctx, long long n) {
   const TileGrid T = tile_grid(ctx);
   k_offsets_unsorted<<<(T.n_bins + 1 + 255) / 256, 256, 0, ctx->stream>>>(ctx->f32.offsets, T.n_tiles, T.n_bins,
-                                                                          (int)n);
+                                                                          (int)n, ctx->f32.work_count);
   CK(cudaGetLastError());
   return MITHRA_OK;
 }
@@ -394,6 +400,11 @@ int fp32_sort(mithra_ctx* ctx) {
   if (r) return r;
   r = timed(ctx, "tile_scan_add", [&] {
     k_scan_add<<<nsb, 1024, 0, ctx->stream>>>(f.counts, f.offsets, f.block_sums, T.n_bins, nsb, ctx->st);
+  });
+  if (r) return r;
+  CK(cudaMemsetAsync(f.work_count, 0, 2 * sizeof(int), ctx->stream));
+  r = timed(ctx, "tile_worklist", [&] {
+    k_tile_worklist<<<(T.n_tiles + 255) / 256, 256, 0, ctx->stream>>>(f.offsets, T.n_tiles, f.work, f.work_count);
   });
   if (r) return r;
   r = timed(ctx, "tile_scatter", [&] {

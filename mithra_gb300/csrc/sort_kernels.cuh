@@ -129,11 +129,12 @@ __global__ void __launch_bounds__(1024) k_scan_add(int* counts, int* offsets, co
   }
 }
 
-// Bin offsets before the first sort: every tile empty, all n particles in the bin outside the
-// tiles, no erased ones.
-__global__ void k_offsets_unsorted(int* offsets, int n_tiles, int n_bins, int n) {
+// Bin offsets before the first sort: every tile empty (an empty work list), all n particles in the
+// bin outside the tiles, no erased ones.
+__global__ void k_offsets_unsorted(int* offsets, int n_tiles, int n_bins, int n, int* work_count) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b <= n_bins) offsets[b] = b <= n_tiles ? 0 : n;
+  if (b == 0) work_count[0] = work_count[1] = 0;  // no occupied tile until the first sort
 }
 
 // Pass 3: scatter every particle to its sorted slot in the other buffer set.
@@ -293,37 +294,18 @@ __device__ __forceinline__ void global_both(float* J, long long cs, long long m,
 }
 
 constexpr int kDepositBlock = 128;
-constexpr int kOutsideBlocks = 304;  // blocks for the particles outside the tiles (2 per SM)
+constexpr int kDepositBlocksPerSM = 6;  // persistent deposit blocks per SM (shared copy and registers)
+constexpr int kHeavyTile = 512;         // tiles with this many particles lead the work list
 // Tiles with fewer particles than this skip the shared copy (zeroing and flushing its 1452 chunks
 // costs more than the particles' global atomics).
 constexpr int kSparseTile = 64;
 
-__global__ void __launch_bounds__(kDepositBlock, 6)
-    k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets, StateDev* st, float* J,
-                    float* rho, long long cs, long long plane, int P1) {
-  extern __shared__ float sJ[];  // 3 * TILE_NODES
-  const int b = blockIdx.x;
-  const bool tile_block = b < T.n_tiles;
-  // Blocks past the tiles share the particles that follow the tiles' bins (one block for them
-  // would serialise 10^5 particles): block n_tiles + r takes the particles r * kDepositBlock + t,
-  // stepping by kOutsideBlocks * kDepositBlock.  Those are the bin of particles outside the tiled
-  // cells and, on a step that did not sort, the particles appended since the last sort (they
-  // follow the live particles of the sort, where the bin of erased particles began).
-  const int bin = tile_block ? b : T.bin_outside;
-  const int stride = tile_block ? kDepositBlock : kOutsideBlocks * kDepositBlock;
-  const int beg = offsets[bin] + (tile_block ? 0 : (b - T.n_tiles) * kDepositBlock);
-  const int end = tile_block ? offsets[b + 1] : (int)st->n_particles;
-  if (beg >= end) return;
-  const bool tiled = tile_block && end - beg >= kSparseTile;
-  int i0 = 0, j0 = 0, k0 = 0;
-  if (tiled) {
-    const int ti = b % T.ntx, tj = (b / T.ntx) % T.nty, tk = b / (T.ntx * T.nty);
-    i0 = ti * TX - 1; j0 = tj * TY - JOFF; k0 = tk * TZ - 1;  // halo of one cell below
-    float4* s4 = reinterpret_cast<float4*>(sJ);
-    for (int s = threadIdx.x; s < 3 * TILE_NODES / 4; s += blockDim.x) s4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-  }
-  int kmin = 0x7fffffff, kmax = -0x7fffffff;
+// The deposit of one run of particles: p = beg + threadIdx.x, stepping by `stride`, below `end`.
+// `tiled`: the currents go to the shared tile copy whose node (0, 0, 0) is mesh node (i0, j0, k0)
+// (the block then flushes it to J); otherwise straight to J with global atomics.
+__device__ __forceinline__ void deposit_run(const DepositF32& D, const ParticlesF32& pt, float* sJ, float* J, float* rho,
+                                            long long cs, long long plane, int P1, int beg, int end, int stride,
+                                            bool tiled, int i0, int j0, int k0, int& kmin, int& kmax) {
   const long long sI = P1, sK = plane;
   // The particle data of the next iteration is loaded before the current particle's atomics, so
   // each thread keeps two particles' loads in flight (the loop is bound by global-load latency).
@@ -415,7 +397,6 @@ __global__ void __launch_bounds__(kDepositBlock, 6)
     }
     cur = nxt;
   }
-  slab_update(st, kmin, kmax);
   if (!tiled) return;
   __syncthreads();
   // Flush: the node values of every chunk of four nodes along j, node(n) = edge(n) + edge(n - unit
@@ -463,6 +444,66 @@ __global__ void __launch_bounds__(kDepositBlock, 6)
     for (int u = 0; u < U; u++)
       if (v[u].x != 0.0f || v[u].y != 0.0f || v[u].z != 0.0f || v[u].w != 0.0f)
         atomicAdd(reinterpret_cast<float4*>(Jc + goff[u]), v[u]);
+  }
+}
+
+// The occupied tiles of the last sort are handed out one at a time to persistent blocks (a few per
+// SM), which take the next entry of the work list with one atomic: the heavy tiles (at least
+// kHeavyTile particles) come first, so the light ones even out the blocks' ends, and the empty
+// tiles of the mesh (most of them) cost nothing.  A tile's particles deposit into the shared
+// copy, which is flushed to J; tiles holding fewer than kSparseTile particles deposit with global
+// atomics.  Afterwards every block takes its share of the particles that follow the tiles' bins:
+// the bin outside the tiled cells and, on a step that did not sort, the particles appended since
+// the last sort (they follow the live particles of the sort, where the bin of erased particles
+// began).
+__global__ void __launch_bounds__(kDepositBlock, 6)
+    k_deposit_tiled(DepositF32 D, TileGrid T, ParticlesF32 pt, const int* offsets, const int* work,
+                    const int* work_count, int* work_next, StateDev* st, float* J, float* rho, long long cs,
+                    long long plane, int P1) {
+  extern __shared__ float sJ[];  // 3 * TILE_NODES
+  __shared__ int s_w;
+  int kmin = 0x7fffffff, kmax = -0x7fffffff;
+  const int n_heavy = work_count[0], n_work = work_count[0] + work_count[1];
+  for (;;) {
+    if (threadIdx.x == 0) s_w = atomicAdd(work_next, 1);
+    __syncthreads();
+    const int w = s_w;
+    if (w >= n_work) break;
+    const int b = w < n_heavy ? work[w] : work[T.n_tiles - 1 - (w - n_heavy)];
+    const int beg = offsets[b], end = offsets[b + 1];
+    const bool tiled = end - beg >= kSparseTile;
+    int i0 = 0, j0 = 0, k0 = 0;
+    if (tiled) {
+      const int ti = b % T.ntx, tj = (b / T.ntx) % T.nty, tk = b / (T.ntx * T.nty);
+      i0 = ti * TX - 1; j0 = tj * TY - JOFF; k0 = tk * TZ - 1;  // halo of one cell below
+      float4* s4 = reinterpret_cast<float4*>(sJ);
+      for (int q = threadIdx.x; q < 3 * TILE_NODES / 4; q += blockDim.x) s4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();  // the copy is zeroed, and every thread has read s_w
+    deposit_run(D, pt, sJ, J, rho, cs, plane, P1, beg, end, kDepositBlock, tiled, i0, j0, k0, kmin, kmax);
+    __syncthreads();  // the flush has read the copy the next tile zeroes
+  }
+  deposit_run(D, pt, sJ, J, rho, cs, plane, P1, offsets[T.bin_outside] + (int)blockIdx.x * kDepositBlock,
+              (int)st->n_particles, (int)gridDim.x * kDepositBlock, false, 0, 0, 0, kmin, kmax);
+  slab_update(st, kmin, kmax);
+}
+
+// The work list of the deposit, built after a sort: the occupied tiles, those with at least
+// kHeavyTile particles from the front of `work` (count in work_count[0]), the others from its
+// back (count in work_count[1]); one warp-aggregated atomic per warp and list, counts zeroed by
+// the caller.
+__global__ void __launch_bounds__(256) k_tile_worklist(const int* offsets, int n_tiles, int* work, int* work_count) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = b < n_tiles ? offsets[b + 1] - offsets[b] : 0;
+  const int lane = threadIdx.x & 31;
+  for (int heavy = 0; heavy < 2; heavy++) {
+    const bool take = c > 0 && ((c >= kHeavyTile) == (heavy == 0));
+    const unsigned bal = __ballot_sync(0xffffffffu, take);
+    int base = 0;
+    if (lane == 0 && bal) base = atomicAdd(work_count + heavy, __popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    const int r = base + __popc(bal & ((1u << lane) - 1u));
+    if (take) work[heavy == 0 ? r : n_tiles - 1 - r] = b;
   }
 }
 
