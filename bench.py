@@ -9,6 +9,12 @@ form.  Inputs are seeded synthetic bunches (Halton sequence) built by the refere
 initialisation restated on the host; the field state (3.4 GB) exceeds the 129 MB L2, so no L2
 flush is needed between steps.
 
+The timed window lies in the part of the march where the whole bunch is inside the undulator
+(every particle gathers E and B and feels the undulator field): the march is run from its start
+to 90 % of its steps, then W warm-up and K timed steps follow.  The whole march (start to
+undulator exit) is timed beside it.  The CPU legs start the oracle from a snapshot of the same
+march at the window's first step.
+
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Under torchrun (N > 1) every rank runs an independent replica on its own GPU (the path is a
@@ -38,6 +44,8 @@ WORKLOADS = {
     "fel-98x98x1026": "fel-98x98x1026.job",  # profiling case (about 1 GB on the device)
 }
 METRIC = "cell+particle updates/s"
+# First step of the timed window, as a fraction of the march (see window_start).
+WINDOW_AT = 0.9
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
 
 # Algorithmic bytes per unit (each array element counted once, halo re-reads free).
@@ -73,6 +81,10 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp32-compare", action="store_true",
                     help="with --precision fp64, skip the mixed-form run reported under fp32_form")
+    ap.add_argument("--snapshot-fd", type=int, default=None, help=argparse.SUPPRESS)
+    ap.add_argument("--write-snapshot", default=None, metavar="DIR",
+                    help="write the workload's march state at the timed window's first step (FP64 form) to "
+                         "DIR and exit; `python -m mithra_gb300.snapshot <job> --resume DIR` marches on from it")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -201,21 +213,88 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
-STATE_DIR = os.path.join(REPO, "oracle", "_build", "state")
+def march_steps(setup, ctx) -> int:
+    """Field steps of the march (`while (time_ < mesh_.totalTime_)`, src/solver.cpp:1300) from
+    the context's time, which run_prelude has brought to the march's start."""
+    t, total, dt = ctx.get_time().time, setup.total_time(), setup.meta()["dt"]
+    n = 0
+    while t < total:
+        t += dt
+        n += 1
+    return n
 
 
-def initial_state_dir(jobpath):
-    return os.path.join(STATE_DIR, os.path.splitext(os.path.basename(jobpath))[0])
+def window_start(total: int, warmup: int, steps: int) -> int:
+    """First step of the timed window.  Particles gather E and B and feel the undulator only once
+    they have passed its entrance (the e flag, src/solver.cpp:1509-1514); the bunch of the default
+    workload is wholly inside by 85 % of its march (step 1623 of 1905), so the window starts at 90 %,
+    or earlier if the window and the legs after it would run past the undulator exit."""
+    return max(warmup, min(int(WINDOW_AT * total), total - warmup - 3 * steps - 3))
 
 
-def oracle_run_for(jobpath):
-    """The CPU restatement (oracle/) started from the job's seeded initial state, read from the
-    file that build() (or a child process) wrote: this process does not load the CUDA library."""
-    from oracle import initial_state
+def oracle_run_for(snap_info, snap):
+    """The CPU restatement (oracle/) started from a snapshot of the march."""
     from oracle import pyoracle as po
-    d = initial_state.ensure(jobpath, initial_state_dir(jobpath))
-    m, anp1, an, anm1, parts, solver, order, _ = initial_state.load(d)
-    return po, po.OracleRun(m, an, anm1, anp1, parts, solver=solver, order=order), m
+    a = snap.fields
+    return po, po.OracleRun(snap_info["meta"], a[1], a[2], a[0], snap.particles, solver=snap_info["solver"],
+                            order=snap_info["order"])
+
+
+def window_snapshot_child(args, jobpath):
+    """(info, snapshot) of the job at the window's first step, marched by the FP64 form in a child
+    process (this process never loads the CUDA library) and streamed back through a pipe."""
+    from mithra_gb300 import snapshot
+    r, w = os.pipe()
+    cmd = [sys.executable, os.path.abspath(__file__), "--snapshot-fd", str(w), "--workload", args.workload,
+           "--steps", str(args.steps), "--warmup", str(args.warmup)]
+    p = subprocess.Popen(cmd, cwd=REPO, pass_fds=(w,), stdout=sys.stderr)
+    os.close(w)
+    try:
+        with os.fdopen(r, "rb") as f:
+            info, snap = snapshot.read_stream(f)
+    finally:
+        rc = p.wait()
+    if rc != 0:
+        raise RuntimeError("window snapshot process exited with status %d" % rc)
+    return info, snap
+
+
+def write_window_snapshot(args):
+    """--snapshot-fd / --write-snapshot: march the workload (FP64 form) to the window's first step
+    and stream the snapshot to the descriptor or write it to the directory."""
+    import mithra_gb300 as mg
+    from mithra_gb300 import snapshot
+    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
+    setup = mg.Setup.from_job(jobpath)
+    with mg.Context.from_setup(setup, mg.FP64) as ctx:
+        ctx.run_prelude()
+        start = window_start(march_steps(setup, ctx), args.warmup, args.steps)
+        ctx.run(start)
+        snap = snapshot.take(ctx)
+    if args.write_snapshot:
+        snapshot.save(snap, args.write_snapshot, jobpath, setup, start)
+        return
+    with os.fdopen(args.snapshot_fd, "wb") as f:
+        snapshot.write_stream(snap, f, jobpath, setup, start)
+
+
+def snapshot_info(setup, jobpath, snap, step):
+    from mithra_gb300 import snapshot
+    return snapshot._info(snap, jobpath, setup, step)
+
+
+def touched_nodes(parts, meta) -> int:
+    """Mesh nodes whose E and B the particles' gathers read: the 8 corners of each occupied cell
+    (x index i < N0, y index j < N1, z plane k < np)."""
+    lo = np.array([meta["xmin"], meta["ymin"], meta["zmin"]])
+    h = np.array([meta["dx"], meta["dy"], meta["dz"]])
+    ext = np.array([int(meta["N0"]), int(meta["N1"]), int(meta["np"])], dtype=np.int64)
+    c = np.floor((parts[:, 1:4] - lo) / h).astype(np.int64)
+    c = c[np.all((c >= 0) & (c < ext - 1), axis=1)]
+    cells = np.unique((c[:, 2] * ext[1] + c[:, 1]) * ext[0] + c[:, 0])
+    i, j, k = cells % ext[0], (cells // ext[0]) % ext[1], cells // (ext[0] * ext[1])
+    corners = [((k + dk) * ext[1] + j + dj) * ext[0] + i + di for dk in (0, 1) for dj in (0, 1) for di in (0, 1)]
+    return int(np.unique(np.concatenate(corners)).size)
 
 
 def units_per_step(meta, n_particles):
@@ -266,28 +345,34 @@ def time_oracle(run, po, threads, min_seconds, max_steps):
     return steps, el
 
 
-def cpu_baseline(jobpath, sample_seconds):
-    po, run, m = oracle_run_for(jobpath)
+def cpu_baseline(snap_info, snap, sample_seconds):
+    po, run = oracle_run_for(snap_info, snap)
     threads = cpu_threads()
-    nodes, pushes, _ = units_per_step(m, run.n)
+    nodes, pushes, _ = units_per_step(snap_info["meta"], run.n)
     po.set_threads(threads)
     run.step()  # first-touch of the arrays
     steps, el = time_oracle(run, po, threads, sample_seconds, 200)
     return {"value": (nodes + pushes) * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": "%d field steps of the same job (after one untimed step), C restatement of the "
-                      "reference with OpenMP over %d host threads, %.1f s" % (steps, threads, el)}
+            "sample": "%d field steps from step %d of the same march (after one untimed step; the "
+                      "bench window's part of the march, every particle inside the undulator), C "
+                      "restatement of the reference with OpenMP over %d host threads, %.1f s"
+                      % (steps, snap_info["step"], threads, el)}
 
 
 def run_reference(args, dist):
     """The reference algorithm on the host cores: the oracle's C restatement (pinned bit for bit
     to the reference in the container that has the reference tree; that tree is not on the GPU
-    host, so its binary cannot be built here), all host threads, then one thread."""
+    host, so its binary cannot be built here), all host threads, then one thread.  It starts from
+    the march state at the window's first step, which a child process computes with the FP64
+    form (this process loads no CUDA library): the CPU would take about 15 minutes to march there."""
     jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
     if dist.rank != 0:
         return
-    po, run, m = oracle_run_for(jobpath)
+    info, snap = window_snapshot_child(args, jobpath)
+    po, run = oracle_run_for(info, snap)
+    del snap
     threads = cpu_threads()
-    nodes, pushes, nsub = units_per_step(m, run.n)
+    nodes, pushes, nsub = units_per_step(info["meta"], run.n)
     po.set_threads(threads)
     for _ in range(args.warmup):
         run.step()
@@ -300,16 +385,21 @@ def run_reference(args, dist):
     s1, el1 = time_oracle(run, po, 1, args.cpu_sample_seconds, 3)
     po.set_threads(1)
     v1 = (nodes + pushes) * s1 / el1
+    entered = float(np.mean(run.particles[:, 10] > 0.5))
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Halton bunch of the job file)",
         "config": run_config(args.workload, nodes, run.n, nsub, "fp64", dist.world),
+        "window": {"first_step": info["step"] + args.warmup, "steps": args.steps, "entered_fraction": entered,
+                   "how": "the march state of step %d (FP64 form on the GPU, in a child process, streamed "
+                          "through a pipe), W warm-up and K timed steps on the host" % info["step"]},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
-                         "sample": "%d timed field steps after %d warm-up steps, C restatement of the reference "
-                                   "(oracle/) with OpenMP over %d host threads, one process (the reference's "
-                                   "MPI decomposition is not used: a single domain)" % (args.steps, args.warmup, threads)},
+                         "sample": "%d timed field steps after %d warm-up steps from step %d of the march, C "
+                                   "restatement of the reference (oracle/) with OpenMP over %d host threads, one "
+                                   "process (the reference's MPI decomposition is not used: a single domain)"
+                                   % (args.steps, args.warmup, info["step"], threads)},
         "one_thread": {"value": v1, "unit": METRIC, "cores": 1, "threads": 1, "ms_per_step": 1e3 * el1 / s1,
                        "sample": "%d further field steps of the same march on one thread" % s1,
                        "threads_speedup": value / v1},
@@ -319,14 +409,31 @@ def run_reference(args, dist):
     print(json.dumps(out), flush=True)
 
 
-def measure_form(mg, setup, prec_name, args, dist, units, interior, clocks=True):
-    """One precision form on the workload: K timed graph-replayed steps (CUDA events on the context
-    stream), the per-kernel breakdown and roofline of an instrumented pass over K more steps, and
-    the end-to-end rate through the public API with host buffers."""
+def measure_form(mg, setup, prec_name, args, dist, units, interior, keep_snapshot=False):
+    """One precision form on the workload, march order:
+
+    steps 0..W        untimed (every step graph captured)
+    steps W..S        timed: the entry phase of the march
+    step S            snapshot of the state into page-locked host memory
+    S..S+W            warm-up at the window
+    S+W..S+W+K        timed: the headline window (CUDA events on the context stream)
+    S+W+K..S+W+2K     per-kernel times (each kernel bracketed by CUDA events)
+    e2e               the step-S snapshot uploaded from host memory, K steps, power rows read
+    S+K..exit         timed: the rest of the march
+
+    The whole march's device time is the timed parts plus steps 0..W at the entry phase's rate
+    and S..S+K at the window's."""
+    from mithra_gb300 import snapshot
     prec = mg.FP64 if prec_name == "fp64" else mg.FP32
     ctx = mg.Context.from_setup(setup, prec, device=dist.local)
     n_part = ctx.particle_count()
     ctx.run_prelude()
+    total = march_steps(setup, ctx)
+    start = window_start(total, args.warmup, args.steps)
+    ctx.run(args.warmup)
+    ms_entry = ctx.run_timed(start - args.warmup)
+    snap = snapshot.take(ctx, pinned=True)
+    entered = float(np.mean(snap.particles[:, 10] > 0.5))
     ctx.run(args.warmup)
     ctx.synchronize()
     dist.barrier()
@@ -336,6 +443,10 @@ def measure_form(mg, setup, prec_name, args, dist, units, interior, clocks=True)
     ms_max = dist.max(ms)
     out = {"ms_total": ms_max, "ms_per_step": ms_max / args.steps,
            "value": dist.world * units * args.steps / (ms_max / 1e3), "clocks": clk.summary()}
+    window = {"first_step": start + args.warmup, "steps": args.steps, "march_steps": total,
+              "entered_fraction": entered,
+              "how": "K timed steps after W warm-up steps from step %d of the %d-step march, where "
+                     "%.4f of the particles are inside the undulator" % (start, total, entered)}
 
     # Per-kernel device times: the same K steps again, each kernel bracketed by CUDA events on
     # the context stream (direct launches instead of the step graph).
@@ -346,60 +457,78 @@ def measure_form(mg, setup, prec_name, args, dist, units, interior, clocks=True)
     total_k = sum(v[0] for v in kt.values())
     dominant = max(kt.items(), key=lambda kv: kv[1][0])[0]
     dom_ms, dom_launches = kt[dominant]
-    unit_count = n_part if dominant in ("push", "deposit", "erase", "tile_scatter") else interior
-    per_unit = ALGO_BYTES[prec_name].get(dominant)
+    particle_kernels = ("push", "deposit", "erase", "tile_scatter")
+    unit_count = n_part if dominant in particle_kernels else interior
+    # the push's gathers read E and B (two float triples, 24 B) of every node around an occupied
+    # cell once per launch
+    gather = touched_nodes(snap.particles, setup.meta()) if entered > 0.0 else 0
+    window["gather_nodes"] = gather
+
+    def algo_bytes(k, count):
+        pu = ALGO_BYTES[prec_name].get(k)
+        if not pu:
+            return None
+        return pu * count + (24 * gather if k == "push" else 0)
+
     peak, peak_kind = measured_peaks()
     roof = None
-    if per_unit:
+    ab = algo_bytes(dominant, unit_count)
+    if ab:
         avg_s = dom_ms / dom_launches / 1e3
-        achieved = per_unit * unit_count / avg_s / 1e9
+        achieved = ab / avg_s / 1e9
         tr = traffic_table().get(prec_name, {}).get(dominant)
         roof = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": per_unit * unit_count,
+                "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": ab,
                 "traffic": (tr * unit_count if tr else None),
                 "avg_launch_ms": dom_ms / dom_launches, "share": dom_ms / total_k}
     out["roofline"] = roof
     out["dominant"] = (dominant, dom_ms / dom_launches, unit_count)
     out["kernels"] = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k}
                       for k, v in kt.items()}
-    # per-kernel HBM fractions for the kernels with an algorithmic byte count
     for k, v in out["kernels"].items():
-        pu = ALGO_BYTES[prec_name].get(k)
-        if pu:
-            cnt = n_part if k in ("push", "deposit", "erase") else interior
-            v["hbm_frac"] = pu * cnt / (v["ms_per_launch"] / 1e3) / 1e9 / peak
+        ab = algo_bytes(k, n_part if k in particle_kernels else interior)
+        if ab:
+            v["hbm_frac"] = ab / (v["ms_per_launch"] / 1e3) / 1e9 / peak
 
-    # End to end through the public API with host buffers: upload the initial state from pinned
-    # host memory, march K steps, read the power rows back.
+    # End to end through the public API with host buffers: the step-S state uploaded from
+    # page-locked host memory (a resumed march), K steps, the power rows read back.
     e2e = None
     if not args.no_e2e:
-        anp1, an, anm1 = setup.fields()
-        parts = setup.particles()
-        bufs = [mg.PinnedArray(anp1.shape), mg.PinnedArray(an.shape), mg.PinnedArray(anm1.shape),
-                mg.PinnedArray(parts.shape)]
-        for b, src in zip(bufs, (anp1, an, anm1, parts)):
-            b.array[...] = src
-        t0_state = setup.time()
-        h2d = sum(b.array.nbytes for b in bufs)
         dist.barrier()
         t0 = time.perf_counter()
-        ctx.upload_fields(bufs[0].array, bufs[1].array, bufs[2].array)
-        ctx.upload_particles(bufs[3].array)
-        ctx.set_time(t0_state)
+        snapshot.restore(ctx, snap)
         ctx.run(args.steps)
         rows = ctx.power_rows()
-        el = time.perf_counter() - t0
-        el = dist.max(el)
+        el = dist.max(time.perf_counter() - t0)
         e2e = {"value": dist.world * units * args.steps / el, "unit": METRIC,
-               "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": rows.nbytes / args.steps,
-               "ms_per_step": 1e3 * el / args.steps}
-        for b in bufs:
-            b.free()
+               "h2d_bytes_per_step": snap.nbytes / args.steps, "d2h_bytes_per_step": rows.nbytes / args.steps,
+               "ms_per_step": 1e3 * el / args.steps,
+               "how": "march state of step %d (fields, particles, time) uploaded from page-locked host "
+                      "memory, K steps, power rows read back" % start}
+        rest_from = start + args.steps
+    else:
+        rest_from = start + args.warmup + 2 * args.steps
+    ms_rest = ctx.run_timed(total - rest_from) if total > rest_from else 0.0
+    march_ms = (args.warmup * ms_entry / max(start - args.warmup, 1) + ms_entry
+                + (rest_from - start) * ms / args.steps + ms_rest)
+    window["march"] = {"steps": total, "device_s": march_ms / 1e3,
+                       "value": dist.world * units * total / (march_ms / 1e3), "unit": METRIC,
+                       "entry_phase_ms_per_step": ms_entry / max(start - args.warmup, 1),
+                       "rest_ms_per_step": ms_rest / max(total - rest_from, 1),
+                       "how": "device time of the whole march from its start to the undulator exit: steps "
+                              "%d..%d and %d..%d timed, the %d steps before and the %d at the window at "
+                              "their phase's rate" % (args.warmup, start, rest_from, total, args.warmup,
+                                                      rest_from - start)}
+    out["window"] = window
     out["e2e"] = e2e
     out["launches"] = ctx.launches_per_step() * args.steps
     out["n_part"] = n_part
     ctx.close()
+    if keep_snapshot:
+        out["snapshot"] = (snapshot_info(setup, os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload]),
+                                         snap, start), snap)
+    else:
+        snap.free()
     return out
 
 
@@ -448,9 +577,17 @@ def run_gpu(args, dist):
     n_part = setup.particles().shape[0]
     nodes, pushes, nsub = units_per_step(meta, n_part)
     units = nodes + pushes
-    main = measure_form(mg, setup, args.precision, args, dist, units, interior)
+    want_cpu = dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline
+    main = measure_form(mg, setup, args.precision, args, dist, units, interior, keep_snapshot=want_cpu)
     ms_max = main["ms_total"]
     value = main["value"]
+    cpu = None
+    if want_cpu:  # the oracle from the same march state as the window, on the host cores
+        info, snap = main.pop("snapshot")
+        try:
+            cpu = cpu_baseline(info, snap, args.cpu_sample_seconds)
+        finally:
+            snap.free()
 
     # The FP64 form is bound by GB300's FP64 pipe, not by HBM: its dominant kernel is also placed
     # against the FP64 rate measured on this device (FLOPs per unit counted by ncu on the
@@ -472,7 +609,8 @@ def run_gpu(args, dist):
         f = measure_form(mg, setup, "fp32", args, dist, units, interior)
         fp32_form = {"value": f["value"], "unit": METRIC, "ms_per_step": f["ms_per_step"],
                      "speedup_vs_fp64": f["value"] / value, "roofline": f["roofline"], "kernels": f["kernels"],
-                     "e2e": f["e2e"], "clocks": f["clocks"], "gpu_launches": f["launches"]}
+                     "e2e": f["e2e"], "clocks": f["clocks"], "gpu_launches": f["launches"], "window": f["window"],
+                     "march_speedup_vs_fp64": f["window"]["march"]["value"] / main["window"]["march"]["value"]}
 
     runs = None
     if args.workload == "fel-130x130x2050" and args.sweep_leg_designs > 0:
@@ -480,9 +618,6 @@ def run_gpu(args, dist):
 
     if dist.rank != 0:
         return
-    cpu = None
-    if dist.world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(jobpath, args.cpu_sample_seconds)
     out = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -491,6 +626,7 @@ def run_gpu(args, dist):
         "config": run_config(args.workload, nodes, n_part, nsub, args.precision, dist.world),
         "cell_updates_per_s": dist.world * nodes * args.steps / (ms_max / 1e3),
         "particle_pushes_per_s": dist.world * pushes * args.steps / (ms_max / 1e3),
+        "window": main["window"],
         "roofline": main["roofline"],
         "fp64_pipe": fp64_pipe,
         "fp32_form": fp32_form,
@@ -574,6 +710,9 @@ def run_sweep(args, dist):
 
 def main():
     args = parse_args()
+    if args.snapshot_fd is not None or args.write_snapshot:
+        write_window_snapshot(args)
+        return
     dist = Dist(args.gpus)
     try:
         if args.impl == "reference":

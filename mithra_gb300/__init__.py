@@ -217,6 +217,11 @@ def probe_fp64_tflops(device: int = 0) -> float:
     return float(out[0])
 
 
+def _check_out(a, n):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or a.size != n or not a.flags.c_contiguous:
+        raise MithraError("output buffer must be a C-contiguous float64 array of %d elements" % n)
+
+
 class PinnedArray:
     """A page-locked host buffer (cudaMallocHost) exposed as a numpy array."""
 
@@ -623,9 +628,13 @@ class Context:
         a, b, c = conv(anp1), conv(an), conv(anm1)
         self.call("mithra_gpu_upload_fields", dptr(a), dptr(b), dptr(c))
 
-    def download_fields(self):
+    def download_fields(self, out=None):
+        """(anp1_, an_, anm1_) as FP64 arrays of nodes x 3; `out`: three such arrays to fill
+        (pinned host buffers, say)."""
         n = self.nodes * 3
-        anp1, an, anm1 = np.empty(n), np.empty(n), np.empty(n)
+        anp1, an, anm1 = out if out is not None else (np.empty(n), np.empty(n), np.empty(n))
+        for a in (anp1, an, anm1):
+            _check_out(a, n)
         self.call("mithra_gpu_download_fields", dptr(anp1), dptr(an), dptr(anm1))
         return anp1, an, anm1
 
@@ -633,9 +642,11 @@ class Context:
         conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
         self.call("mithra_gpu_upload_scalar", dptr(conv(fnp1)), dptr(conv(fn)), dptr(conv(fnm1)))
 
-    def download_scalar(self):
+    def download_scalar(self, out=None):
         n = self.nodes
-        a, b, c = np.empty(n), np.empty(n), np.empty(n)
+        a, b, c = out if out is not None else (np.empty(n), np.empty(n), np.empty(n))
+        for x in (a, b, c):
+            _check_out(x, n)
         self.call("mithra_gpu_download_scalar", dptr(a), dptr(b), dptr(c))
         return a, b, c
 
@@ -654,9 +665,16 @@ class Context:
         self.call("mithra_gpu_particle_count", C.byref(n))
         return n.value
 
-    def download_particles(self) -> np.ndarray:
+    def download_particles(self, out=None) -> np.ndarray:
+        """The particle records (rows of 11 doubles); `out`: an array of at least
+        particle_count() such rows to fill.  Returns the filled rows."""
         cap = self.particle_count()
-        out = np.zeros((max(cap, 1), 11))
+        if out is None:
+            out = np.zeros((max(cap, 1), 11))
+        elif out.dtype != np.float64 or out.ndim != 2 or out.shape[1] != 11 or out.shape[0] < cap \
+                or not out.flags.c_contiguous:
+            raise MithraError("download_particles: out must be a C-contiguous float64 array of at least "
+                              "%d x 11" % cap)
         n = C.c_size_t()
         self.call("mithra_gpu_download_particles", dptr(out), cap, C.byref(n))
         return out[: n.value]
