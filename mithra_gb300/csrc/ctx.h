@@ -35,6 +35,10 @@ struct Fp32State {
   ParticlesF32 pt{};
   ParticlesF32 alt{};  // second buffer set: the tile sort scatters into it, then the two swap
   int parity = 0;      // which of the two sets is current (flips at every sort)
+  // Particles uploaded since the last sort: the next step sorts whatever its rotation (run
+  // directly, outside the step graphs), so that a resumed march does not push and deposit
+  // unsorted particles until the next step of the sort's rotation.
+  bool sort_pending = false;
   int* counts = nullptr;
   int* offsets = nullptr;
   int* key = nullptr;
@@ -73,8 +77,8 @@ struct mithra_ctx {
   double* Jedge = nullptr;  // FP64 form: current of the deposit in edge form (k_deposit_fp64)
   mithra::ParticlesDev<double> pt{};
   mithra::Fp32State f32{};
-  float* E = nullptr;  // mixed form: E and B, 3 components, cstride apart
-  float* B = nullptr;
+  float* E = nullptr;  // mixed form: E and B as node records {E, 0, B, 0} (kEBNode floats per node)
+  float* B = nullptr;  // unused (B of node m is E[kEBNode m + 4 + c])
   double* E64 = nullptr;  // FP64 form: E and B as doubles holding float-rounded values
   double* B64 = nullptr;
   uint8_t* plane_needed = nullptr;  // N2 flags: planes read by a power sample

@@ -71,11 +71,22 @@ struct UndDev {
   int has_prev, has_next;
   // FP32 copies for the mixed form.
   float ct_f, st_f, ku_f, b0_f, ul_f, r0_prev_f, r0_next_f;
+  double kgdz;  // ku * gamma * dz: the phase advance across one cell along z
+};
+
+// FP64 form: a static module's lz and the sine and cosine of its phase ku*lz on node plane k,
+// for the bunch time of one substep (k_undulator_table64).
+struct UndPlane64 {
+  double lz, s, c;
 };
 
 struct PushDev {
   double dtb, r1, r2, gamma, beta, c0, dt_shift, bunch_time_step;
   double inv_r2;  // 1 / r2
+  // FP64 form: per-plane undulator phases (UndPlane64, n_und x (N2 + 1)), or null where the
+  // phase advance across a cell is too large for the short series of the push.
+  const UndPlane64* und_planes;
+  double gdz;     // gamma * dz
   int n_und;
   double und0_dist;
   // Laser beams acting on the particles: optical undulators (indexed by UndDev::beam) and,
@@ -177,6 +188,20 @@ struct PowerDev {
   long long row_cap;
 };
 
+// E and B of the mixed form are stored node by node: node m holds the 32-byte record
+// {Ex, Ey, Ez, 0, Bx, By, Bz, 0} at EB + 8 m.  A particle's gather reads each of its 8 nodes with
+// two 16-byte loads from one 32-byte sector (component planes would take 6 sectors per node), and
+// the evaluation writes a node with two 16-byte stores.  Component c of node m: E at
+// EB[8 m + c], B at EB[8 m + 4 + c].
+constexpr int kEBNode = 8;
+
+__device__ __forceinline__ void store_eb(float* EB, long long m, float e0, float e1, float e2, float b0, float b1,
+                                         float b2) {
+  float4* p = reinterpret_cast<float4*>(EB + (long long)kEBNode * m);
+  p[0] = make_float4(e0, e1, e2, 0.0f);
+  p[1] = make_float4(b0, b1, b2, 0.0f);
+}
+
 // True when node plane k has to be evaluated: inside the particle slab (with two cells of margin
 // for the motion during the step) or read by a power sample.
 __device__ __forceinline__ bool eb_plane_wanted(int k, const StateDev* st, const uint8_t* planes, int N2) {
@@ -254,6 +279,71 @@ __host__ __device__ __forceinline__ double to_double(float f) {
   if ((b & 0x7fffffffu) == 0u) return double_of((unsigned long long)(b & 0x80000000u) << 32);  // +-0
   return (double)f;
 }
+
+// Comparisons, floors and truncations of doubles on the integer pipes, for the FP64 kernels that
+// GB300's FP64 rate bounds: a DSETP, DMNMX, FRND or F2I takes an FP64 issue slot, a few integer
+// instructions do not.  All are exact.
+//
+// dkey: a 64-bit integer that orders as the double does (not NaN; -0 and +0 equal):
+// a < b exactly when dkey(a) < dkey(b).
+__host__ __device__ __forceinline__ long long dkey(double x) {
+  const long long b = (long long)bits_of(x);
+  const long long s = b >> 63;  // -1 for negative, else 0
+  return (b ^ (s & 0x7fffffffffffffffLL)) - s;
+}
+
+// floor(t) as an int for |t| < 2^31, from the bits of t (negative t, rare in the callers, takes
+// the hardware path).
+__host__ __device__ __forceinline__ int ifloor_d(double t) {
+  const long long b = (long long)bits_of(t);
+  if (b < 0) return (int)floor(t);
+  const int e = (int)(b >> 52) - 1023;
+  if (e < 0) return 0;
+  const long long m = (b & 0xfffffffffffffLL) | 0x10000000000000LL;
+  return (int)(m >> (52 - e));
+}
+
+// modf for |t| < 2^31: returns t - trunc(t) and stores trunc(t), formed by clearing the fraction
+// bits of t (one FP64 subtraction, exact; an integral t gives +0 where modf gives a signed zero).
+__host__ __device__ __forceinline__ double modf_d(double t, double* ip) {
+  const long long b = (long long)bits_of(t);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  long long tb;
+  if (e < 0) tb = b & (long long)0x8000000000000000ULL;  // |t| < 1: trunc(t) = +-0
+  else if (e >= 52) tb = b;                                // already integral
+  else tb = b & ~((1LL << (52 - e)) - 1);
+  const double tr = double_of((unsigned long long)tb);
+  *ip = tr;
+  return t - tr;
+}
+
+// trunc(t) as an int for |t| < 2^31 and the bits of trunc(t) from modf_d (no FP64 conversion).
+__host__ __device__ __forceinline__ int itrunc_d(double tr) {
+  const long long b = (long long)bits_of(tr);
+  const int e = (int)((b >> 52) & 0x7ff) - 1023;
+  if (e < 0) return 0;
+  const int mag = (int)(((b & 0xfffffffffffffLL) | 0x10000000000000LL) >> (52 - e));
+  return b < 0 ? -mag : mag;
+}
+
+// (double)n for an int, exactly, from the bits (no FP64 conversion).
+__host__ __device__ __forceinline__ double double_of_int(int n) {
+  if (n == 0) return 0.0;
+  const unsigned long long sign = n < 0 ? 0x8000000000000000ULL : 0ULL;
+  const unsigned mag = n < 0 ? 0u - (unsigned)n : (unsigned)n;
+#ifdef __CUDA_ARCH__
+  const int top = 31 - __clz(mag);
+#else
+  const int top = 31 - __builtin_clz(mag);
+#endif
+  const unsigned long long m = ((unsigned long long)mag << (52 - top)) & 0xfffffffffffffULL;
+  return double_of(sign | ((unsigned long long)(1023 + top) << 52) | m);
+}
+
+// The smaller / larger of two doubles (not NaN) by their integer keys (fmin / fmax up to the
+// sign of a zero result).
+__host__ __device__ __forceinline__ double dmin_k(double a, double b) { return dkey(b) < dkey(a) ? b : a; }
+__host__ __device__ __forceinline__ double dmax_k(double a, double b) { return dkey(a) < dkey(b) ? b : a; }
 
 // pmod, src/stdinclude.cpp:88-93.
 __device__ __forceinline__ double pmod_d(double a, double b) {

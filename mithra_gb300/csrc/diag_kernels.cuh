@@ -217,10 +217,12 @@ __global__ void k_diag_finish(const double2* partial, int nblocks, int nv, doubl
 }
 
 // FdTd::fieldSample (src/fdtd.cpp:851-950): E, B and A^n at each point, trilinear with the
-// reference's weights (modf of the cell coordinate); out[9 p + 0..8] = E, B, A.
+// reference's weights (modf of the cell coordinate); out[9 p + 0..8] = E, B, A.  Component c of
+// node m of E (B) is E[c * ecs + m * ens] (see k_power_sample); A is in component planes.
 template <typename TE, typename TA>
-__global__ void k_field_sample(GridDev g, const TE* __restrict__ E, const TE* __restrict__ B, const TA* __restrict__ A,
-                               const double* __restrict__ pts, int n, double* __restrict__ out) {
+__global__ void k_field_sample(GridDev g, const TE* __restrict__ E, const TE* __restrict__ B, long long ecs, int ens,
+                               const TA* __restrict__ A, const double* __restrict__ pts, int n,
+                               double* __restrict__ out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const double* r = pts + 3 * p;
@@ -242,8 +244,8 @@ __global__ void k_field_sample(GridDev g, const TE* __restrict__ E, const TE* __
   for (int comp = 0; comp < 3; comp++) {
     double e = 0.0, b = 0.0, a = 0.0;
     for (int q = 0; q < 8; q++) {
-      e += w[q] * (double)E[comp * cs + nd[q]];
-      b += w[q] * (double)B[comp * cs + nd[q]];
+      e += w[q] * (double)E[comp * ecs + nd[q] * ens];
+      b += w[q] * (double)B[comp * ecs + nd[q] * ens];
       a += w[q] * (double)A[comp * cs + nd[q]];
     }
     o[comp] = e; o[3 + comp] = b; o[6 + comp] = a;

@@ -7,8 +7,8 @@
 // (three components of A^n and of A^{n+1}, boxes of the interior stencil's A^n tensor map: the
 // tile plus its halo) is brought into shared memory once by cp.async.bulk.tensor, in a ring of
 // EB_R plane slots kept EB_D planes ahead of the plane computed, so A is read from HBM once per
-// slab (plus the thin halos) and E, B are written with coalesced row stores: 24 + 24 bytes per
-// node, the 48 B/node of the roofline.
+// slab (plus the thin halos) and E, B are written as the node records of the mixed form (two
+// 16-byte stores per node, 32 bytes of which 24 carry E and B).
 //
 // Waits are bounded, as in the interior stencil: a CTA whose barrier does not complete records
 // the failure in the error word, waits (with the default limit) for the copy groups it issued
@@ -26,10 +26,9 @@ constexpr int EB_PLANE = 6 * EB_BOX_SLOT;       // X, Y, Z of A^n then of A^{n+1
 constexpr size_t kEbTmaSmem = (size_t)EB_R * EB_PLANE + 128;
 
 struct EbTmaArgs {
-  float* E;
-  float* B;
+  float* EB;  // node records {E, 0, B, 0} (store_eb)
   int N0, N1, N2, P1;
-  long long plane, cstride;
+  long long plane;
   float rdt, hx, hy, hz;
   int ks;                 // planes per slab
   const StateDev* st;     // particle slab (k_lo, k_hi); null: every plane
@@ -132,20 +131,10 @@ __global__ void __launch_bounds__(TMA_TJ * TMA_TI) k_eval_eb_tma(const __grid_co
                        ((Z0[y + 1][x] + Z1[y + 1][x]) - (Z0[y - 1][x] + Z1[y - 1][x])) * hx;
       const float b2 = ((Y0[y + 1][x] + Y1[y + 1][x]) - (Y0[y - 1][x] + Y1[y - 1][x])) * hx -
                        ((X0[y][x + 1] + X1[y][x + 1]) - (X0[y][x - 1] + X1[y][x - 1])) * hy;
-      const long long cs = a.cstride;
       const long long m = (long long)k * a.plane + (long long)i * a.P1 + j;
-      a.E[m] = e0; a.E[cs + m] = e1; a.E[2 * cs + m] = e2;
-      a.B[m] = b0; a.B[cs + m] = b1; a.B[2 * cs + m] = b2;
-      if (k == 1) {  // plane 0 is a copy of plane 1 (src/fdtd.cpp:755-772)
-        const long long q = m - a.plane;
-        a.E[q] = e0; a.E[cs + q] = e1; a.E[2 * cs + q] = e2;
-        a.B[q] = b0; a.B[cs + q] = b1; a.B[2 * cs + q] = b2;
-      }
-      if (k == a.N2 - 2) {
-        const long long q = m + a.plane;
-        a.E[q] = e0; a.E[cs + q] = e1; a.E[2 * cs + q] = e2;
-        a.B[q] = b0; a.B[cs + q] = b1; a.B[2 * cs + q] = b2;
-      }
+      store_eb(a.EB, m, e0, e1, e2, b0, b1, b2);
+      if (k == 1) store_eb(a.EB, m - a.plane, e0, e1, e2, b0, b1, b2);  // plane 0 copies plane 1 (src/fdtd.cpp:755-772)
+      if (k == a.N2 - 2) store_eb(a.EB, m + a.plane, e0, e1, e2, b0, b1, b2);
     }
     __syncthreads();  // slot of plane k-1 free: the next group may overwrite it
     if (s_abort) break;

@@ -287,6 +287,20 @@ __global__ void k_aos_to_soa(GridDev g, const Thost* __restrict__ src, Tdev* __r
   }
 }
 
+// E or B (off = 0 or 4) of every node as records of 3 floats in the reference's node order
+// (mithra_gpu_download_eb).
+static __global__ void k_eb_to_aos(GridDev g, const float* __restrict__ EB, int off, float* __restrict__ dst) {
+  const long long total = (long long)g.N0 * g.N1 * g.N2;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(r % g.N1);
+    const long long ki = r / g.N1;
+    const int i = (int)(ki % g.N0), k = (int)(ki / g.N0);
+    const float* src = EB + (long long)kEBNode * node_index(g, k, i, j) + off;
+    for (int c = 0; c < 3; c++) dst[r * 3 + c] = src[c];
+  }
+}
+
 template <typename Tdev, typename Thost>
 __global__ void k_soa_to_aos(GridDev g, const Tdev* __restrict__ src, Thost* __restrict__ dst, int ncomp) {
   const long long total = (long long)g.N0 * g.N1 * g.N2;

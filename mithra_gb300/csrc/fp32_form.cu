@@ -257,8 +257,8 @@ int fp32_eval_eb(mithra_ctx* ctx, bool full) {
     // Bulk-tensor z-slabs over the planes the particles occupy (every plane when `full`), then
     // the power-sampling planes outside them.
     EbTmaArgs a;
-    a.E = ctx->E; a.B = ctx->B;
-    a.N0 = g.N0; a.N1 = g.N1; a.N2 = g.N2; a.P1 = g.P1; a.plane = g.plane; a.cstride = g.cstride;
+    a.EB = ctx->E;
+    a.N0 = g.N0; a.N1 = g.N1; a.N2 = g.N2; a.P1 = g.P1; a.plane = g.plane;
     a.rdt = c.rdt; a.hx = c.hx; a.hy = c.hy; a.hz = c.hz;
     a.ks = ctx->tune.slab_planes;
     a.st = full ? nullptr : ctx->st;
@@ -277,7 +277,7 @@ int fp32_eval_eb(mithra_ctx* ctx, bool full) {
     const int by = 256 / bx;
     dim3 pblk(bx, by), pgrd((g.N1 - 2 + bx - 1) / bx, (g.N0 - 2 + by - 1) / by, ctx->n_eb_planes);
     return timed(ctx, "eval_eb_planes", [&] {
-      k_eval_eb_planes_f32<<<pgrd, pblk, 0, ctx->stream>>>(g, c, f.A[ctx->idx[0]], f.A[ctx->idx[1]], ctx->E, ctx->B,
+      k_eval_eb_planes_f32<<<pgrd, pblk, 0, ctx->stream>>>(g, c, f.A[ctx->idx[0]], f.A[ctx->idx[1]], ctx->E,
                                                           ctx->eb_planes);
     });
   }
@@ -290,7 +290,7 @@ int fp32_eval_eb(mithra_ctx* ctx, bool full) {
   dim3 blk(bx, by), grd((g.N1 - 2 + bx - 1) / bx, (g.N0 - 2 + by - 1) / by, g.N2 - 2);
   return timed(ctx, "eval_eb", [&] {
     k_eval_eb_f32<<<grd, blk, 0, ctx->stream>>>(g, c, ctx->f32.A[ctx->idx[0]], ctx->f32.A[ctx->idx[1]], fn, ctx->E,
-                                                 ctx->B, 1, g.N2 - 2, full ? nullptr : ctx->st, ctx->plane_needed);
+                                                 1, g.N2 - 2, full ? nullptr : ctx->st, ctx->plane_needed);
   });
 }
 
@@ -323,11 +323,11 @@ int fp32_push(mithra_ctx* ctx, int save_rnm) {
   r = timed(ctx, "push", [&] {
     const int blocks = grid_stride_blocks(ctx, (long long)ctx->capacity, 256);
     if (C.P64.n_opt + C.P64.n_ext > 0)
-      k_push_f32<true><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, ctx->B, g.cstride,
-                                                        g.plane, g.P1, ctx->st, save_rnm);
+      k_push_f32<true><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, g.plane, g.P1,
+                                                        ctx->st, save_rnm);
     else
-      k_push_f32<false><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, ctx->B, g.cstride,
-                                                         g.plane, g.P1, ctx->st, save_rnm);
+      k_push_f32<false><<<blocks, 256, 0, ctx->stream>>>(C, ctx->und_dev, table, ctx->f32.pt, ctx->E, g.plane, g.P1,
+                                                         ctx->st, save_rnm);
   });
   if (r) return r;
   return timed(ctx, "substep_end", [&] {
@@ -359,7 +359,7 @@ int fp32_current(mithra_ctx* ctx) {
   DepositF32 D{g.N0, g.N1, g.N2, (float)g.dx, (float)g.dy, (float)g.dz};
   Fp32State& f = ctx->f32;
   const TileGrid T = tile_grid(ctx);
-  if (fp32_sorts_this_step(ctx)) {
+  if (fp32_sorts_this_step(ctx) || f.sort_pending) {
     const int r = fp32_sort(ctx);
     if (r) return r;
   }
@@ -412,6 +412,7 @@ int fp32_sort(mithra_ctx* ctx) {
   });
   if (r) return r;
   fp32_after_step(ctx);  // the sorted set becomes current
+  f.sort_pending = false;
   return MITHRA_OK;
 }
 

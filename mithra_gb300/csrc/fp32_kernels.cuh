@@ -17,12 +17,13 @@ struct EBConstF32 {
   float rdt, hx, hy, hz;  // 1/dt and 0.5/(2 d) per axis
 };
 
+
 // E and B of one interior node (FdTd::fieldEvaluate, src/fdtd.cpp:818-845; SC src/fdtdSC.cpp:1110-1140)
 // from A^{n+1} (A1), A^n (A0) and phi^n (fn, space charge only), with the copies of planes 1 and
 // N2-2 into the boundary planes (src/fdtd.cpp:755-772).
 __device__ __forceinline__ void eval_eb_node_f32(const GridDev& g, const EBConstF32& c, const float* __restrict__ A1,
                                                  const float* __restrict__ A0, const float* __restrict__ fn,
-                                                 float* __restrict__ E, float* __restrict__ B, int k, int i, int j) {
+                                                 float* __restrict__ EB, int k, int i, int j) {
   const long long m = node_index(g, k, i, j);
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
   const float rdt = c.rdt, hx = c.hx, hy = c.hy, hz = c.hz;
@@ -41,39 +42,32 @@ __device__ __forceinline__ void eval_eb_node_f32(const GridDev& g, const EBConst
                    ((Z0[m + sI] + Z1[m + sI]) - (Z0[m - sI] + Z1[m - sI])) * hx;
   const float b2 = ((Y0[m + sI] + Y1[m + sI]) - (Y0[m - sI] + Y1[m - sI])) * hx -
                    ((X0[m + 1] + X1[m + 1]) - (X0[m - 1] + X1[m - 1])) * hy;
-  E[m] = e0; E[cs + m] = e1; E[2 * cs + m] = e2;
-  B[m] = b0; B[cs + m] = b1; B[2 * cs + m] = b2;
-  if (k == 1) {
-    E[m - sK] = e0; E[cs + m - sK] = e1; E[2 * cs + m - sK] = e2;
-    B[m - sK] = b0; B[cs + m - sK] = b1; B[2 * cs + m - sK] = b2;
-  }
-  if (k == g.N2 - 2) {
-    E[m + sK] = e0; E[cs + m + sK] = e1; E[2 * cs + m + sK] = e2;
-    B[m + sK] = b0; B[cs + m + sK] = b1; B[2 * cs + m + sK] = b2;
-  }
+  store_eb(EB, m, e0, e1, e2, b0, b1, b2);
+  if (k == 1) store_eb(EB, m - sK, e0, e1, e2, b0, b1, b2);
+  if (k == g.N2 - 2) store_eb(EB, m + sK, e0, e1, e2, b0, b1, b2);
 }
 
 __global__ void __launch_bounds__(256) k_eval_eb_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
                                                      const float* __restrict__ A0,
-                                                     const float* __restrict__ fn, float* __restrict__ E,
-                                                     float* __restrict__ B, int k_lo, int k_hi, const StateDev* st,
+                                                     const float* __restrict__ fn, float* __restrict__ EB,
+                                                     int k_lo, int k_hi, const StateDev* st,
                                                      const uint8_t* plane_needed) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z + k_lo;
   if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
   if (!eb_plane_wanted(k, st, plane_needed, g.N2)) return;
-  eval_eb_node_f32(g, c, A1, A0, fn, E, B, k, i, j);
+  eval_eb_node_f32(g, c, A1, A0, fn, EB, k, i, j);
 }
 
 // E and B on the planes of a list (the power-sampling planes outside the particle slab).
 __global__ void __launch_bounds__(256) k_eval_eb_planes_f32(GridDev g, EBConstF32 c, const float* __restrict__ A1,
-                                                            const float* __restrict__ A0, float* __restrict__ E,
-                                                            float* __restrict__ B, const int* __restrict__ planes) {
+                                                            const float* __restrict__ A0, float* __restrict__ EB,
+                                                            const int* __restrict__ planes) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (j > g.N1 - 2 || i > g.N0 - 2) return;
-  eval_eb_node_f32(g, c, A1, A0, nullptr, E, B, planes[blockIdx.z], i, j);
+  eval_eb_node_f32(g, c, A1, A0, nullptr, EB, planes[blockIdx.z], i, j);
 }
 
 // Per-launch constants of the mixed-precision push, prepared on the host from GridDev/PushDev.
@@ -208,9 +202,8 @@ __device__ __forceinline__ void undulator_f32(const UndDev* __restrict__ und, co
 template <bool BEAMS>
 __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, const UndDev* __restrict__ und,
                                                   const UndTableEntry* __restrict__ table, ParticlesF32 pt,
-                                                  const float* __restrict__ E, const float* __restrict__ B,
-                                                  long long cstride, long long plane, int P1, StateDev* st,
-                                                  int save_rnm) {
+                                                  const float* __restrict__ EB, long long plane, int P1,
+                                                  StateDev* st, int save_rnm) {
   const long long n = st->n_particles;
   const double tb = st->time_bunch;
   const double tshift = C.bc * (tb + C.dt_shift);  // beta c0 (timeBunch + dt_)
@@ -273,15 +266,15 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
           const float w[8] = {wx0 * wy0 * wz0, fx * wy0 * wz0, wx0 * fy * wz0, fx * fy * wz0,
                               wx0 * wy0 * fz, fx * wy0 * fz, wx0 * fy * fz, fx * fy * fz};
           const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
+          // Node records {E, 0, B, 0}: two 16-byte loads per node.  Each component still sums
+          // its eight terms in node order onto the undulator field.
+          const float4* EB4 = reinterpret_cast<const float4*>(EB);
 #pragma unroll
-          for (int c = 0; c < 3; c++) {
-            float se = et[c], sb = bt[c];
-#pragma unroll
-            for (int q = 0; q < 8; q++) {
-              se = fmaf(w[q], __ldg(E + c * cstride + nd[q]), se);
-              sb = fmaf(w[q], __ldg(B + c * cstride + nd[q]), sb);
-            }
-            et[c] = se; bt[c] = sb;
+          for (int q = 0; q < 8; q++) {
+            const float4 e = __ldg(EB4 + 2 * nd[q]);
+            const float4 b = __ldg(EB4 + 2 * nd[q] + 1);
+            et[0] = fmaf(w[q], e.x, et[0]); et[1] = fmaf(w[q], e.y, et[1]); et[2] = fmaf(w[q], e.z, et[2]);
+            bt[0] = fmaf(w[q], b.x, bt[0]); bt[1] = fmaf(w[q], b.y, bt[1]); bt[2] = fmaf(w[q], b.z, bt[2]);
           }
         } else if (!b1x && !b1y && b1z) {
           local_nt++;

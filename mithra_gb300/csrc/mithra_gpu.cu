@@ -168,7 +168,18 @@ int stage_field_update(mithra_ctx* ctx) {
 
 int stage_push(mithra_ctx* ctx, int save_rnm) {
   if (ctx->precision == MITHRA_PRECISION_FP32) return fp32_push(ctx, save_rnm);
-  int r = timed(ctx, "push", [&] {
+  int r;
+  if (ctx->P.und_planes) {
+    const GridDev& g = ctx->g;
+    const int n = ctx->P.n_und * (g.N2 + 1);
+    r = timed(ctx, "undulator_table", [&] {
+      k_undulator_table64<<<std::max(1, (n + 255) / 256), 256, 0, ctx->stream>>>(
+          ctx->und_dev, ctx->P.n_und, g.N2, g.zmin, g.dz, ctx->P.gamma, ctx->P.beta * ctx->P.c0, ctx->P.dt_shift,
+          ctx->st, (UndPlane64*)ctx->und_table);
+    });
+    if (r) return r;
+  }
+  r = timed(ctx, "push", [&] {
     const int blocks = grid_stride_blocks(ctx, (long long)ctx->capacity, 256);
     if (ctx->P.n_opt + ctx->P.n_ext > 0)
       k_push_fp64<true><<<blocks, 256, 0, ctx->stream>>>(ctx->g, ctx->P, ctx->und_dev, ctx->pt, ctx->E64, ctx->B64,
@@ -208,9 +219,11 @@ int stage_power(mithra_ctx* ctx, double* partial = nullptr) {
     const size_t shm = (size_t)kPowerBlock * pw.Nl * sizeof(double);
     int r = timed(ctx, "power_sample", [&] {
       if (ctx->precision == MITHRA_PRECISION_FP64)
-        k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E64, ctx->B64, ctx->st);
+        k_power_sample<kPowerBlock, double><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E64, ctx->B64,
+                                                                                        ctx->g.cstride, 1, ctx->st);
       else
-        k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E, ctx->B, ctx->st);
+        k_power_sample<kPowerBlock, float><<<blocks, kPowerBlock, shm, ctx->stream>>>(ctx->g, pw, ctx->E, ctx->E + 4, 1,
+                                                                                       kEBNode, ctx->st);
     });
     if (r) return r;
     const int last = (o + 1 == ctx->power.size());
@@ -371,6 +384,7 @@ int step_key(const mithra_ctx* ctx) { return ctx->idx[0] + 3 * ctx->f32.parity; 
 int capture_step(mithra_ctx* ctx, cudaGraph_t* out) {
   const int saved[3] = {ctx->idx[0], ctx->idx[1], ctx->idx[2]};
   const Fp32State saved_f32 = ctx->f32;
+  ctx->f32.sort_pending = false;  // a step graph sorts on its rotation only
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   ctx->launch_counter = 0;
   const int r = enqueue_step(ctx);
@@ -387,7 +401,10 @@ int capture_step(mithra_ctx* ctx, cudaGraph_t* out) {
 
 void after_step(mithra_ctx* ctx) {
   rotate(ctx);
-  if (ctx->precision == MITHRA_PRECISION_FP32 && fp32_sorts_this_step(ctx)) fp32_after_step(ctx);
+  if (ctx->precision == MITHRA_PRECISION_FP32 && fp32_sorts_this_step(ctx)) {
+    fp32_after_step(ctx);
+    ctx->f32.sort_pending = false;
+  }
 }
 
 int prepare_run(mithra_ctx* ctx, int64_t nsteps) {
@@ -468,6 +485,8 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
     P.dtb = pd->dtb; P.r1 = pd->r1; P.r2 = pd->r2; P.gamma = pd->gamma; P.beta = pd->beta; P.c0 = pd->c0;
     P.dt_shift = pd->dt_shift; P.bunch_time_step = pd->bunch_time_step; P.n_und = 0; P.und0_dist = 0.0;
     P.inv_r2 = 1.0 / pd->r2;
+    P.und_planes = nullptr;
+    P.gdz = pd->gamma * gd->dz;
     P.beams = nullptr; P.ext0 = 0; P.n_ext = 0; P.n_opt = 0;
     CK(dalloc(&ctx->und_dev, kMaxUndulators));
     CK(dalloc(&ctx->beams_dev, kMaxUndulators + MITHRA_MAX_EXT_FIELDS));
@@ -501,10 +520,9 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
       CK(cudaMemsetAsync(ctx->E64, 0, nf * sizeof(double), ctx->stream));
       CK(cudaMemsetAsync(ctx->B64, 0, nf * sizeof(double), ctx->stream));
     } else {
-      CK(dalloc(&ctx->E, nf));
-      CK(dalloc(&ctx->B, nf));
-      CK(cudaMemsetAsync(ctx->E, 0, nf * sizeof(float), ctx->stream));
-      CK(cudaMemsetAsync(ctx->B, 0, nf * sizeof(float), ctx->stream));
+      const size_t ne = (size_t)kEBNode * g.cstride;  // node records {E, 0, B, 0}
+      CK(dalloc(&ctx->E, ne));
+      CK(cudaMemsetAsync(ctx->E, 0, ne * sizeof(float), ctx->stream));
     }
     CK(dalloc(&ctx->plane_needed, (size_t)g.N2));
     CK(cudaMemsetAsync(ctx->plane_needed, 0, (size_t)g.N2, ctx->stream));
@@ -585,17 +603,29 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
     if (u + 1 < n) U.r0_next = und[u + 1].rb - U.rb - U.length * U.lu;                  // src/beam.cc:60
     U.ct_f = (float)U.ct; U.st_f = (float)U.st; U.ku_f = (float)U.ku; U.b0_f = (float)U.b0; U.ul_f = (float)U.ul;
     U.r0_prev_f = (float)U.r0_prev; U.r0_next_f = (float)U.r0_next;
+    U.kgdz = U.ku * ctx->P.gdz;
     U.beam = -1;
     if (U.type == 1) {
       U.beam = (int)ctx->opt_beams.size();
       ctx->opt_beams.push_back(beam_from_desc(und[u].beam));
     }
   }
+  cudaFree(ctx->und_table);
+  ctx->und_table = nullptr;
+  ctx->P.und_planes = nullptr;
   if (ctx->precision == MITHRA_PRECISION_FP32) {
-    cudaFree(ctx->und_table);
-    ctx->und_table = nullptr;
     if (n) CK(cudaMalloc(&ctx->und_table, (size_t)n * (ctx->g.N2 + 1) * 2 * sizeof(float)));
+  } else if (n) {
+    // FP64 form: the per-plane phase table, where every static module advances its phase by
+    // less than kUndTableMaxKgdz across a cell
+    bool small = true;
+    for (const UndDev& U : ctx->und_host) small = small && (U.type != 0 || std::fabs(U.kgdz) <= kUndTableMaxKgdz);
+    if (small) {
+      CK(cudaMalloc(&ctx->und_table, (size_t)n * (ctx->g.N2 + 1) * sizeof(UndPlane64)));
+      ctx->P.und_planes = (const UndPlane64*)ctx->und_table;
+    }
   }
+  invalidate_graphs(ctx);  // the push's launch arguments change
   ctx->P.n_und = n;
   ctx->P.und0_dist = n ? und[0].dist : 0.0;
   return upload_beams(ctx);
@@ -839,14 +869,13 @@ int mithra_gpu_download_eb(mithra_ctx* ctx, float* en, float* bn) {
   float* staging = nullptr;
   { int r = mithra::staging(ctx, n * sizeof(float), (void**)&staging); if (r) return r; }
   float* dst[2] = {en, bn};
-  const float* srcs[2] = {ctx->E, ctx->B};
   const double* srcs64[2] = {ctx->E64, ctx->B64};
   for (int l = 0; l < 2; l++) {
     if (!dst[l]) continue;
     if (ctx->precision == MITHRA_PRECISION_FP64)
       k_soa_to_aos<double, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs64[l], staging, 3);
     else
-      k_soa_to_aos<float, float><<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, srcs[l], staging, 3);
+      k_eb_to_aos<<<grid_stride_blocks(ctx, n / 3, 256), 256, 0, ctx->stream>>>(g, ctx->E, 4 * l, staging);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(dst[l], staging, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -898,9 +927,11 @@ int particles_from_device_records(mithra_ctx* ctx, const double* staging, size_t
   CK(cudaMemcpyAsync(ctx->st, ctx->st_host, sizeof(StateDev), cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->precision == MITHRA_PRECISION_FP32) {
     // Until the first sort, the deposit takes every particle as one outside the tiles (the
-    // particles keep their upload order, which z-face copies and downloads follow).
+    // particles keep their upload order, which z-face copies and downloads follow); the next
+    // step sorts.
     const int r = fp32_unsorted(ctx, (long long)n);
     if (r) return r;
+    ctx->f32.sort_pending = true;
   }
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->particles_loaded = true;
@@ -1047,6 +1078,13 @@ int mithra_gpu_run(mithra_ctx* ctx, int64_t nsteps) {
     return check_state(ctx);
   }
   for (int64_t s = 0; s < nsteps; s++) {
+    if (ctx->precision == MITHRA_PRECISION_FP32 && ctx->f32.sort_pending) {
+      // The step's deposit runs after its rotation, which brings idx[2] to idx[0].
+      if (ctx->idx[2] != 0) {  // not a sorting step: the sort an upload asks for, outside the graphs
+        if ((r = enqueue_step(ctx))) return r;
+        continue;
+      }
+    }
     const int key = step_key(ctx);
     if (!ctx->graph[key]) {
       cudaGraph_t graph;
@@ -1243,11 +1281,11 @@ int mithra_gpu_field_sample(mithra_ctx* ctx, const double* points, size_t n, dou
   CK(cudaMemcpyAsync(buf, points, n * 3 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   const int blocks = (int)((n + 127) / 128);
   if (ctx->precision == MITHRA_PRECISION_FP64)
-    k_field_sample<double, double><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E64, ctx->B64, ctx->A[ctx->idx[1]], buf,
-                                                                    (int)n, buf + 3 * n);
+    k_field_sample<double, double><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E64, ctx->B64, ctx->g.cstride, 1,
+                                                                    ctx->A[ctx->idx[1]], buf, (int)n, buf + 3 * n);
   else
-    k_field_sample<float, float><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E, ctx->B, fp32_field(ctx, 1), buf,
-                                                                  (int)n, buf + 3 * n);
+    k_field_sample<float, float><<<blocks, 128, 0, ctx->stream>>>(ctx->g, ctx->E, ctx->E + 4, 1, kEBNode,
+                                                                  fp32_field(ctx, 1), buf, (int)n, buf + 3 * n);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(out, buf + 3 * n, n * 9 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));

@@ -7,25 +7,61 @@
 
 namespace mithra {
 
+// Per-plane undulator lz and phase for the FP64 push: lz_k = gamma (zmin + k dz + beta c0
+// (timeBunch + dt_)) - rb on node plane k, with the sine and cosine of ku lz_k.  One entry per
+// static module and plane k = 0..N2.
+__global__ void k_undulator_table64(const UndDev* __restrict__ und, int n_und, int N2, double zmin, double dz,
+                                    double gamma, double bc, double dt_shift, const StateDev* st,
+                                    UndPlane64* __restrict__ table) {
+  const double tshift = bc * (st->time_bunch + dt_shift);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_und * (N2 + 1); t += gridDim.x * blockDim.x) {
+    const int u = t / (N2 + 1), k = t % (N2 + 1);
+    const double lz = gamma * (zmin + (double)k * dz + tshift) - und[u].rb;
+    double s, c;
+    sincos(und[u].ku * lz, &s, &c);
+    table[t] = UndPlane64{lz, s, c};
+  }
+}
+
+// Largest phase advance across one cell (ku gamma dz) for which the push takes the undulator
+// phase from the plane table: the series below then truncate below 1e-19 relative.
+constexpr double kUndTableMaxKgdz = 0.05;
+
 // Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
 // Solver::staticUndulator (src/beam.cc:14-76).  Adds the lab-frame undulator field, boosted
 // into the bunch frame, to bt/et.  Optical modules are laser beams (laser_beams_add), added
 // after the static ones.
+// kz, fz: node plane below z and the offset above it in cells ((z - zmin)/dz = kz + fz).  On a
+// plane of the table, lz = lz_k + gamma dz fz and sin, cos of ku lz come from the plane's values
+// and the short series of the phase advance d = ku gamma dz fz (|d| < kUndTableMaxKgdz) by the
+// angle-sum formulas: a few FP64 operations instead of a sincos with its range reduction.
 __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
                                                        const PushDev& P, double timeBunch,
-                                                       double x, double y, double z,
+                                                       double x, double y, double z, int N2, int kz, double fz,
                                                        double* bt, double* et) {
+  const bool tab = P.und_planes != nullptr && kz >= 0 && kz <= N2;
   for (int u = 0; u < n_und; u++) {
     const UndDev& U = und[u];
     if (U.type != 0) continue;  // optical modules: laser_beams_add
-    const double lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift)) - U.rb;
+    double lz, sn = 0.0, cs = 0.0;
+    if (tab) {
+      const UndPlane64 te = P.und_planes[u * (N2 + 1) + kz];
+      lz = fma(P.gdz, fz, te.lz);
+      const double d = U.kgdz * fz, d2 = d * d;
+      const double sd = d * (1.0 - d2 * (1.0 / 6.0) * (1.0 - d2 * (1.0 / 20.0) * (1.0 - d2 * (1.0 / 42.0) * (1.0 - d2 * (1.0 / 72.0)))));
+      const double cd = 1.0 - d2 * 0.5 * (1.0 - d2 * (1.0 / 12.0) * (1.0 - d2 * (1.0 / 30.0) * (1.0 - d2 * (1.0 / 56.0) * (1.0 - d2 * (1.0 / 90.0)))));
+      sn = te.s * cd + te.c * sd;
+      cs = te.c * cd - te.s * sd;
+    } else {
+      lz = P.gamma * (z + P.beta * P.c0 * (timeBunch + P.dt_shift)) - U.rb;
+    }
     const double ly = x * U.ct + y * U.st;
     double s_ly, c_ly;
     {
       // cosh and sinh: Taylor series for |ku ly| < 0.1 (truncation below 1e-19 relative; the FP64
       // pipe is the bound of this kernel), else from one exponential.
       const double kl = U.ku * ly;
-      if (fabs(kl) < 0.1) {
+      if ((long long)(bits_of(kl) & 0x7fffffffffffffffULL) < 0x3fb999999999999aLL) {  // |kl| < 0.1
         const double a2 = kl * kl;
         s_ly = kl * (1.0 + a2 * (1.0 / 6.0) * (1.0 + a2 * (1.0 / 20.0) * (1.0 + a2 * (1.0 / 42.0) * (1.0 + a2 * (1.0 / 72.0)))));
         c_ly = 1.0 + a2 * 0.5 * (1.0 + a2 * (1.0 / 12.0) * (1.0 + a2 * (1.0 / 30.0) * (1.0 + a2 * (1.0 / 56.0) * (1.0 + a2 * (1.0 / 90.0)))));
@@ -36,9 +72,9 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
       }
     }
     double d1, bz;
-    if (lz >= 0.0 && lz <= U.ul) {
-      double sn, cs;
-      sincos(U.ku * lz, &sn, &cs);
+    const long long klz = dkey(lz);
+    if (klz >= 0 && klz <= dkey(U.ul)) {  // 0 <= lz <= ul
+      if (!tab) sincos(U.ku * lz, &sn, &cs);
       d1 = U.b0 * c_ly * sn * P.gamma;
       bz = U.b0 * s_ly * cs;
     } else {
@@ -77,27 +113,37 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
   const double timeBunch = st->time_bunch;
   const long long cs = g.cstride;
   unsigned long long local_cross = 0, local_nt = 0;
+  // Comparisons, modf and the index conversions on the integer pipes (see k_deposit_fp64).
+  const long long kxh = dkey(g.xmax - g.dx), kxl = dkey(g.xmin + g.dx), kyh = dkey(g.ymax - g.dy),
+                  kyl = dkey(g.ymin + g.dy), kzh = dkey(g.zp1), kzl = dkey(g.zp0), kLz = dkey(g.Lz);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     int8_t cross = 0;
     if (!(pt.status[p] & 1)) {
       double x = pt.x[p], y = pt.y[p], z = pt.z[p];
       if (save_rnm) { pt.mx[p] = x; pt.my[p] = y; pt.mz[p] = z; }
-      double zr = pmod_d(z - g.zmin, g.Lz) + g.zmin;
-      if ((zr >= g.zp0) && (zr < g.zp1)) {
-        const bool b1x = (x < g.xmax - g.dx && x > g.xmin + g.dx);
-        const bool b1y = (y < g.ymax - g.dy && y > g.ymin + g.dy);
-        const bool b1z = (z < g.zp1 && z >= g.zp0);
+      const double za = z - g.zmin;
+      const long long kza = dkey(za);
+      double zr = ((kza >= 0 && kza < kLz) ? za : pmod_d(za, g.Lz)) + g.zmin;  // pmod_d's own fast path
+      const long long kzr = dkey(zr);
+      if (kzr >= kzl && kzr < kzh) {
+        const long long kx = dkey(x), ky = dkey(y), kz = dkey(z);
+        const bool b1x = (kx < kxh && kx > kxl);
+        const bool b1y = (ky < kyh && ky > kyl);
+        const bool b1z = (kz < kzh && kz >= kzl);
+        // z in cells, split as the gather's modf does: plane k and offset dzr
+        double kd;
+        const double dzr = modf_d(za * g.rdz, &kd);
+        const int k = itrunc_d(kd);
         double bt[3] = {0.0, 0.0, 0.0}, et[3] = {0.0, 0.0, 0.0};
-        static_undulator_field(und, P.n_und, P, timeBunch, x, y, z, bt, et);
+        static_undulator_field(und, P.n_und, P, timeBunch, x, y, z, g.N2, (kza >= 0) ? k : -1, dzr, bt, et);
         if (BEAMS) laser_beams_add(P, und, P.n_und, timeBunch, x, y, z, bt, et);
         double e = pt.e[p];
-        if (e == 1.0) {
+        if (__double_as_longlong(e) == 0x3ff0000000000000LL) {  // e == 1.0
           if (b1x && b1y && b1z) {
             double d1;
-            const double dxr = modf((x - g.xmin) * g.rdx, &d1); const int i = (int)d1;
-            const double dyr = modf((y - g.ymin) * g.rdy, &d1); const int j = (int)d1;
-            const double dzr = modf((z - g.zmin) * g.rdz, &d1); const int k = (int)d1;
+            const double dxr = modf_d((x - g.xmin) * g.rdx, &d1); const int i = itrunc_d(d1);
+            const double dyr = modf_d((y - g.ymin) * g.rdy, &d1); const int j = itrunc_d(d1);
             const long long m = node_index(g, k, i, j);
             const long long sI = g.P1, sK = g.plane;
             const double wx0 = 1.0 - dxr, wy0 = 1.0 - dyr, wz0 = 1.0 - dzr;
@@ -127,8 +173,11 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         // Boris rotation, src/solver.cpp:1519-1535.
         double gx = pt.gx[p], gy = pt.gy[p], gz = pt.gz[p];
         const double mx = gx + P.r1 * et[0], my = gy + P.r1 * et[1], mz = gz + P.r1 * et[2];
-        const double d1 = sqrt(1.0 + (mx * mx + my * my + mz * mz));
-        const double rd1 = 1.0 / d1;
+        // d1 = sqrt(1 + |m|^2) and 1/d1 from one reciprocal square root (the reference divides
+        // by the square root; the two differ by rounding)
+        const double u1 = 1.0 + (mx * mx + my * my + mz * mz);
+        const double rd1 = rsqrt(u1);
+        const double d1 = u1 * rd1;
         const double f = P.r2 * rd1;
         const double px = f * (my * bt[2] - mz * bt[1]) + mx;
         const double py = f * (mz * bt[0] - mx * bt[2]) + my;
@@ -144,8 +193,9 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         const double drz = gg * gz;
         pt.x[p] = x + gg * gx; pt.y[p] = y + gg * gy; pt.z[p] = z + drz;
         zr += drz;
-        if (zr < g.zp0) cross = 1;
-        else if (zr >= g.zp1) cross = 2;
+        const long long kzn = dkey(zr);
+        if (kzn < kzl) cross = 1;
+        else if (kzn >= kzh) cross = 2;
       }
     }
     pt.cross[p] = cross;
@@ -281,39 +331,46 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
   if (blockIdx.x == 0 && threadIdx.x == 0) st->j_edges = 1;  // J is written in edge form
   int kmin = 0x7fffffff, kmax = -0x7fffffff;
+  // The kernel is bound by GB300's FP64 issue rate: comparisons, floors, conversions, min/max and
+  // modf's truncation run on the integer pipes (dkey, ifloor_d, double_of_int, dmin_k, modf_d),
+  // with the same results as the FP64 instructions.
+  const long long kxh = dkey(g.xmax - g.dx), kxl = dkey(g.xmin + g.dx), kyh = dkey(g.ymax - g.dy),
+                  kyl = dkey(g.ymin + g.dy), kzh = dkey(g.zp1), kzl = dkey(g.zp0);
+  auto inside = [&](double a, double b, double c) {
+    const long long ka = dkey(a), kb = dkey(b), kc = dkey(c);
+    return ka < kxh && ka > kxl && kb < kyh && kb > kyl && kc < kzh && kc >= kzl;
+  };
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     if (pt.status[p] & 1) continue;
     const double rp0 = pt.x[p], rp1 = pt.y[p], rp2 = pt.z[p];
-    {
-      const int kc = (int)floor((rp2 - g.zmin) * g.rdz);
-      kmin = min(kmin, kc);
-      kmax = max(kmax, kc);
-    }
+    const int kp = ifloor_d((rp2 - g.zmin) * g.rdz);
+    kmin = min(kmin, kp);
+    kmax = max(kmax, kp);
     const double rm0 = pt.mx[p], rm1 = pt.my[p], rm2 = pt.mz[p];
-    const bool bp = (rp0 < g.xmax - g.dx && rp0 > g.xmin + g.dx && rp1 < g.ymax - g.dy &&
-                     rp1 > g.ymin + g.dy && rp2 < g.zp1 && rp2 >= g.zp0);
-    const bool bm = (rm0 < g.xmax - g.dx && rm0 > g.xmin + g.dx && rm1 < g.ymax - g.dy &&
-                     rm1 > g.ymin + g.dy && rm2 < g.zp1 && rm2 >= g.zp0);
+    const bool bp = inside(rp0, rp1, rp2);
+    const bool bm = inside(rm0, rm1, rm2);
     if (!(bp || bm)) continue;
     const double qh = pt.q[p] * 0.5;
-    const int ip = (int)floor((rp0 - g.xmin) * g.rdx), jp = (int)floor((rp1 - g.ymin) * g.rdy),
-              kp = (int)floor((rp2 - g.zmin) * g.rdz);
-    const int im = (int)floor((rm0 - g.xmin) * g.rdx), jm = (int)floor((rm1 - g.ymin) * g.rdy),
-              km = (int)floor((rm2 - g.zmin) * g.rdz);
-    const double r0 = fmin(min(im, ip) * g.dx + g.dx + g.xmin, fmax(max(im, ip) * g.dx + g.xmin, 0.5 * (rm0 + rp0)));
-    const double r1 = fmin(min(jm, jp) * g.dy + g.dy + g.ymin, fmax(max(jm, jp) * g.dy + g.ymin, 0.5 * (rm1 + rp1)));
-    const double r2 = fmin(min(km, kp) * g.dz + g.dz + g.zmin, fmax(max(km, kp) * g.dz + g.zmin, 0.5 * (rm2 + rp2)));
+    const int ip = ifloor_d((rp0 - g.xmin) * g.rdx), jp = ifloor_d((rp1 - g.ymin) * g.rdy);
+    const int im = ifloor_d((rm0 - g.xmin) * g.rdx), jm = ifloor_d((rm1 - g.ymin) * g.rdy),
+              km = ifloor_d((rm2 - g.zmin) * g.rdz);
+    const double r0 = dmin_k(double_of_int(min(im, ip)) * g.dx + g.dx + g.xmin,
+                             dmax_k(double_of_int(max(im, ip)) * g.dx + g.xmin, 0.5 * (rm0 + rp0)));
+    const double r1 = dmin_k(double_of_int(min(jm, jp)) * g.dy + g.dy + g.ymin,
+                             dmax_k(double_of_int(max(jm, jp)) * g.dy + g.ymin, 0.5 * (rm1 + rp1)));
+    const double r2 = dmin_k(double_of_int(min(km, kp)) * g.dz + g.dz + g.zmin,
+                             dmax_k(double_of_int(max(km, kp)) * g.dz + g.zmin, 0.5 * (rm2 + rp2)));
     double c;
     if (bp) {
       const long long m = node_index(g, kp, ip, jp);
-      const double dxp = modf((0.5 * (rp0 + r0) - g.xmin) * g.rdx, &c);
-      const double dyp = modf((0.5 * (rp1 + r1) - g.ymin) * g.rdy, &c);
-      const double dzp = modf((0.5 * (rp2 + r2) - g.zmin) * g.rdz, &c);
+      const double dxp = modf_d((0.5 * (rp0 + r0) - g.xmin) * g.rdx, &c);
+      const double dyp = modf_d((0.5 * (rp1 + r1) - g.ymin) * g.rdy, &c);
+      const double dzp = modf_d((0.5 * (rp2 + r2) - g.zmin) * g.rdz, &c);
       deposit_half_edges(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
       if (rho) {
-        const double fx = modf((rp0 - g.xmin) * g.rdx, &c), fy = modf((rp1 - g.ymin) * g.rdy, &c),
-                     fz = modf((rp2 - g.zmin) * g.rdz, &c);
+        const double fx = modf_d((rp0 - g.xmin) * g.rdx, &c), fy = modf_d((rp1 - g.ymin) * g.rdy, &c),
+                     fz = modf_d((rp2 - g.zmin) * g.rdz, &c);
         const double q = pt.q[p];
         const double x1 = 1.0 - fx, y1 = 1.0 - fy, z1 = 1.0 - fz;
         atomicAdd(rho + m, q * x1 * y1 * z1);
@@ -328,9 +385,9 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
     }
     if (bm) {
       const long long m = node_index(g, km, im, jm);
-      const double dxm = modf((0.5 * (rm0 + r0) - g.xmin) * g.rdx, &c);
-      const double dym = modf((0.5 * (rm1 + r1) - g.ymin) * g.rdy, &c);
-      const double dzm = modf((0.5 * (rm2 + r2) - g.zmin) * g.rdz, &c);
+      const double dxm = modf_d((0.5 * (rm0 + r0) - g.xmin) * g.rdx, &c);
+      const double dym = modf_d((0.5 * (rm1 + r1) - g.ymin) * g.rdy, &c);
+      const double dzm = modf_d((0.5 * (rm2 + r2) - g.zmin) * g.rdz, &c);
       deposit_half_edges(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
     }
   }

@@ -11,9 +11,12 @@
 
 namespace mithra {
 
+// Component c of node m of E (B) is E[c * ecs + m * ens]: component planes (ecs = cstride,
+// ens = 1) in the FP64 form, the node records of the mixed form (ecs = 1, ens = kEBNode, B = E + 4).
 template <int BLOCK, typename TE>
 __global__ void __launch_bounds__(BLOCK) k_power_sample(GridDev g, PowerDev pw, const TE* __restrict__ E,
-                                                        const TE* __restrict__ B, const StateDev* st) {
+                                                        const TE* __restrict__ B, long long ecs, int ens,
+                                                        const StateDev* st) {
   extern __shared__ double s_red[];  // Nl * BLOCK
   const int plane = blockIdx.x / pw.blocks_per_plane;
   const int bip = blockIdx.x % pw.blocks_per_plane;
@@ -24,8 +27,8 @@ __global__ void __launch_bounds__(BLOCK) k_power_sample(GridDev g, PowerDev pw, 
   for (int l = 0; l < pw.Nl; l++) s_red[l * BLOCK + threadIdx.x] = 0.0;
   if (k_cell >= 0 && t < nodes) {
     const int i = 2 + (int)(t / pw.nodes_j), j = 2 + (int)(t % pw.nodes_j);
-    const long long mi = node_index(g, k_cell, i, j);
-    const long long cs = g.cstride, sK = g.plane;
+    const long long mi = node_index(g, k_cell, i, j) * ens;
+    const long long cs = ecs, sK = g.plane * ens;
     const double dzr = pw.plane_dzr[plane];
     const double et0 = (1.0 - dzr) * (double)E[mi] + dzr * (double)E[mi + sK];
     const double et1 = (1.0 - dzr) * (double)E[cs + mi] + dzr * (double)E[cs + mi + sK];
