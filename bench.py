@@ -58,6 +58,10 @@ ALGO_BYTES = {
 }
 
 
+# Bytes of E and B per node that a push's gathers read: six doubles (FP64 form), six floats (mixed).
+GATHER_BYTES = {"fp64": 48, "fp32": 24}
+
+
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -297,6 +301,18 @@ def touched_nodes(parts, meta) -> int:
     return int(np.unique(np.concatenate(corners)).size)
 
 
+def slab_nodes(parts, meta) -> int:
+    """Interior nodes on the planes the E/B evaluation covers: the particles' cell planes with two
+    planes of margin below and three above (eb_plane_wanted in the kernels)."""
+    ext = int(meta["np"])
+    k = np.floor((parts[:, 3] - meta["zmin"]) / meta["dz"]).astype(np.int64)
+    k = k[(k >= 0) & (k < ext - 1)]
+    if k.size == 0:
+        return 0
+    lo, hi = max(1, int(k.min()) - 2), min(ext - 2, int(k.max()) + 3)
+    return (hi - lo + 1) * (int(meta["N0"]) - 2) * (int(meta["N1"]) - 2)
+
+
 def units_per_step(meta, n_particles):
     nsub = 0
     t = 0.0
@@ -458,18 +474,25 @@ def measure_form(mg, setup, prec_name, args, dist, units, interior, keep_snapsho
     dominant = max(kt.items(), key=lambda kv: kv[1][0])[0]
     dom_ms, dom_launches = kt[dominant]
     particle_kernels = ("push", "deposit", "erase", "tile_scatter")
-    unit_count = n_part if dominant in particle_kernels else interior
-    # the push's gathers read E and B (two float triples, 24 B) of every node around an occupied
-    # cell once per launch
+    # the push's gathers read E and B of every node around an occupied cell once per launch
     gather = touched_nodes(snap.particles, setup.meta()) if entered > 0.0 else 0
     window["gather_nodes"] = gather
+    # E and B are evaluated on the particles' planes only
+    eb_nodes = slab_nodes(snap.particles, setup.meta())
+    window["eb_slab_nodes"] = eb_nodes
+
+    def units_of(k):
+        if k in particle_kernels:
+            return n_part
+        return eb_nodes if k == "eval_eb" else interior
 
     def algo_bytes(k, count):
         pu = ALGO_BYTES[prec_name].get(k)
         if not pu:
             return None
-        return pu * count + (24 * gather if k == "push" else 0)
+        return pu * count + (GATHER_BYTES[prec_name] * gather if k == "push" else 0)
 
+    unit_count = units_of(dominant)
     peak, peak_kind = measured_peaks()
     roof = None
     ab = algo_bytes(dominant, unit_count)
@@ -486,9 +509,10 @@ def measure_form(mg, setup, prec_name, args, dist, units, interior, keep_snapsho
     out["kernels"] = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / total_k}
                       for k, v in kt.items()}
     for k, v in out["kernels"].items():
-        ab = algo_bytes(k, n_part if k in particle_kernels else interior)
+        ab = algo_bytes(k, units_of(k))
         if ab:
             v["hbm_frac"] = ab / (v["ms_per_launch"] / 1e3) / 1e9 / peak
+            v["units"] = units_of(k)
 
     # End to end through the public API with host buffers: the step-S state uploaded from
     # page-locked host memory (a resumed march), K steps, the power rows read back.
@@ -497,12 +521,14 @@ def measure_form(mg, setup, prec_name, args, dist, units, interior, keep_snapsho
         dist.barrier()
         t0 = time.perf_counter()
         snapshot.restore(ctx, snap)
+        t1 = time.perf_counter()
         ctx.run(args.steps)
         rows = ctx.power_rows()
-        el = dist.max(time.perf_counter() - t0)
+        t2 = time.perf_counter()
+        el = dist.max(t2 - t0)
         e2e = {"value": dist.world * units * args.steps / el, "unit": METRIC,
                "h2d_bytes_per_step": snap.nbytes / args.steps, "d2h_bytes_per_step": rows.nbytes / args.steps,
-               "ms_per_step": 1e3 * el / args.steps,
+               "ms_per_step": 1e3 * el / args.steps, "upload_ms": 1e3 * (t1 - t0), "march_ms": 1e3 * (t2 - t1),
                "how": "march state of step %d (fields, particles, time) uploaded from page-locked host "
                       "memory, K steps, power rows read back" % start}
         rest_from = start + args.steps

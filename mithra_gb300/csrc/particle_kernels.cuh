@@ -24,8 +24,9 @@ __global__ void k_undulator_table64(const UndDev* __restrict__ und, int n_und, i
 }
 
 // Largest phase advance across one cell (ku gamma dz) for which the push takes the undulator
-// phase from the plane table: the series below then truncate below 1e-19 relative.
-constexpr double kUndTableMaxKgdz = 0.05;
+// phase from the plane table: with |d| <= 1 the Taylor series of sin_cos_series truncate below
+// 1e-17 relative (d^21/21!, d^22/22!).  The bench jobs advance 0.78 rad per boosted-frame cell.
+constexpr double kUndTableMaxKgdz = 1.0;
 
 // Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
 // Solver::staticUndulator (src/beam.cc:14-76).  Adds the lab-frame undulator field, boosted
@@ -33,8 +34,8 @@ constexpr double kUndTableMaxKgdz = 0.05;
 // after the static ones.
 // kz, fz: node plane below z and the offset above it in cells ((z - zmin)/dz = kz + fz).  On a
 // plane of the table, lz = lz_k + gamma dz fz and sin, cos of ku lz come from the plane's values
-// and the short series of the phase advance d = ku gamma dz fz (|d| < kUndTableMaxKgdz) by the
-// angle-sum formulas: a few FP64 operations instead of a sincos with its range reduction.
+// and the series of the phase advance d = ku gamma dz fz (|d| < kUndTableMaxKgdz) by the
+// angle-sum formulas: about 27 FP64 operations instead of a sincos with its range reduction.
 __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
                                                        const PushDev& P, double timeBunch,
                                                        double x, double y, double z, int N2, int kz, double fz,
@@ -47,9 +48,8 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
     if (tab) {
       const UndPlane64 te = P.und_planes[u * (N2 + 1) + kz];
       lz = fma(P.gdz, fz, te.lz);
-      const double d = U.kgdz * fz, d2 = d * d;
-      const double sd = d * (1.0 - d2 * (1.0 / 6.0) * (1.0 - d2 * (1.0 / 20.0) * (1.0 - d2 * (1.0 / 42.0) * (1.0 - d2 * (1.0 / 72.0)))));
-      const double cd = 1.0 - d2 * 0.5 * (1.0 - d2 * (1.0 / 12.0) * (1.0 - d2 * (1.0 / 30.0) * (1.0 - d2 * (1.0 / 56.0) * (1.0 - d2 * (1.0 / 90.0)))));
+      double sd, cd;
+      sin_cos_series(U.kgdz * fz, &sd, &cd);
       sn = te.s * cd + te.c * sd;
       cs = te.c * cd - te.s * sd;
     } else {
