@@ -190,16 +190,25 @@ struct PowerDev {
 
 // E and B of the mixed form are stored node by node: node m holds the 32-byte record
 // {Ex, Ey, Ez, 0, Bx, By, Bz, 0} at EB + 8 m.  A particle's gather reads each of its 8 nodes with
-// two 16-byte loads from one 32-byte sector (component planes would take 6 sectors per node), and
-// the evaluation writes a node with two 16-byte stores.  Component c of node m: E at
+// one 32-byte load from one sector (component planes would take 6 sectors per node), and the
+// evaluation writes a node with one 32-byte store (256-bit vector loads and stores, sm_100 and
+// later).  Component c of node m: E at
 // EB[8 m + c], B at EB[8 m + 4 + c].
 constexpr int kEBNode = 8;
 
 __device__ __forceinline__ void store_eb(float* EB, long long m, float e0, float e1, float e2, float b0, float b1,
                                          float b2) {
-  float4* p = reinterpret_cast<float4*>(EB + (long long)kEBNode * m);
-  p[0] = make_float4(e0, e1, e2, 0.0f);
-  p[1] = make_float4(b0, b1, b2, 0.0f);
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(EB + (long long)kEBNode * m), "f"(e0),
+               "f"(e1), "f"(e2), "f"(0.0f), "f"(b0), "f"(b1), "f"(b2), "f"(0.0f)
+               : "memory");
+}
+
+// One node record as a single 32-byte load (a 256-bit vector load, sm_100 and later), through
+// the read-only path: the gather reads 8 records per particle, one load instruction each.
+__device__ __forceinline__ void load_eb(const float* EB, long long m, float4& e, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(e.x), "=f"(e.y), "=f"(e.z), "=f"(e.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(EB + (long long)kEBNode * m));
 }
 
 // True when node plane k has to be evaluated: inside the particle slab (with two cells of margin

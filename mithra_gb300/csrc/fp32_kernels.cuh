@@ -266,13 +266,12 @@ __global__ void __launch_bounds__(256, BEAMS ? 1 : 4) k_push_f32(PushF32 C, cons
           const float w[8] = {wx0 * wy0 * wz0, fx * wy0 * wz0, wx0 * fy * wz0, fx * fy * wz0,
                               wx0 * wy0 * fz, fx * wy0 * fz, wx0 * fy * fz, fx * fy * fz};
           const long long nd[8] = {m, m + sI, m + 1, m + sI + 1, m + sK, m + sK + sI, m + sK + 1, m + sK + sI + 1};
-          // Node records {E, 0, B, 0}: two 16-byte loads per node.  Each component still sums
+          // Node records {E, 0, B, 0}: one 32-byte load per node.  Each component still sums
           // its eight terms in node order onto the undulator field.
-          const float4* EB4 = reinterpret_cast<const float4*>(EB);
 #pragma unroll
           for (int q = 0; q < 8; q++) {
-            const float4 e = __ldg(EB4 + 2 * nd[q]);
-            const float4 b = __ldg(EB4 + 2 * nd[q] + 1);
+            float4 e, b;
+            load_eb(EB, nd[q], e, b);
             et[0] = fmaf(w[q], e.x, et[0]); et[1] = fmaf(w[q], e.y, et[1]); et[2] = fmaf(w[q], e.z, et[2]);
             bt[0] = fmaf(w[q], b.x, bt[0]); bt[1] = fmaf(w[q], b.y, bt[1]); bt[2] = fmaf(w[q], b.z, bt[2]);
           }
