@@ -49,9 +49,11 @@ WINDOW_AT = 0.9
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
 
 # Algorithmic bytes per unit (each array element counted once, halo re-reads free).
-# Units: interior node for the field kernels, particle for the particle kernels.
+# Units: interior node for the stencils, interior node of the particle slab for E/B (read A^n and
+# A^{n+1}, write E and B: doubles in the FP64 form, floats in the mixed form), particle for the
+# particle kernels (plus the gathered E/B nodes for the push, GATHER_BYTES).
 ALGO_BYTES = {
-    "fp64": {"potential_interior_fd": 96, "potential_interior_nsfd": 96, "eval_eb": 72, "push": 96 + 1,
+    "fp64": {"potential_interior_fd": 96, "potential_interior_nsfd": 96, "eval_eb": 96, "push": 96 + 1,
              "deposit": 48 + 8, "erase": 8 + 1},
     "fp32": {"potential_interior_fd": 48, "potential_interior_nsfd": 48, "eval_eb": 48, "push": 56 + 1,
              "deposit": 24 + 4 + 20, "erase": 12 + 1},
