@@ -46,6 +46,7 @@ WORKLOADS = {
 METRIC = "cell+particle updates/s"
 # First step of the timed window, as a fraction of the march (see window_start).
 WINDOW_AT = 0.9
+DEFAULT_STEPS, DEFAULT_WARMUP = 10, 3
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 dense FP64, nominal
 
 # Algorithmic bytes per unit (each array element counted once, halo re-reads free).
@@ -67,8 +68,8 @@ GATHER_BYTES = {"fp64": 48, "fp32": 24}
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=DEFAULT_STEPS)
+    ap.add_argument("--warmup", type=int, default=DEFAULT_WARMUP)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS) + ["sweep-192"])
@@ -90,7 +91,8 @@ def parse_args():
     ap.add_argument("--snapshot-fd", type=int, default=None, help=argparse.SUPPRESS)
     ap.add_argument("--write-snapshot", default=None, metavar="DIR",
                     help="write the workload's march state at the timed window's first step (FP64 form) to "
-                         "DIR and exit; `python -m mithra_gb300.snapshot <job> --resume DIR` marches on from it")
+                         "DIR and exit (nothing to do when DIR holds it already); `python -m "
+                         "mithra_gb300.snapshot <job> --resume DIR` marches on from it")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -246,6 +248,39 @@ def oracle_run_for(snap_info, snap):
                             order=snap_info["order"])
 
 
+STATE_DIR = os.path.join(REPO, "oracle", "_build", "state")
+
+
+def window_snapshot_dir(workload):
+    """Where build() leaves the workload's window snapshot (on a machine with a GPU)."""
+    return os.path.join(STATE_DIR, os.path.splitext(WORKLOADS[workload])[0] + "-window")
+
+
+def window_snapshot_ready(d, args, jobpath):
+    """`d` holds the snapshot of the job file as it is now at the window's first step for these
+    --steps/--warmup (checked from meta.json alone, without the CUDA library)."""
+    from mithra_gb300 import snapshot
+    try:
+        with open(os.path.join(d, "meta.json")) as f:
+            info = json.load(f)
+    except (OSError, ValueError):
+        return False
+    total = info.get("march_steps")
+    return total is not None and snapshot.current(d, jobpath, window_start(int(total), args.warmup, args.steps))
+
+
+def window_snapshot_file(args, jobpath):
+    """(info, snapshot) of the window's first step from the snapshot build() wrote, or None when
+    it is absent or was taken at another step (read without the CUDA library)."""
+    from mithra_gb300 import snapshot
+    d = window_snapshot_dir(args.workload)
+    if not window_snapshot_ready(d, args, jobpath):
+        return None
+    with open(os.path.join(d, "meta.json")) as f:
+        info = json.load(f)
+    return info, snapshot.load(d)
+
+
 def window_snapshot_child(args, jobpath):
     """(info, snapshot) of the job at the window's first step, marched by the FP64 form in a child
     process (this process never loads the CUDA library) and streamed back through a pipe."""
@@ -268,20 +303,25 @@ def window_snapshot_child(args, jobpath):
 def write_window_snapshot(args):
     """--snapshot-fd / --write-snapshot: march the workload (FP64 form) to the window's first step
     and stream the snapshot to the descriptor or write it to the directory."""
+    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
+    if args.write_snapshot and window_snapshot_ready(args.write_snapshot, args, jobpath):
+        print("window snapshot in %s is current" % args.write_snapshot, file=sys.stderr)
+        return
     import mithra_gb300 as mg
     from mithra_gb300 import snapshot
-    jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
     setup = mg.Setup.from_job(jobpath)
     with mg.Context.from_setup(setup, mg.FP64) as ctx:
         ctx.run_prelude()
-        start = window_start(march_steps(setup, ctx), args.warmup, args.steps)
+        total = march_steps(setup, ctx)
+        start = window_start(total, args.warmup, args.steps)
         ctx.run(start)
         snap = snapshot.take(ctx)
+    extra = {"march_steps": total}
     if args.write_snapshot:
-        snapshot.save(snap, args.write_snapshot, jobpath, setup, start)
+        snapshot.save(snap, args.write_snapshot, jobpath, setup, start, extra)
         return
     with os.fdopen(args.snapshot_fd, "wb") as f:
-        snapshot.write_stream(snap, f, jobpath, setup, start)
+        snapshot.write_stream(snap, f, jobpath, setup, start, extra)
 
 
 def snapshot_info(setup, jobpath, snap, step):
@@ -381,12 +421,19 @@ def run_reference(args, dist):
     """The reference algorithm on the host cores: the oracle's C restatement (pinned bit for bit
     to the reference in the container that has the reference tree; that tree is not on the GPU
     host, so its binary cannot be built here), all host threads, then one thread.  It starts from
-    the march state at the window's first step, which a child process computes with the FP64
-    form (this process loads no CUDA library): the CPU would take about 15 minutes to march there."""
+    the march state at the window's first step, computed by the FP64 form (the CPU would take
+    about 15 minutes to march there): the snapshot build() writes on a machine with a GPU, or,
+    when that is absent, one a child process marches and streams back.  This process loads no
+    CUDA library either way."""
     jobpath = os.path.join(REPO, "mithra_gb300", "jobs", WORKLOADS[args.workload])
     if dist.rank != 0:
         return
-    info, snap = window_snapshot_child(args, jobpath)
+    got = window_snapshot_file(args, jobpath)
+    source = "written by build()"
+    if got is None:
+        got = window_snapshot_child(args, jobpath)
+        source = "marched by a child process and streamed through a pipe"
+    info, snap = got
     po, run = oracle_run_for(info, snap)
     del snap
     threads = cpu_threads()
@@ -411,8 +458,8 @@ def run_reference(args, dist):
         "data": "synthetic (seeded Halton bunch of the job file)",
         "config": run_config(args.workload, nodes, run.n, nsub, "fp64", dist.world),
         "window": {"first_step": info["step"] + args.warmup, "steps": args.steps, "entered_fraction": entered,
-                   "how": "the march state of step %d (FP64 form on the GPU, in a child process, streamed "
-                          "through a pipe), W warm-up and K timed steps on the host" % info["step"]},
+                   "how": "the march state of step %d (FP64 form on the GPU, %s), W warm-up and K timed "
+                          "steps on the host" % (info["step"], source)},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
                          "sample": "%d timed field steps after %d warm-up steps from step %d of the march, C "
                                    "restatement of the reference (oracle/) with OpenMP over %d host threads, one "

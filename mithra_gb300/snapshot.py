@@ -104,17 +104,21 @@ def restore(ctx: Context, snap: Snapshot):
     ctx.set_time(TimeState(snap.time[0], snap.time[1], snap.time[2], snap.time[3]))
 
 
-def save(snap: Snapshot, out_dir: str, job_path: str, setup: Setup, step: int | None = None):
+def save(snap: Snapshot, out_dir: str, job_path: str, setup: Setup, step: int | None = None,
+         extra: dict | None = None):
     """Writes `snap` of `job_path` (initialised as `setup`) to `out_dir`; `step`: the field steps
-    marched since the job's start (default: the snapshot's nTime)."""
+    marched since the job's start (default: the snapshot's nTime); `extra`: more keys for
+    meta.json."""
     os.makedirs(out_dir, exist_ok=True)
+    if os.path.exists(os.path.join(out_dir, "meta.json")):  # no stale marker while the arrays change
+        os.remove(os.path.join(out_dir, "meta.json"))
     anp1, an, anm1 = snap.fields
     np.savez(os.path.join(out_dir, "fields.npz"), anp1=anp1, an=an, anm1=anm1)
     if snap.scalar is not None:
         fnp1, fn, fnm1 = snap.scalar
         np.savez(os.path.join(out_dir, "scalar.npz"), fnp1=fnp1, fn=fn, fnm1=fnm1)
     np.save(os.path.join(out_dir, "particles.npy"), np.ascontiguousarray(snap.particles))
-    info = _info(snap, job_path, setup, step)
+    info = _info(snap, job_path, setup, step, extra)
     tmp = os.path.join(out_dir, "meta.json.tmp")
     with open(tmp, "w") as f:
         json.dump(info, f)
@@ -136,15 +140,17 @@ def load(in_dir: str) -> Snapshot:
                     (float(t[0]), float(t[1]), int(t[2]), int(t[3])))
 
 
-def _info(snap: Snapshot, job_path: str, setup: Setup, step: int | None) -> dict:
+def _info(snap: Snapshot, job_path: str, setup: Setup, step: int | None, extra: dict | None = None) -> dict:
     g = setup.grid()
     meta = dict(setup.meta())
     meta.update({"time": snap.time[0], "timeBunch": snap.time[1], "nTime": snap.time[2],
                  "nTimeBunch": snap.time[3]})
-    return {"format": FORMAT, "job": os.path.abspath(job_path), "job_mtime": os.path.getmtime(job_path),
+    info = {"format": FORMAT, "job": os.path.abspath(job_path), "job_mtime": os.path.getmtime(job_path),
             "step": snap.step if step is None else int(step), "solver": int(g.solver),
             "order": int(g.truncation_order), "total_time": setup.total_time(),
             "n_particles": int(snap.particles.shape[0]), "time": list(snap.time), "meta": meta}
+    info.update(extra or {})
+    return info
 
 
 class _Pipe:
@@ -167,12 +173,12 @@ class _Pipe:
         self._f.flush()
 
 
-def write_stream(snap: Snapshot, f, job_path: str, setup: Setup, step: int | None = None):
-    """Writes `snap` to the binary stream `f` (a pipe, say): one JSON line as in meta.json with
-    the names of the arrays, then each array in .npy format."""
+def write_stream(snap: Snapshot, f, job_path: str, setup: Setup, step: int | None = None, extra: dict | None = None):
+    """Writes `snap` to the binary stream `f` (a pipe, say): one JSON line as in meta.json (plus
+    `extra`) with the names of the arrays, then each array in .npy format."""
     names = ["anp1", "an", "anm1"] + (["fnp1", "fn", "fnm1"] if snap.scalar is not None else []) + ["particles"]
     arrays = list(snap.fields) + (list(snap.scalar) if snap.scalar is not None else []) + [snap.particles]
-    info = _info(snap, job_path, setup, step)
+    info = _info(snap, job_path, setup, step, extra)
     info["arrays"] = names
     f = _Pipe(f)
     f.write((json.dumps(info) + "\n").encode())
