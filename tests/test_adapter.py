@@ -2,7 +2,7 @@
 initialised Solver, the same descriptors as the library's host set-up, bit for bit.
 
 The adapter is compiled against the reference's headers and linked with the reference's objects
-(oracle/Makefile.ref, target `adapter`); the driver oracle/adapter_check.cpp parses each job as
+(oracle/Makefile.ref, target `adapter`); the test program oracle/adapter_check.cpp parses each job as
 the reference's main does, runs Solver::initialize through the adapter's solver class and writes
 what describe_for_gpu() returns, stopping before any device call.  Skipped where the reference
 tree is absent."""
@@ -25,7 +25,7 @@ CHECK = os.path.join(REPO, "oracle", "_ref", "adapter_check")
 
 @pytest.fixture(scope="module")
 def adapter_check():
-    mg.lib()  # the library the driver links against
+    mg.lib()  # the library the test program links against
     cmd = ["make", "-s", "-f", os.path.join(REPO, "oracle", "Makefile.ref"), "adapter", "-j8"]
     ref = os.environ.get("MITHRA_REFERENCE_SRC")
     if ref:
