@@ -220,55 +220,88 @@ struct EBArgs {
 };
 
 
+// The evaluation marches along z: a block owns a 32 x 8 (j, i) tile and a run of `ks` planes.  The
+// curl reads S = A^n + A^{n+1} of each component at the node's neighbours, where every value is read
+// by four neighbouring nodes; each S is formed once per plane (with a one-node halo in i and j)
+// into a ring of three planes in shared memory, with a third fewer FP64 operations than forming it
+// at every use (the FP64 form is bound by the FP64 pipe).  Planes outside the particle slab and the
+// power planes are skipped, and a run of wanted planes starts by forming S of its first plane's
+// two neighbours.
+constexpr int EBZ_TJ = 32, EBZ_TI = 8, EBZ_W = EBZ_TJ + 2, EBZ_H = EBZ_TI + 2;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_eval_eb(GridDev g, EBArgs<T> p, int k_lo, int k_hi) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int k = blockIdx.z + k_lo;
-  if (j > g.N1 - 2 || i > g.N0 - 2 || k > k_hi) return;
-  if (!eb_plane_wanted(k, p.st, p.plane_needed, g.N2)) return;
-  const long long m = node_index(g, k, i, j);
+__global__ void __launch_bounds__(EBZ_TJ * EBZ_TI) k_eval_eb_z(GridDev g, EBArgs<T> p, int ks) {
+  __shared__ double sS[3][3][EBZ_H][EBZ_W];  // ring slot (plane % 3), component, local i, local j
+  const int tx = threadIdx.x % EBZ_TJ, ty = threadIdx.x / EBZ_TJ;
+  const int i0 = blockIdx.y * EBZ_TI, j0 = blockIdx.x * EBZ_TJ;  // halo origin: node (i0, j0)
+  const int i = i0 + 1 + ty, j = j0 + 1 + tx;                    // this thread's node
+  const bool in = i <= g.N0 - 2 && j <= g.N1 - 2;
+  const int kb = 1 + (int)blockIdx.z * ks, ke = min(g.N2 - 2, kb + ks - 1);
   const long long cs = g.cstride, sI = g.P1, sK = g.plane;
-  const double rmdt = p.rmdt;
-  const double rdx2 = p.rdx2, rdy2 = p.rdy2, rdz2 = p.rdz2;
   const T *A1 = p.anp1, *A0 = p.an;
-  float e[3], b[3];
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    float ef = to_float_rn((double)A1[c * cs + m] * rmdt);
-    ef = to_float_rn(to_double(ef) - (double)A0[c * cs + m] * rmdt);
-    e[c] = ef;
-  }
-  if (p.fn) {
-    e[0] = to_float_rn(to_double(e[0]) - ((double)p.fn[m + sI] - (double)p.fn[m - sI]) * rdx2);
-    e[1] = to_float_rn(to_double(e[1]) - ((double)p.fn[m + 1] - (double)p.fn[m - 1]) * rdy2);
-    e[2] = to_float_rn(to_double(e[2]) - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
-  }
-  const T *X0 = A0, *Y0 = A0 + cs, *Z0 = A0 + 2 * cs, *X1 = A1, *Y1 = A1 + cs, *Z1 = A1 + 2 * cs;
-  // 0.5 * (curl A^n + curl A^{n+1}) with the two levels summed first.
+  const double rmdt = p.rmdt, rdx2 = p.rdx2, rdy2 = p.rdy2, rdz2 = p.rdz2;
   const double hx = 0.5 * rdx2, hy = 0.5 * rdy2, hz = 0.5 * rdz2;
-  double bx = (((double)Z0[m + 1] + Z1[m + 1]) - ((double)Z0[m - 1] + Z1[m - 1])) * hy -
-              (((double)Y0[m + sK] + Y1[m + sK]) - ((double)Y0[m - sK] + Y1[m - sK])) * hz;
-  double by = (((double)X0[m + sK] + X1[m + sK]) - ((double)X0[m - sK] + X1[m - sK])) * hz -
-              (((double)Z0[m + sI] + Z1[m + sI]) - ((double)Z0[m - sI] + Z1[m - sI])) * hx;
-  double bz = (((double)Y0[m + sI] + Y1[m + sI]) - ((double)Y0[m - sI] + Y1[m - sI])) * hx -
-              (((double)X0[m + 1] + X1[m + 1]) - ((double)X0[m - 1] + X1[m - 1])) * hy;
-  b[0] = to_float_rn(bx); b[1] = to_float_rn(by); b[2] = to_float_rn(bz);
-  T eo[3], bo[3];
+  auto fill = [&](int k) {  // S of plane k over the tile and its halo
+    const int slot = k % 3;
+    for (int t = threadIdx.x; t < EBZ_H * EBZ_W; t += EBZ_TJ * EBZ_TI) {
+      const int li = t / EBZ_W, lj = t % EBZ_W;
+      const int gi = i0 + li, gj = j0 + lj;
+      if (gi < g.N0 && gj < g.N1) {
+        const long long m = node_index(g, k, gi, gj);
 #pragma unroll
-  for (int c = 0; c < 3; c++) {
-    eo[c] = (T)to_double(e[c]);
-    bo[c] = (T)to_double(b[c]);
-    p.E[c * cs + m] = eo[c];
-    p.B[c * cs + m] = bo[c];
-  }
-  if (k == 1) {
+        for (int c = 0; c < 3; c++) sS[slot][c][li][lj] = (double)A0[c * cs + m] + A1[c * cs + m];
+      }
+    }
+  };
+  int filled = -2;  // highest plane whose S is in the ring, with the two below it
+  for (int k = kb; k <= ke; k++) {
+    if (!eb_plane_wanted(k, p.st, p.plane_needed, g.N2)) continue;  // uniform across the block
+    if (filled != k) {  // a new run: S of planes k-1 and k
+      __syncthreads();
+      fill(k - 1);
+      fill(k);
+    } else {
+      __syncthreads();  // every thread is done with plane k-2, whose slot plane k+1 takes
+    }
+    fill(k + 1);
+    filled = k + 1;
+    __syncthreads();
+    if (!in) continue;
+    const long long m = node_index(g, k, i, j);
+    float e[3], b[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = eo[c]; p.B[c * cs + m - sK] = bo[c]; }
-  }
-  if (k == g.N2 - 2) {
+    for (int c = 0; c < 3; c++) {
+      float ef = to_float_rn((double)A1[c * cs + m] * rmdt);
+      ef = to_float_rn(to_double(ef) - (double)A0[c * cs + m] * rmdt);
+      e[c] = ef;
+    }
+    if (p.fn) {
+      e[0] = to_float_rn(to_double(e[0]) - ((double)p.fn[m + sI] - (double)p.fn[m - sI]) * rdx2);
+      e[1] = to_float_rn(to_double(e[1]) - ((double)p.fn[m + 1] - (double)p.fn[m - 1]) * rdy2);
+      e[2] = to_float_rn(to_double(e[2]) - ((double)p.fn[m + sK] - (double)p.fn[m - sK]) * rdz2);
+    }
+    const int sc = k % 3, sm = (k + 2) % 3, sp = (k + 1) % 3;
+    const int li = ty + 1, lj = tx + 1;
+    const double bx = (sS[sc][2][li][lj + 1] - sS[sc][2][li][lj - 1]) * hy - (sS[sp][1][li][lj] - sS[sm][1][li][lj]) * hz;
+    const double by = (sS[sp][0][li][lj] - sS[sm][0][li][lj]) * hz - (sS[sc][2][li + 1][lj] - sS[sc][2][li - 1][lj]) * hx;
+    const double bz = (sS[sc][1][li + 1][lj] - sS[sc][1][li - 1][lj]) * hx - (sS[sc][0][li][lj + 1] - sS[sc][0][li][lj - 1]) * hy;
+    b[0] = to_float_rn(bx); b[1] = to_float_rn(by); b[2] = to_float_rn(bz);
+    T eo[3], bo[3];
 #pragma unroll
-    for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = eo[c]; p.B[c * cs + m + sK] = bo[c]; }
+    for (int c = 0; c < 3; c++) {
+      eo[c] = (T)to_double(e[c]);
+      bo[c] = (T)to_double(b[c]);
+      p.E[c * cs + m] = eo[c];
+      p.B[c * cs + m] = bo[c];
+    }
+    if (k == 1) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) { p.E[c * cs + m - sK] = eo[c]; p.B[c * cs + m - sK] = bo[c]; }
+    }
+    if (k == g.N2 - 2) {
+#pragma unroll
+      for (int c = 0; c < 3; c++) { p.E[c * cs + m + sK] = eo[c]; p.B[c * cs + m + sK] = bo[c]; }
+    }
   }
 }
 

@@ -148,8 +148,9 @@ int stage_eval_eb(mithra_ctx* ctx, bool full = false) {
   EBArgs<double> eb{ctx->A[ctx->idx[0]], ctx->A[ctx->idx[1]], fn, ctx->E64, ctx->B64,
                     full ? nullptr : ctx->st, ctx->plane_needed,
                     -1.0 / g.dt, 1.0 / (2.0 * g.dx), 1.0 / (2.0 * g.dy), 1.0 / (2.0 * g.dz)};
-  dim3 blk(32, 8), grd((g.N1 - 2 + 31) / 32, (g.N0 - 2 + 7) / 8, g.N2 - 2);
-  return timed(ctx, "eval_eb", [&] { k_eval_eb<double><<<grd, blk, 0, ctx->stream>>>(g, eb, 1, g.N2 - 2); });
+  constexpr int ks = 32;  // planes per block of the z-marching kernel
+  dim3 grd((g.N1 - 2 + EBZ_TJ - 1) / EBZ_TJ, (g.N0 - 2 + EBZ_TI - 1) / EBZ_TI, (g.N2 - 2 + ks - 1) / ks);
+  return timed(ctx, "eval_eb", [&] { k_eval_eb_z<double><<<grd, EBZ_TJ * EBZ_TI, 0, ctx->stream>>>(g, eb, ks); });
 }
 
 int stage_field_update(mithra_ctx* ctx) {
