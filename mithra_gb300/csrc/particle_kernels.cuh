@@ -344,7 +344,8 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
        p += (long long)gridDim.x * blockDim.x) {
     if (pt.status[p] & 1) continue;
     const double rp0 = pt.x[p], rp1 = pt.y[p], rp2 = pt.z[p];
-    const int kp = ifloor_d((rp2 - g.zmin) * g.rdz);
+    const double tzp = (rp2 - g.zmin) * g.rdz;  // positions in cells from here on
+    const int kp = ifloor_d(tzp);
     kmin = min(kmin, kp);
     kmax = max(kmax, kp);
     const double rm0 = pt.mx[p], rm1 = pt.my[p], rm2 = pt.mz[p];
@@ -352,25 +353,25 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
     const bool bm = inside(rm0, rm1, rm2);
     if (!(bp || bm)) continue;
     const double qh = pt.q[p] * 0.5;
-    const int ip = ifloor_d((rp0 - g.xmin) * g.rdx), jp = ifloor_d((rp1 - g.ymin) * g.rdy);
-    const int im = ifloor_d((rm0 - g.xmin) * g.rdx), jm = ifloor_d((rm1 - g.ymin) * g.rdy),
-              km = ifloor_d((rm2 - g.zmin) * g.rdz);
-    const double r0 = dmin_k(double_of_int(min(im, ip)) * g.dx + g.dx + g.xmin,
-                             dmax_k(double_of_int(max(im, ip)) * g.dx + g.xmin, 0.5 * (rm0 + rp0)));
-    const double r1 = dmin_k(double_of_int(min(jm, jp)) * g.dy + g.dy + g.ymin,
-                             dmax_k(double_of_int(max(jm, jp)) * g.dy + g.ymin, 0.5 * (rm1 + rp1)));
-    const double r2 = dmin_k(double_of_int(min(km, kp)) * g.dz + g.dz + g.zmin,
-                             dmax_k(double_of_int(max(km, kp)) * g.dz + g.zmin, 0.5 * (rm2 + rp2)));
+    const double txp = (rp0 - g.xmin) * g.rdx, typ = (rp1 - g.ymin) * g.rdy;
+    const double txm = (rm0 - g.xmin) * g.rdx, tym = (rm1 - g.ymin) * g.rdy, tzm = (rm2 - g.zmin) * g.rdz;
+    const int ip = ifloor_d(txp), jp = ifloor_d(typ);
+    const int im = ifloor_d(txm), jm = ifloor_d(tym), km = ifloor_d(tzm);
+    // The relay point of the zigzag scheme in cells: the midpoint clamped to [origin of the upper
+    // cell, origin of the lower cell + 1] (src/fdtd.cpp:80-85 in length units; the half segments'
+    // midpoints and currents follow from it with fewer FP64 operations in cell units).
+    const double u0 = dmin_k(double_of_int(min(im, ip)) + 1.0, dmax_k(double_of_int(max(im, ip)), 0.5 * (txm + txp)));
+    const double u1 = dmin_k(double_of_int(min(jm, jp)) + 1.0, dmax_k(double_of_int(max(jm, jp)), 0.5 * (tym + typ)));
+    const double u2 = dmin_k(double_of_int(min(km, kp)) + 1.0, dmax_k(double_of_int(max(km, kp)), 0.5 * (tzm + tzp)));
     double c;
     if (bp) {
       const long long m = node_index(g, kp, ip, jp);
-      const double dxp = modf_d((0.5 * (rp0 + r0) - g.xmin) * g.rdx, &c);
-      const double dyp = modf_d((0.5 * (rp1 + r1) - g.ymin) * g.rdy, &c);
-      const double dzp = modf_d((0.5 * (rp2 + r2) - g.zmin) * g.rdz, &c);
-      deposit_half_edges(J, cs, m, sI, sK, qh, dxp, dyp, dzp, rp0 - r0, rp1 - r1, rp2 - r2);
+      const double dxp = modf_d(0.5 * (txp + u0), &c);
+      const double dyp = modf_d(0.5 * (typ + u1), &c);
+      const double dzp = modf_d(0.5 * (tzp + u2), &c);
+      deposit_half_edges(J, cs, m, sI, sK, qh, dxp, dyp, dzp, (txp - u0) * g.dx, (typ - u1) * g.dy, (tzp - u2) * g.dz);
       if (rho) {
-        const double fx = modf_d((rp0 - g.xmin) * g.rdx, &c), fy = modf_d((rp1 - g.ymin) * g.rdy, &c),
-                     fz = modf_d((rp2 - g.zmin) * g.rdz, &c);
+        const double fx = modf_d(txp, &c), fy = modf_d(typ, &c), fz = modf_d(tzp, &c);
         const double q = pt.q[p];
         const double x1 = 1.0 - fx, y1 = 1.0 - fy, z1 = 1.0 - fz;
         atomicAdd(rho + m, q * x1 * y1 * z1);
@@ -385,10 +386,10 @@ __global__ void __launch_bounds__(256) k_deposit_fp64(GridDev g, ParticlesDev<do
     }
     if (bm) {
       const long long m = node_index(g, km, im, jm);
-      const double dxm = modf_d((0.5 * (rm0 + r0) - g.xmin) * g.rdx, &c);
-      const double dym = modf_d((0.5 * (rm1 + r1) - g.ymin) * g.rdy, &c);
-      const double dzm = modf_d((0.5 * (rm2 + r2) - g.zmin) * g.rdz, &c);
-      deposit_half_edges(J, cs, m, sI, sK, qh, dxm, dym, dzm, r0 - rm0, r1 - rm1, r2 - rm2);
+      const double dxm = modf_d(0.5 * (txm + u0), &c);
+      const double dym = modf_d(0.5 * (tym + u1), &c);
+      const double dzm = modf_d(0.5 * (tzm + u2), &c);
+      deposit_half_edges(J, cs, m, sI, sK, qh, dxm, dym, dzm, (u0 - txm) * g.dx, (u1 - tym) * g.dy, (u2 - tzm) * g.dz);
     }
   }
   slab_update(st, kmin, kmax);
