@@ -71,8 +71,12 @@ struct UndDev {
   int has_prev, has_next;
   // FP32 copies for the mixed form.
   float ct_f, st_f, ku_f, b0_f, ul_f, r0_prev_f, r0_next_f;
-  double kgdz;  // ku * gamma * dz: the phase advance across one cell along z
+  double kgdz;      // ku * gamma * dz: the phase advance across one cell along z
+  double kgdz_sub;  // the same across one sub-plane interval of the FP64 phase table
 };
+
+// Sub-planes per cell of the FP64 form's undulator phase table (k_undulator_table64).
+constexpr int kUndSub = 4;
 
 // FP64 form: a static module's lz and the sine and cosine of its phase ku*lz on node plane k,
 // for the bunch time of one substep (k_undulator_table64).
@@ -87,6 +91,7 @@ struct PushDev {
   // phase advance across a cell is too large for the short series of the push.
   const UndPlane64* und_planes;
   double gdz;     // gamma * dz
+  double gdz_sub; // gamma * dz / kUndSub
   int n_und;
   double und0_dist;
   // Laser beams acting on the particles: optical undulators (indexed by UndDev::beam) and,
@@ -354,31 +359,41 @@ __host__ __device__ __forceinline__ double double_of_int(int n) {
 __host__ __device__ __forceinline__ double dmin_k(double a, double b) { return dkey(b) < dkey(a) ? b : a; }
 __host__ __device__ __forceinline__ double dmax_k(double a, double b) { return dkey(a) < dkey(b) ? b : a; }
 
-// sin d and cos d for |d| <= 1 (the push's plane-table phase advance): Taylor series in d^2 (coefficients (-1)^n/(2n+1)!
-// and (-1)^n/(2n)!) by Horner's rule, 21 FP64 operations with no range reduction.
-__host__ __device__ __forceinline__ void sin_cos_series(double d, double* sd, double* cd) {
+// sin d and cos d for |d| <= 1/4 (the push's advance within one sub-plane interval of the phase
+// table): Taylor series in d^2 (coefficients (-1)^n/(2n+1)! and (-1)^n/(2n)!) by Horner's rule,
+// cut after d^11 and d^12 (the first terms left out, d^13/13! and d^14/14!, stay below 3e-18), 14
+// FP64 operations and no range reduction.
+__host__ __device__ __forceinline__ void sin_cos_series_short(double d, double* sd, double* cd) {
   const double d2 = d * d;
-  double ps = -1.0 / 121645100408832000.0;                 // -1/19!
-  ps = fma(ps, d2, 1.0 / 355687428096000.0);               //  1/17!
-  ps = fma(ps, d2, -1.0 / 1307674368000.0);                // -1/15!
-  ps = fma(ps, d2, 1.0 / 6227020800.0);                    //  1/13!
-  ps = fma(ps, d2, -1.0 / 39916800.0);                     // -1/11!
+  double ps = -1.0 / 39916800.0;                           // -1/11!
   ps = fma(ps, d2, 1.0 / 362880.0);                        //  1/9!
   ps = fma(ps, d2, -1.0 / 5040.0);                         // -1/7!
   ps = fma(ps, d2, 1.0 / 120.0);                           //  1/5!
   ps = fma(ps, d2, -1.0 / 6.0);                            // -1/3!
   *sd = fma(d * d2, ps, d);
-  double pc = 1.0 / 2432902008176640000.0;                 //  1/20!
-  pc = fma(pc, d2, -1.0 / 6402373705728000.0);             // -1/18!
-  pc = fma(pc, d2, 1.0 / 20922789888000.0);                //  1/16!
-  pc = fma(pc, d2, -1.0 / 87178291200.0);                  // -1/14!
-  pc = fma(pc, d2, 1.0 / 479001600.0);                     //  1/12!
+  double pc = 1.0 / 479001600.0;                           //  1/12!
   pc = fma(pc, d2, -1.0 / 3628800.0);                      // -1/10!
   pc = fma(pc, d2, 1.0 / 40320.0);                         //  1/8!
   pc = fma(pc, d2, -1.0 / 720.0);                          // -1/6!
   pc = fma(pc, d2, 1.0 / 24.0);                            //  1/4!
   pc = fma(pc, d2, -0.5);                                  // -1/2!
   *cd = fma(d2, pc, 1.0);
+}
+
+// 1/x for a positive normal x: the hardware's approximate reciprocal and two Newton steps (each
+// doubling the correct bits), within about one unit in the last place of the correctly rounded
+// quotient; five FP64 operations where a division takes about ten.
+__device__ __forceinline__ double rcp_nr(double x) {
+  double r;
+#ifdef __CUDA_ARCH__
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+#else
+  r = 1.0 / x;
+#endif
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
 }
 
 // pmod, src/stdinclude.cpp:88-93.

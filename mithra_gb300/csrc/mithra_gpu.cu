@@ -172,7 +172,7 @@ int stage_push(mithra_ctx* ctx, int save_rnm) {
   int r;
   if (ctx->P.und_planes) {
     const GridDev& g = ctx->g;
-    const int n = ctx->P.n_und * (g.N2 + 1);
+    const int n = ctx->P.n_und * (g.N2 + 1) * kUndSub;
     r = timed(ctx, "undulator_table", [&] {
       k_undulator_table64<<<std::max(1, (n + 255) / 256), 256, 0, ctx->stream>>>(
           ctx->und_dev, ctx->P.n_und, g.N2, g.zmin, g.dz, ctx->P.gamma, ctx->P.beta * ctx->P.c0, ctx->P.dt_shift,
@@ -488,6 +488,7 @@ int mithra_gpu_create(const mithra_grid_desc* gd, const mithra_push_desc* pd, in
     P.inv_r2 = 1.0 / pd->r2;
     P.und_planes = nullptr;
     P.gdz = pd->gamma * gd->dz;
+    P.gdz_sub = P.gdz / kUndSub;
     P.beams = nullptr; P.ext0 = 0; P.n_ext = 0; P.n_opt = 0;
     CK(dalloc(&ctx->und_dev, kMaxUndulators));
     CK(dalloc(&ctx->beams_dev, kMaxUndulators + MITHRA_MAX_EXT_FIELDS));
@@ -605,6 +606,7 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
     U.ct_f = (float)U.ct; U.st_f = (float)U.st; U.ku_f = (float)U.ku; U.b0_f = (float)U.b0; U.ul_f = (float)U.ul;
     U.r0_prev_f = (float)U.r0_prev; U.r0_next_f = (float)U.r0_next;
     U.kgdz = U.ku * ctx->P.gdz;
+    U.kgdz_sub = U.ku * ctx->P.gdz_sub;
     U.beam = -1;
     if (U.type == 1) {
       U.beam = (int)ctx->opt_beams.size();
@@ -622,7 +624,7 @@ int mithra_gpu_set_undulators(mithra_ctx* ctx, const mithra_undulator_desc* und,
     bool small = true;
     for (const UndDev& U : ctx->und_host) small = small && (U.type != 0 || std::fabs(U.kgdz) <= kUndTableMaxKgdz);
     if (small) {
-      CK(cudaMalloc(&ctx->und_table, (size_t)n * (ctx->g.N2 + 1) * sizeof(UndPlane64)));
+      CK(cudaMalloc(&ctx->und_table, (size_t)n * (ctx->g.N2 + 1) * kUndSub * sizeof(UndPlane64)));
       ctx->P.und_planes = (const UndPlane64*)ctx->und_table;
     }
   }

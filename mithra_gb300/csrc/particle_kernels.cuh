@@ -7,16 +7,17 @@
 
 namespace mithra {
 
-// Per-plane undulator lz and phase for the FP64 push: lz_k = gamma (zmin + k dz + beta c0
-// (timeBunch + dt_)) - rb on node plane k, with the sine and cosine of ku lz_k.  One entry per
-// static module and plane k = 0..N2.
+// Undulator lz and phase for the FP64 push on kUndSub sub-planes per cell: lz = gamma (zmin +
+// (k + s / kUndSub) dz + beta c0 (timeBunch + dt_)) - rb on sub-plane s of node plane k, with the
+// sine and cosine of ku lz.  Entries per static module: (N2 + 1) * kUndSub.
 __global__ void k_undulator_table64(const UndDev* __restrict__ und, int n_und, int N2, double zmin, double dz,
                                     double gamma, double bc, double dt_shift, const StateDev* st,
                                     UndPlane64* __restrict__ table) {
   const double tshift = bc * (st->time_bunch + dt_shift);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_und * (N2 + 1); t += gridDim.x * blockDim.x) {
-    const int u = t / (N2 + 1), k = t % (N2 + 1);
-    const double lz = gamma * (zmin + (double)k * dz + tshift) - und[u].rb;
+  const int per = (N2 + 1) * kUndSub;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n_und * per; t += gridDim.x * blockDim.x) {
+    const int u = t / per, q = t % per;
+    const double lz = gamma * (zmin + ((double)(q / kUndSub) + (double)(q % kUndSub) / kUndSub) * dz + tshift) - und[u].rb;
     double s, c;
     sincos(und[u].ku * lz, &s, &c);
     table[t] = UndPlane64{lz, s, c};
@@ -24,8 +25,8 @@ __global__ void k_undulator_table64(const UndDev* __restrict__ und, int n_und, i
 }
 
 // Largest phase advance across one cell (ku gamma dz) for which the push takes the undulator
-// phase from the plane table: with |d| <= 1 the Taylor series of sin_cos_series truncate below
-// 1e-17 relative (d^21/21!, d^22/22!).  The bench jobs advance 0.78 rad per boosted-frame cell.
+// phase from the table: the advance within a sub-plane interval then stays below 1/4, where
+// sin_cos_series_short holds.  The bench jobs advance 0.78 rad per boosted-frame cell.
 constexpr double kUndTableMaxKgdz = 1.0;
 
 // Solver::undulatorField for static modules (src/solver.cpp:1798-1824) and
@@ -33,9 +34,10 @@ constexpr double kUndTableMaxKgdz = 1.0;
 // into the bunch frame, to bt/et.  Optical modules are laser beams (laser_beams_add), added
 // after the static ones.
 // kz, fz: node plane below z and the offset above it in cells ((z - zmin)/dz = kz + fz).  On a
-// plane of the table, lz = lz_k + gamma dz fz and sin, cos of ku lz come from the plane's values
-// and the series of the phase advance d = ku gamma dz fz (|d| < kUndTableMaxKgdz) by the
-// angle-sum formulas: about 27 FP64 operations instead of a sincos with its range reduction.
+// plane of the table, with fz = (s + r) / kUndSub for sub-plane s, lz = lz_ks + gamma dz r /
+// kUndSub and sin, cos of ku lz come from the sub-plane's values and the series of the phase
+// advance d = ku gamma dz r / kUndSub (|d| < 1/4) by the angle-sum formulas: about 22 FP64
+// operations instead of a sincos with its range reduction.
 __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict__ und, int n_und,
                                                        const PushDev& P, double timeBunch,
                                                        double x, double y, double z, int N2, int kz, double fz,
@@ -46,10 +48,13 @@ __device__ __forceinline__ void static_undulator_field(const UndDev* __restrict_
     if (U.type != 0) continue;  // optical modules: laser_beams_add
     double lz, sn = 0.0, cs = 0.0;
     if (tab) {
-      const UndPlane64 te = P.und_planes[u * (N2 + 1) + kz];
-      lz = fma(P.gdz, fz, te.lz);
+      const double f4 = fz * kUndSub;        // exact
+      const int sub = ifloor_d(f4);           // 0 .. kUndSub - 1
+      const double r = f4 - double_of_int(sub);  // exact
+      const UndPlane64 te = P.und_planes[(u * (N2 + 1) + kz) * kUndSub + sub];
+      lz = fma(P.gdz_sub, r, te.lz);
       double sd, cd;
-      sin_cos_series(U.kgdz * fz, &sd, &cd);
+      sin_cos_series_short(U.kgdz_sub * r, &sd, &cd);
       sn = te.s * cd + te.c * sd;
       cs = te.c * cd - te.s * sd;
     } else {
@@ -183,7 +188,7 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         const double py = f * (mz * bt[0] - mx * bt[2]) + my;
         const double pz = f * (mx * bt[1] - my * bt[0]) + mz;
         const double bt2 = bt[0] * bt[0] + bt[1] * bt[1] + bt[2] * bt[2];
-        const double s = 2.0 / (d1 * P.inv_r2 + f * bt2);
+        const double s = 2.0 * rcp_nr(d1 * P.inv_r2 + f * bt2);
         gx = s * (py * bt[2] - pz * bt[1]) + mx + P.r1 * et[0];
         gy = s * (pz * bt[0] - px * bt[2]) + my + P.r1 * et[1];
         gz = s * (px * bt[1] - py * bt[0]) + mz + P.r1 * et[2];
