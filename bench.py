@@ -6,8 +6,8 @@ divided by the step time, where particle pushes = particles x bunch substeps.  T
 workload is the 128 x 128 x 2048-cell job (130 x 130 x 2050 nodes, ~8.1e6 macro-particles,
 two bunch substeps per field step) in the plain FP64 form; --precision fp32 selects the mixed
 form.  Inputs are seeded synthetic bunches (Halton sequence) built by the reference's own
-initialisation restated on the host; the field state (3.4 GB) exceeds the 129 MB L2, so no L2
-flush is needed between steps.
+initialisation restated on the host; the march state (2.5 GB of potentials, 3.2 GB with the
+particles) exceeds the 129 MB L2, so no L2 flush is needed between steps.
 
 The timed window lies in the part of the march where the whole bunch is inside the undulator
 (every particle gathers E and B and feels the undulator field): the march is run from its start
