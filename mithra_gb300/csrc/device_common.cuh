@@ -306,6 +306,12 @@ __host__ __device__ __forceinline__ long long dkey(double x) {
   return (b ^ (s & 0x7fffffffffffffffLL)) - s;
 }
 
+// x is a NaN, from its bits: dkey orders NaNs beyond the infinities, where every FP64 comparison
+// with them is false, so a caller that relies on those comparisons being false tests for NaN first.
+__host__ __device__ __forceinline__ bool is_nan_bits(double x) {
+  return (bits_of(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
+}
+
 // floor(t) as an int for |t| < 2^31, from the bits of t (negative t, rare in the callers, takes
 // the hardware path).
 __host__ __device__ __forceinline__ int ifloor_d(double t) {

@@ -199,8 +199,10 @@ __global__ void __launch_bounds__(256) k_push_fp64(GridDev g, PushDev P, const U
         pt.x[p] = x + gg * gx; pt.y[p] = y + gg * gy; pt.z[p] = z + drz;
         zr += drz;
         const long long kzn = dkey(zr);
-        if (kzn < kzl) cross = 1;
-        else if (kzn >= kzh) cross = 2;
+        if (!is_nan_bits(zr)) {  // a NaN position crosses no face (its FP64 comparisons are false)
+          if (kzn < kzl) cross = 1;
+          else if (kzn >= kzh) cross = 2;
+        }
       }
     }
     pt.cross[p] = cross;
@@ -287,14 +289,20 @@ __global__ void k_advance_time(StateDev* st, double dt) {
 
 // Solver::recycleParticles / the erasure in FdTd::currentCommunicate (src/solver.cpp:493-503,
 // src/fdtd.cpp:214-224): erase particles whose wrapped z lies outside [zp0, zp1).
+// The comparisons run on the integer pipes (dkey): with the FP64 ones the pass was bound by the
+// FP64 pipe, with them it is a read of z and the status byte.
 template <typename T>
 __global__ void __launch_bounds__(256) k_erase_outside(GridDev g, ParticlesDev<T> pt, StateDev* st) {
   const long long n = st->n_particles;
+  const long long kLz = dkey(g.Lz), kz0 = dkey(g.zp0), kz1 = dkey(g.zp1);
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
        p += (long long)gridDim.x * blockDim.x) {
     if (pt.status[p] & 1) continue;
-    const double zr = pmod_d((double)pt.z[p] - g.zmin, g.Lz) + g.zmin;
-    if (zr < g.zp0 || zr >= g.zp1) pt.status[p] |= 1;
+    const double za = (double)pt.z[p] - g.zmin;
+    const long long ka = dkey(za);
+    const double zr = ((ka >= 0 && ka < kLz) ? za : pmod_d(za, g.Lz)) + g.zmin;  // pmod_d's own fast path
+    const long long kr = dkey(zr);
+    if ((kr < kz0 || kr >= kz1) && !is_nan_bits(zr)) pt.status[p] |= 1;  // a NaN compares false
   }
 }
 

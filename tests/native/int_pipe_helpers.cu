@@ -1,5 +1,5 @@
 // Host check of the integer-pipe double helpers of device_common.cuh (dkey, ifloor_d, modf_d,
-// itrunc_d, double_of_int, dmin_k, dmax_k, sin_cos_series_short) against the C library on many values: powers of two and their neighbours, integers
+// itrunc_d, double_of_int, dmin_k, dmax_k, is_nan_bits, sin_cos_series_short) against the C library on many values: powers of two and their neighbours, integers
 // and near-integers of both signs, signed zeros and random values over 40 binades.
 #include <cmath>
 #include <cstdio>
@@ -12,6 +12,10 @@
 using namespace mithra;
 
 int main() {
+  // NaNs and infinities only for is_nan_bits (the other helpers are not defined on them)
+  const double special[] = {std::nan(""), -std::nan(""), (double)INFINITY, -(double)INFINITY, 1e308, -1e308};
+  for (double x : special)
+    if (is_nan_bits(x) != std::isnan(x)) { printf("is_nan_bits(%g)\n", x); return 1; }
   std::vector<double> v = {0.0, -0.0, 1.0, -1.0, 0.5, -0.5, 1e-300, -1e-300, 4.9e-324, -4.9e-324,
                            2147483647.0, -2147483647.0, 2147483646.5, -2147483646.5};
   for (int e = -60; e <= 30; e++) {
@@ -47,6 +51,8 @@ int main() {
       checks++;
       if (double_of_int(n) != (double)n) { if (bad++ < 10) printf("double_of_int(%d) = %.17g\n", n, double_of_int(n)); }
     }
+    checks++;
+    if (is_nan_bits(t) != std::isnan(t)) { if (bad++ < 10) printf("is_nan_bits(%.17g)\n", t); }
     const double s = v[(a * 7919 + 13) % v.size()];
     checks++;
     if (!(dmin_k(t, s) == std::fmin(t, s) && dmax_k(t, s) == std::fmax(t, s))) {
