@@ -300,7 +300,8 @@ constexpr int kHeavyTile = 512;         // tiles with this many particles lead t
 // costs more than the particles' global atomics).
 constexpr int kSparseTile = 64;
 
-// The deposit of one run of particles: p = beg + threadIdx.x, stepping by `stride`, below `end`.
+// The deposit of one run of particles: the chunks of kDepositBlock particles from `beg`, stepping
+// by `stride`, below `end`, each thread taking one particle of each chunk.
 // `tiled`: the currents go to the shared tile copy whose node (0, 0, 0) is mesh node (i0, j0, k0)
 // (the block then flushes it to J); otherwise straight to J with global atomics.
 __device__ __forceinline__ void deposit_run(const DepositF32& D, const ParticlesF32& pt, float* sJ, float* J, float* rho,
@@ -323,7 +324,11 @@ __device__ __forceinline__ void deposit_run(const DepositF32& D, const Particles
     L.q = pt.q[p];
     return L;
   };
-  int p = beg + threadIdx.x;
+  // The lanes of a warp take particles four apart (thread t: offset 4 * lane + warp in each run of
+  // kDepositBlock): consecutive particles, often the four members of one shot-noise beamlet in
+  // neighbouring cells, go to different warps, so fewer lanes of one shared atomic meet on an edge.
+  static_assert(kDepositBlock == 128, "four warps per deposit block");
+  int p = beg + (int)((threadIdx.x & 31) * 4 + (threadIdx.x >> 5));
   Loaded cur{};
   if (p < end) cur = load(p);
   for (; p < end; p += stride) {
