@@ -248,6 +248,36 @@ def noise_floor(ps: list[dict], n_perturb: int, spectrum_points: int, workdir: s
     return P, rel_sd, rel_dev
 
 
+ROUGH_INPUTS = ("gamma", "K", "lambda_u", "charge_pc", "sigma_r", "energy_spread")
+
+
+def roughness(ps: list[dict], deltas, spectrum_points: int, workdir: str, device: int = 0):
+    """How far P_sat moves when one design input moves by a small relative step: every design
+    solved as drawn and with each input of ROUGH_INPUTS multiplied by (1 + delta), one input at a
+    time, for every delta.  A smooth map of the inputs changes P_sat by about its logarithmic
+    slope times delta; a change far above that at small delta is the roughness that limits any
+    regressor trained on a feasible number of designs.  Returns {delta: |P_sat(moved) / P_sat - 1|
+    as an array [n_designs x len(ROUGH_INPUTS)]}."""
+    runs = []
+    for p in ps:
+        runs.append(dict(p))
+        for d in deltas:
+            for k in ROUGH_INPUTS:
+                q = dict(p)
+                q[k] = p[k] * (1.0 + d)
+                runs.append(q)
+    for j, q in enumerate(runs):
+        q["index"] = j
+    _, _, psat, _, _ = solve_designs(runs, spectrum_points, workdir, device)
+    per = 1 + len(deltas) * len(ROUGH_INPUTS)
+    P = psat.reshape(len(ps), per)
+    out = {}
+    for a, d in enumerate(deltas):
+        moved = P[:, 1 + a * len(ROUGH_INPUTS):1 + (a + 1) * len(ROUGH_INPUTS)]
+        out[d] = np.abs(moved / P[:, :1] - 1.0)
+    return out
+
+
 def to_log(x: np.ndarray, scale: float) -> np.ndarray:
     return np.log10(np.maximum(x, FLOOR * scale))
 
@@ -377,6 +407,9 @@ def main(argv=None):
     ap.add_argument("--perturb", type=int, default=8, help="--noise-floor: solves per design")
     ap.add_argument("--perturb-step", type=float, default=4,
                     help="--noise-floor: particles added per solve (>= 1) or fraction of the count (< 1)")
+    ap.add_argument("--roughness", type=int, default=0, metavar="N",
+                    help="measure how far P_sat moves under small relative input steps on N designs and exit")
+    ap.add_argument("--deltas", default="1e-4,1e-3,1e-2", help="--roughness: relative input steps")
     a = ap.parse_args(argv)
 
     if a.gemm_bench:
@@ -391,6 +424,16 @@ def main(argv=None):
                               median_rel_sd=float(np.median(sd)), p90_rel_sd=float(np.quantile(sd, 0.9)),
                               median_rel_dev=float(np.median(dev)), p90_rel_dev=float(np.quantile(dev, 0.9)),
                               rel_sd=[float(x) for x in sd], psat=P.tolist())))
+        return
+    if a.roughness:
+        ps = design_parameters(a.roughness, a.seed, small=a.small, seeded=a.seeded)
+        deltas = [float(x) for x in a.deltas.split(",")]
+        r = roughness(ps, deltas, a.spectrum, tempfile.mkdtemp(prefix="mithra-rough-"))
+        print(json.dumps(dict(designs=a.roughness, small=a.small, seeded=a.seeded, inputs=list(ROUGH_INPUTS),
+                              steps=[dict(delta=d, median=float(np.median(v)), p90=float(np.quantile(v, 0.9)),
+                                          median_per_input={k: float(np.median(v[:, i]))
+                                                            for i, k in enumerate(ROUGH_INPUTS)})
+                                     for d, v in r.items()])))
         return
     if a.load:
         d = np.load(a.load)

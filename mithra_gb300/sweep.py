@@ -58,8 +58,8 @@ def job_text(p: dict, spectrum_points: int = 0) -> str:
     4.8 cells per resonant wavelength lambda_u (1 + K^2 / 2) / (2 gamma^2) along z, so that every
     design resolves its own radiation; a fixed lz leaves the radiation of high-gamma designs
     below one cell per wavelength, and such marches diverge;
-    spectrum_points > 0 samples the power at that many normalized frequencies in 0.9 .. 1.1
-    instead of at 1.0 only.  p["seed_a0"] > 0 adds a continuous gaussian-beam seed at the
+    spectrum_points > 0 samples the power at that many normalized frequencies in 0.89 .. 1.11
+    (centred on 1.0) instead of at 1.0 only.  p["seed_a0"] > 0 adds a continuous gaussian-beam seed at the
     resonant wavelength lambda_u (1 + K^2/2) / (2 gamma^2), polarised along y, focused at the
     undulator start with a waist of 2 sigma_r and that strength parameter."""
     lam = p["lambda_u"] * (1.0 + 0.5 * p["K"] ** 2) / (2.0 * p["gamma"] ** 2)
@@ -74,7 +74,11 @@ def job_text(p: dict, spectrum_points: int = 0) -> str:
     # march from the bunch's start to the undulator exit (plus the 2-period default gap)
     total_time = (periods + 2) * p["lambda_u"] / 299.792458 * 1.05
     if spectrum_points > 0:
-        freq = ("minimum-normalized-frequency = 0.9\n    maximum-normalized-frequency = 1.1\n"
+        # The DFT window of the power sampling is Nf = int(3 T / dt) samples, T the period of the
+        # lowest frequency (src/radiation.cpp:88-93); this family's time step is T_1.0 / 9.6, so a band
+        # starting at 0.9 puts 3 T / dt at exactly 32 and rounding picks Nf = 31 or 32 (a jump of
+        # several percent in the sampled power) from design to design.  0.89 gives 32.36: Nf = 32.
+        freq = ("minimum-normalized-frequency = 0.89\n    maximum-normalized-frequency = 1.11\n"
                 "    number-of-frequency-points   = %d" % spectrum_points)
     else:
         freq = "normalized-frequency    = 1.0"
