@@ -22,3 +22,21 @@ def test_sweep_jobs_initialise():
         # NSFD may widen the transverse cells (src/solver.cpp:237-245), never narrow them
         assert g.N2 == p["n_longitudinal"] + 2 and 34 <= g.N0 <= p["n_transverse"] + 2
         assert s.particles().shape[0] >= p["particles"]
+
+
+def test_surrogate_family_keeps_one_dft_window_length():
+    """The power band of the surrogate's designs keeps the DFT window (Nf = int(3 T / dt) samples,
+    T the period of the band's lowest frequency, src/radiation.cpp:88-93) at one length: with the
+    family's time step T_1.0 / 9.6 a band starting at 0.9 put 3 T / dt at exactly 32, where
+    rounding chose 31 or 32 from design to design; the central frequency stays at 1.0."""
+    import numpy as np
+
+    from mithra_gb300 import surrogate
+    for small in (False, True):
+        ps = surrogate.design_parameters(48, 7, small=small)
+        setups = sweep.make_setups(ps, tempfile.mkdtemp(), threads=4, spectrum_points=128)
+        metas = [s.meta() for s in setups]
+        assert {m["rp0_Nf"] for m in metas} == {32.0}
+        for m in metas:
+            w1 = 2.0 * np.pi / (9.6 * m["dt"])
+            assert abs(m["rp0_w64"] / w1 - 1.0) < 1e-9
