@@ -76,7 +76,7 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=DEFAULT_WARMUP)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS) + ["sweep-192"])
+    ap.add_argument("--workload", default="fel-130x130x2050", choices=sorted(WORKLOADS) + ["sweep-192", "surrogate"])
     ap.add_argument("--autotune-steps", type=int, default=0,
                     help="sweep-192: autotune every instance on this many steps per candidate shape")
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
@@ -88,6 +88,11 @@ def parse_args():
     ap.add_argument("--sweep-leg-slots", type=int, default=96)
     ap.add_argument("--sweep-check-designs", type=int, default=8,
                     help="designs marched in both forms for the P_sat error of the sweep leg")
+    ap.add_argument("--surrogate-designs", type=int, default=16384,
+                    help="surrogate: designs solved by the full solver (training + held-out)")
+    ap.add_argument("--surrogate-held-out", type=int, default=1024)
+    ap.add_argument("--surrogate-threshold", type=float, default=0.1,
+                    help="surrogate: ensemble spread of P_sat above which a design goes to the full solver")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp32-compare", action="store_true",
@@ -801,6 +806,44 @@ def run_sweep(args, dist):
     print(json.dumps(out), flush=True)
 
 
+def run_surrogate(args, dist):
+    """FEL designs per hour with surrogate screening, against the batched full solver: seeded designs
+    of the surrogate family (48x48x384 cells, 131,072 particles, NSFD, mixed form) solved in batches,
+    an ensemble trained on all but the held-out designs by the library's tcgen05 GEMMs, and the
+    held-out designs screened at the spread threshold (the full solver takes those above it).  A
+    screened design costs the ensemble's inference plus, for the fallback fraction, a full solve."""
+    import tempfile
+
+    from mithra_gb300 import surrogate as sg
+    if dist.rank != 0:
+        return
+    n, held, thr = args.surrogate_designs, args.surrogate_held_out, args.surrogate_threshold
+    ps = sg.design_parameters(n, 7)
+    with ClockSampler(dist.local) as clk:
+        curves, spectra, psat, host_s, dev_s = sg.solve_designs(ps, 128, tempfile.mkdtemp(prefix="mithra-surrogate-"),
+                                                                device=dist.local)
+        out = sg.train_and_screen(sg.features(ps), curves, spectra, psat, host_s, dev_s, held, 128,
+                                  thresholds=sorted({0.02, 0.05, 0.1, 0.2, thr}))
+    row = next(r for r in out["screening"] if r["threshold"] == thr)
+    solve_s = out["solve_s_per_design"]
+    screened_s = out["infer_s_per_design"] + row["fallback"] * solve_s
+    print(json.dumps({
+        "metric": "FEL designs/h (surrogate-screened)", "value": 3600.0 / screened_s, "unit": "designs/h",
+        "n_gpus": 1, "steps": out["train_steps"], "warmup": 0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded designs, Halton bunches)",
+        "config": {"workload": "surrogate-48x48x384", "designs": n, "held_out": held, "threshold": thr,
+                   "precision": "fp32 (mixed form) solves, bf16 network with fp32 accumulation",
+                   "parallelism": "single-gpu"},
+        "full_solve_designs_per_hour": 3600.0 / solve_s,
+        "speedup_vs_full_solve": row["speedup"],
+        "held_out_psat_error": {"median": out["median_err"], "p90": out["p90_err"],
+                                "accepted_median": row["accepted_median_err"], "accepted_p90": row["accepted_p90_err"],
+                                "fallback": row["fallback"], "trivial_median": out["baseline_median_err"]},
+        "train_s": out["train_s"], "infer_s_per_design": out["infer_s_per_design"], "screening": out["screening"],
+        "clocks": clk.summary(),
+    }), flush=True)
+
+
 def main():
     args = parse_args()
     if args.snapshot_fd is not None or args.write_snapshot:
@@ -812,6 +855,8 @@ def main():
             run_reference(args, dist)
         elif args.workload == "sweep-192":
             run_sweep(args, dist)
+        elif args.workload == "surrogate":
+            run_surrogate(args, dist)
         else:
             run_gpu(args, dist)
     finally:
