@@ -506,58 +506,6 @@ __device__ __forceinline__ float relay_axis(int cm, int cp, float fm, float fp, 
   return fminf(hi, fmaxf(lo, 0.5f * (*rm + *rp)));
 }
 
-__global__ void __launch_bounds__(256) k_deposit_f32(DepositF32 D, ParticlesF32 pt, StateDev* st, float* J,
-                                                     float* rho, long long cs, long long plane, int P1) {
-  const long long n = st->n_particles;
-  const long long sI = P1, sK = plane;
-  int kmin = 0x7fffffff, kmax = -0x7fffffff;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n;
-       p += (long long)gridDim.x * blockDim.x) {
-    if (pt.status[p] & 1) continue;
-    int ip, jp, kp, im, jm, km;
-    unpack_cell(pt.cell[p], ip, jp, kp);
-    unpack_cell(pt.mcell[p], im, jm, km);
-    kmin = min(kmin, kp);
-    kmax = max(kmax, kp);
-    const float fxp = pt.fx[p], fyp = pt.fy[p], fzp = pt.fz[p];
-    const float fxm = pt.mfx[p], fym = pt.mfy[p], fzm = pt.mfz[p];
-    const bool bp = inside_f32(D, ip, jp, kp, fxp, fyp);
-    const bool bm = inside_f32(D, im, jm, km, fxm, fym);
-    if (!(bp || bm)) continue;
-    int bx, by, bz;
-    float rxm, rxp, rym, ryp, rzm, rzp;
-    const float rx = relay_axis(im, ip, fxm, fxp, &bx, &rxm, &rxp);
-    const float ry = relay_axis(jm, jp, fym, fyp, &by, &rym, &ryp);
-    const float rz = relay_axis(km, kp, fzm, fzp, &bz, &rzm, &rzp);
-    const float qh = 0.5f * pt.q[p];
-    if (bp) {
-      const long long m = (long long)kp * plane + (long long)ip * P1 + jp;
-      const float ax = 0.5f * (rxp + rx) - (float)(ip - bx), ay = 0.5f * (ryp + ry) - (float)(jp - by),
-                  az = 0.5f * (rzp + rz) - (float)(kp - bz);
-      deposit_half_f32(J, cs, m, sI, sK, qh, ax, ay, az, (rxp - rx) * D.dx, (ryp - ry) * D.dy, (rzp - rz) * D.dz);
-      if (rho) {
-        const float q = pt.q[p];
-        const float x1 = 1.0f - fxp, y1 = 1.0f - fyp, z1 = 1.0f - fzp;
-        atomicAdd(rho + m, q * x1 * y1 * z1);
-        atomicAdd(rho + m + sI, q * fxp * y1 * z1);
-        atomicAdd(rho + m + 1, q * x1 * fyp * z1);
-        atomicAdd(rho + m + sI + 1, q * fxp * fyp * z1);
-        atomicAdd(rho + m + sK, q * x1 * y1 * fzp);
-        atomicAdd(rho + m + sK + sI, q * fxp * y1 * fzp);
-        atomicAdd(rho + m + sK + 1, q * x1 * fyp * fzp);
-        atomicAdd(rho + m + sK + sI + 1, q * fxp * fyp * fzp);
-      }
-    }
-    if (bm) {
-      const long long m = (long long)km * plane + (long long)im * P1 + jm;
-      const float ax = 0.5f * (rxm + rx) - (float)(im - bx), ay = 0.5f * (rym + ry) - (float)(jm - by),
-                  az = 0.5f * (rzm + rz) - (float)(km - bz);
-      deposit_half_f32(J, cs, m, sI, sK, qh, ax, ay, az, (rx - rxm) * D.dx, (ry - rym) * D.dy, (rz - rzm) * D.dz);
-    }
-  }
-  slab_update(st, kmin, kmax);
-}
-
 // Records (11 doubles) <-> mixed-form particles.  Cell = floor((x - xmin)/dx) in FP64.
 struct CellMap {
   double xmin, ymin, zmin, dx, dy, dz;
@@ -592,49 +540,6 @@ __global__ void k_records_to_f32(const double* __restrict__ rec, long long n, Pa
     pt.cross[p] = 0;
     pt.id[p] = (int)p;
   }
-}
-
-__global__ void __launch_bounds__(1024) k_f32_to_records(ParticlesF32 pt, const StateDev* st, double* rec, long long cap,
-                                                         long long* n_out, CellMap M) {
-  __shared__ int s_warp[32];
-  __shared__ long long s_base;
-  const long long n = st->n_particles;
-  if (threadIdx.x == 0) s_base = 0;
-  __syncthreads();
-  for (long long c0 = 0; c0 < n; c0 += blockDim.x) {
-    const long long p = c0 + threadIdx.x;
-    const int take = (p < n) && !(pt.status[p] & 1);
-    const unsigned bal = __ballot_sync(0xffffffffu, take);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) s_warp[warp] = __popc(bal);
-    __syncthreads();
-    int before = 0, total = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-      if (w < warp) before += s_warp[w];
-      total += s_warp[w];
-    }
-    before += __popc(bal & ((1u << lane) - 1u));
-    const long long d = s_base + before;
-    if (take && d < cap) {
-      double* r = rec + 11 * d;
-      int i, j, k;
-      unpack_cell(pt.cell[p], i, j, k);
-      r[0] = pt.q[p];
-      r[1] = M.xmin + ((double)i + (double)pt.fx[p]) * M.dx;
-      r[2] = M.ymin + ((double)j + (double)pt.fy[p]) * M.dy;
-      r[3] = M.zmin + ((double)k + (double)pt.fz[p]) * M.dz;
-      unpack_cell(pt.mcell[p], i, j, k);
-      r[4] = M.xmin + ((double)i + (double)pt.mfx[p]) * M.dx;
-      r[5] = M.ymin + ((double)j + (double)pt.mfy[p]) * M.dy;
-      r[6] = M.zmin + ((double)k + (double)pt.mfz[p]) * M.dz;
-      r[7] = pt.gx[p]; r[8] = pt.gy[p]; r[9] = pt.gz[p];
-      r[10] = pt.e[p] ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) s_base += total;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *n_out = s_base;
 }
 
 }  // namespace mithra
