@@ -7,8 +7,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
-#include <cstdlib>
-#include <ctime>
 #include <fstream>
 #include <sstream>
 #include <stdexcept>
@@ -25,29 +23,26 @@ Vec3 cross(const Vec3& x, const Vec3& y) {
 }
 }  // namespace
 
-// halton, src/stdinclude.cpp:45-73.
-double halton(unsigned i, unsigned j) {
-  if (i > 20) die(" dimension can not be larger than 20. ");
-  static const unsigned prime[20] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71};
-  int p0, p, k, a;
-  double x = 0.0;
-  p = (int)prime[i];
-  p0 = p;
-  k = (int)(j + 1);
-  while (k > 0) {
-    a = k % p;
-    x += a / (double)p0;
-    k = int(k / p);
-    p0 *= p;
+// The bunch generator's quasi-random sequence (src/stdinclude.cpp:45-73): point `index` of the
+// Halton sequence in dimension `dim`, reflected, i.e. 1 minus the radical inverse of index + 1 in
+// the dim-th prime base.
+double halton(unsigned dim, unsigned index) {
+  static const int kPrimes[20] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61, 67, 71};
+  if (dim >= 20) die(" dimension can not be larger than 20. ");
+  const int base = kPrimes[dim];
+  double inverse = 0.0;
+  int scale = base;
+  for (int digits = (int)(index + 1); digits > 0; digits /= base) {
+    inverse += (digits % base) / (double)scale;
+    scale *= base;
   }
-  return 1.0 - x;
+  return 1.0 - inverse;
 }
 
-// pmod, src/stdinclude.cpp:88-93.
+// a modulo b in [0, b) for b > 0 (src/stdinclude.cpp:88-93); a zero remainder comes out as +0.
 double pmod(double a, double b) {
-  double x = std::fmod(a, b);
-  x += (x < 0.0) ? b : 0.0;
-  return x;
+  const double r = std::fmod(a, b);
+  return r + (r < 0.0 ? b : 0.0);
 }
 
 // Signal::self, src/classes.cpp:557-598.
@@ -157,99 +152,99 @@ void init_manual(const BunchInit& b, std::vector<Charge>& qv, int ia) {
   qv.push_back(c);
 }
 
-// Bunch::initializeEllipsoid, src/classes.cpp:104-298 (rank 0 of 1).
+namespace {
+// Draws of an ellipsoid bunch from the Halton sequence, as Bunch::initializeEllipsoid lays them
+// out (src/classes.cpp:104-298): draw i of a bunch uses point base + i (base = particles already
+// in the list) of dimensions 0/1 (transverse position, Box-Muller radius and angle), 2/3
+// (longitudinal position), 4/5 and 6/7 (momentum spread); a beamlet's shot noise uses dimensions
+// 8/9 at the index of its wavelength slot.  Every expression keeps the reference's evaluation
+// order, so the records come out bit for bit the same.
+struct EllipsoidDraws {
+  const BunchInit& b;
+  unsigned base;
+
+  // sigma sqrt(-2 ln u) times cos or sin of 2 pi v, (u, v) the points of dimensions (du, dv)
+  double normal(double sigma, unsigned du, unsigned dv, unsigned i, bool cosine) const {
+    const double radius = sigma * std::sqrt(-2.0 * std::log(halton(du, base + i)));
+    const double angle = 2.0 * PI * halton(dv, base + i);
+    return radius * (cosine ? std::cos(angle) : std::sin(angle));
+  }
+  // longitudinal offset of a draw of the main part
+  double z_main(unsigned i) const {
+    if (b.distribution == "uniform") return (2.0 * halton(2, base + i) - 1.0) * b.sigmaPosition[2];
+    return normal(b.sigmaPosition[2], 2, 3, i, false);
+  }
+  // longitudinal offset of a draw of the uniform profile's edges: a normal of rms 2 lambda moved
+  // out past +-sigma_z
+  double z_edge(unsigned i) const {
+    const double z = normal(2.0 * b.lambda, 2, 3, i, false);
+    return z + ((z < 0.0) ? (-b.sigmaPosition[2]) : (b.sigmaPosition[2]));
+  }
+};
+}  // namespace
+
+// An ellipsoid bunch, Bunch::initializeEllipsoid (src/classes.cpp:104-298) on one rank: the main
+// part's draws, for a uniform profile followed by the draws of its soft edges, each kept inside the
+// truncation and turned into a beamlet of four particles a quarter wavelength apart (one particle
+// when no wavelength is set).  The reference's `random` generator draws from an unseeded rand(),
+// so no two runs agree; it is refused here.
 void init_ellipsoid(BunchInit b, std::vector<Charge>& qv, int ia) {
-  if (b.numberOfParticles % 4 != 0) b.numberOfParticles += 4 - b.numberOfParticles % 4;
-  const unsigned Np = b.numberOfParticles, Np0 = (unsigned)qv.size();
-  Charge charge;
-  charge.q = b.cloudCharge / Np;
-  Vec3 gb;
-  for (int d = 0; d < 3; d++) gb[d] = b.initialGamma * b.betaVector[d];
-  Vec3 r{0, 0, 0}, t{0, 0, 0};
-  double t0, zmin = 1e100, Ne = 0.0, bF = 0.0, bFi;
-  unsigned bmi, i;
-  std::vector<double> randomNumbers;
-  const unsigned ng = (b.lambda == 0.0) ? 1 : 4;
   if (b.bF > 2.0 || b.bF < 0.0) die("The bunching factor can not be larger than one or a negative value !!!");
-  if (b.generator == "random") {
-    // Not reproducible by design (src/classes.cpp:142-150); kept for completeness.
-    srand((unsigned)time(NULL));
-    randomNumbers.resize(Np / ng * 20, 0.0);
-    for (unsigned ri = 0; ri < Np / ng * 20; ri++) randomNumbers[ri] = ((double)rand()) / RAND_MAX;
-  }
-  auto generate = [&](unsigned n, unsigned m) -> double {
-    if (b.generator == "random") return randomNumbers[n * 2 * Np / ng + m];
-    return halton(n, m);
-  };
-  auto insert = [&](Charge q) {
-    for (unsigned ii = 0; ii < ng; ii++) {
-      if (b.shotNoise) {
-        bmi = int((charge.rnp[2] - zmin) / b.lambda);
-        bFi = bF * std::sqrt(-2.0 * std::log(generate(8, bmi)));
-        q.rnp[2] = charge.rnp[2] - b.lambda / 4 * ii;
-        q.rnp[2] -= b.lambda / PI * bFi * std::sin(2.0 * PI / b.lambda * q.rnp[2] + 2.0 * PI * generate(9, bmi));
-      } else if (b.lambda != 0.0) {
-        q.rnp[2] = charge.rnp[2] - b.lambda / 4 * ii;
-        q.rnp[2] -= b.lambda / PI * b.bF * std::sin(2.0 * PI / b.lambda * q.rnp[2] + b.bFP * PI / 180.0);
-      }
-      qv.push_back(q);
-    }
-  };
-  const unsigned n_taper = unsigned(Np / ng * (1.0 + 2.0 * b.lambda * std::sqrt(2.0 * PI) / (2.0 * b.sigmaPosition[2])));
+  if (b.distribution != "uniform" && b.distribution != "gaussian")
+    die("The longitudinal type is not correctly given to the code !!!");
+  if (b.generator == "random")
+    die("generator = random draws from an unseeded random number generator and cannot reproduce a run; use halton");
+  if (b.numberOfParticles % 4 != 0) b.numberOfParticles += 4 - b.numberOfParticles % 4;
+  const unsigned per_beamlet = (b.lambda == 0.0) ? 1 : 4;
+  const unsigned n_main = b.numberOfParticles / per_beamlet;
+  // the uniform profile's edges add 2 lambda sqrt(2 pi) / (2 sigma_z) of the main part's draws
+  const unsigned n_draws =
+      (b.distribution == "uniform")
+          ? unsigned(n_main * (1.0 + 2.0 * b.lambda * std::sqrt(2.0 * PI) / (2.0 * b.sigmaPosition[2])))
+          : n_main;
+  const EllipsoidDraws draw{b, (unsigned)qv.size()};
+  auto z_of = [&](unsigned i) { return i < n_main ? draw.z_main(i) : draw.z_edge(i); };
+
+  // Shot noise: the bunch front (smallest z of all draws) anchors the wavelength slots; each slot
+  // has its own bunching amplitude (default 1 / sqrt(electrons per wavelength)) and phase.
+  double z_front = 1e100, amplitude = 0.0;
   if (b.shotNoise) {
-    for (i = 0; i < Np / ng; i++) {
-      if (b.distribution == "uniform")
-        zmin = std::min((2.0 * generate(2, i + Np0) - 1.0) * b.sigmaPosition[2], zmin);
-      else if (b.distribution == "gaussian")
-        zmin = std::min(b.sigmaPosition[2] * std::sqrt(-2.0 * std::log(generate(2, i + Np0))) *
-                            std::sin(2.0 * PI * generate(3, i + Np0)),
-                        zmin);
-      else
-        die("The longitudinal type is not correctly given to the code !!!");
-    }
-    if (b.distribution == "uniform")
-      for (; i < n_taper; i++) {
-        t0 = 2.0 * b.lambda * std::sqrt(-2.0 * std::log(generate(2, i + Np0))) * std::sin(2.0 * PI * generate(3, i + Np0));
-        t0 += (t0 < 0.0) ? (-b.sigmaPosition[2]) : (b.sigmaPosition[2]);
-        zmin = std::min(t0, zmin);
-      }
-    zmin = zmin + b.position[ia][2];
-    Ne = b.cloudCharge * b.lambda / (2.0 * b.sigmaPosition[2]);
-    bF = (b.bF == 0.0) ? 1.0 / std::sqrt(Ne) : b.bF;
+    for (unsigned i = 0; i < n_draws; i++) z_front = std::min(z_of(i), z_front);
+    z_front = z_front + b.position[ia][2];
+    const double electrons_per_wavelength = b.cloudCharge * b.lambda / (2.0 * b.sigmaPosition[2]);
+    amplitude = (b.bF == 0.0) ? 1.0 / std::sqrt(electrons_per_wavelength) : b.bF;
   }
-  for (i = 0; i < Np / ng; i++) {
-    r[0] = b.sigmaPosition[0] * std::sqrt(-2.0 * std::log(generate(0, i + Np0))) * std::cos(2.0 * PI * generate(1, i + Np0));
-    r[1] = b.sigmaPosition[1] * std::sqrt(-2.0 * std::log(generate(0, i + Np0))) * std::sin(2.0 * PI * generate(1, i + Np0));
-    if (b.distribution == "uniform")
-      r[2] = (2.0 * generate(2, i + Np0) - 1.0) * b.sigmaPosition[2];
-    else if (b.distribution == "gaussian")
-      r[2] = b.sigmaPosition[2] * std::sqrt(-2.0 * std::log(generate(2, i + Np0))) * std::sin(2.0 * PI * generate(3, i + Np0));
-    else
-      die("The longitudinal type is not correctly given to the code !!!");
-    t[0] = b.sigmaGammaBeta[0] * std::sqrt(-2.0 * std::log(generate(4, i + Np0))) * std::cos(2.0 * PI * generate(5, i + Np0));
-    t[1] = b.sigmaGammaBeta[1] * std::sqrt(-2.0 * std::log(generate(4, i + Np0))) * std::sin(2.0 * PI * generate(5, i + Np0));
-    t[2] = b.sigmaGammaBeta[2] * std::sqrt(-2.0 * std::log(generate(6, i + Np0))) * std::cos(2.0 * PI * generate(7, i + Np0));
+  auto add_beamlet = [&](const Charge& centre) {
+    Charge p = centre;
+    for (unsigned m = 0; m < per_beamlet; m++) {
+      if (b.shotNoise) {
+        const unsigned slot = int((centre.rnp[2] - z_front) / b.lambda);
+        const double a = amplitude * std::sqrt(-2.0 * std::log(halton(8, slot)));
+        p.rnp[2] = centre.rnp[2] - b.lambda / 4 * m;
+        p.rnp[2] -= b.lambda / PI * a * std::sin(2.0 * PI / b.lambda * p.rnp[2] + 2.0 * PI * halton(9, slot));
+      } else if (b.lambda != 0.0) {
+        p.rnp[2] = centre.rnp[2] - b.lambda / 4 * m;
+        p.rnp[2] -= b.lambda / PI * b.bF * std::sin(2.0 * PI / b.lambda * p.rnp[2] + b.bFP * PI / 180.0);
+      }
+      qv.push_back(p);
+    }
+  };
+
+  Charge centre;
+  centre.q = b.cloudCharge / b.numberOfParticles;
+  Vec3 gb_mean;
+  for (int d = 0; d < 3; d++) gb_mean[d] = b.initialGamma * b.betaVector[d];
+  for (unsigned i = 0; i < n_draws; i++) {
+    const Vec3 r{draw.normal(b.sigmaPosition[0], 0, 1, i, true), draw.normal(b.sigmaPosition[1], 0, 1, i, false),
+                 z_of(i)};
+    const Vec3 t{draw.normal(b.sigmaGammaBeta[0], 4, 5, i, true), draw.normal(b.sigmaGammaBeta[1], 4, 5, i, false),
+                 draw.normal(b.sigmaGammaBeta[2], 6, 7, i, true)};
     if (std::fabs(r[0]) < b.tranTrun && std::fabs(r[1]) < b.tranTrun && std::fabs(r[2]) < b.longTrun) {
-      for (int d = 0; d < 3; d++) charge.rnp[d] = b.position[ia][d] + r[d];
-      for (int d = 0; d < 3; d++) charge.gb[d] = gb[d] + t[d];
-      insert(charge);
+      for (int d = 0; d < 3; d++) centre.rnp[d] = b.position[ia][d] + r[d];
+      for (int d = 0; d < 3; d++) centre.gb[d] = gb_mean[d] + t[d];
+      add_beamlet(centre);
     }
   }
-  if (b.distribution == "uniform")
-    for (; i < n_taper; i++) {
-      r[0] = b.sigmaPosition[0] * std::sqrt(-2.0 * std::log(generate(0, i + Np0))) * std::cos(2.0 * PI * generate(1, i + Np0));
-      r[1] = b.sigmaPosition[1] * std::sqrt(-2.0 * std::log(generate(0, i + Np0))) * std::sin(2.0 * PI * generate(1, i + Np0));
-      r[2] = 2.0 * b.lambda * std::sqrt(-2.0 * std::log(generate(2, i + Np0))) * std::sin(2.0 * PI * generate(3, i + Np0));
-      r[2] += (r[2] < 0.0) ? (-b.sigmaPosition[2]) : (b.sigmaPosition[2]);
-      t[0] = b.sigmaGammaBeta[0] * std::sqrt(-2.0 * std::log(generate(4, i + Np0))) * std::cos(2.0 * PI * generate(5, i + Np0));
-      t[1] = b.sigmaGammaBeta[1] * std::sqrt(-2.0 * std::log(generate(4, i + Np0))) * std::sin(2.0 * PI * generate(5, i + Np0));
-      t[2] = b.sigmaGammaBeta[2] * std::sqrt(-2.0 * std::log(generate(6, i + Np0))) * std::cos(2.0 * PI * generate(7, i + Np0));
-      if (std::fabs(r[0]) < b.tranTrun && std::fabs(r[1]) < b.tranTrun && std::fabs(r[2]) < b.longTrun) {
-        for (int d = 0; d < 3; d++) charge.rnp[d] = b.position[ia][d] + r[d];
-        for (int d = 0; d < 3; d++) charge.gb[d] = gb[d] + t[d];
-        insert(charge);
-      }
-    }
 }
 
 // Bunch::initialize3DCrystal, src/classes.cpp:307-353 (note: the reference clears the charge

@@ -57,7 +57,7 @@ struct Setup {
   void fill_push(mithra_push_desc* p) const;
 };
 
-double halton(unsigned i, unsigned j);
+double halton(unsigned dim, unsigned index);
 double pmod(double a, double b);
 
 }  // namespace host
