@@ -21,6 +21,10 @@ Under torchrun (N > 1) every rank runs an independent replica on its own GPU (th
 single domain per GPU); the value is the sum over ranks and the time the maximum over ranks.
 `--impl reference` times the reference algorithm on the host cores instead: the C restatement
 in oracle/ (the reference tree itself is not present on the GPU host), with all host threads.
+
+Other workloads: `--workload sweep-192` (192 sweep-family designs stepped by one graph launch
+per field step, FEL runs/h through a refilled queue) and `--workload surrogate` (FEL designs/h
+with surrogate screening against the batched full solver, with the held-out P_sat error).
 """
 from __future__ import annotations
 
