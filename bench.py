@@ -828,10 +828,17 @@ def run_surrogate(args, dist):
                                                                 device=dist.local)
         out = sg.train_and_screen(sg.features(ps), curves, spectra, psat, host_s, dev_s, held, 128,
                                   thresholds=sorted({0.02, 0.05, 0.1, 0.2, thr}))
+    print(json.dumps(surrogate_line(out, n, held, thr, clk.summary())), flush=True)
+
+
+def surrogate_line(out: dict, n: int, held: int, thr: float, clocks: dict) -> dict:
+    """The bench line of the surrogate workload from `surrogate.train_and_screen`'s result: the
+    screened designs per hour at threshold `thr` (inference for every design plus a full solve for
+    the fallback fraction), the batched full solver's designs per hour and the held-out error."""
     row = next(r for r in out["screening"] if r["threshold"] == thr)
     solve_s = out["solve_s_per_design"]
     screened_s = out["infer_s_per_design"] + row["fallback"] * solve_s
-    print(json.dumps({
+    return {
         "metric": "FEL designs/h (surrogate-screened)", "value": 3600.0 / screened_s, "unit": "designs/h",
         "n_gpus": 1, "steps": out["train_steps"], "warmup": 0, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16", "data": "synthetic (seeded designs, Halton bunches)",
@@ -844,8 +851,8 @@ def run_surrogate(args, dist):
                                 "accepted_median": row["accepted_median_err"], "accepted_p90": row["accepted_p90_err"],
                                 "fallback": row["fallback"], "trivial_median": out["baseline_median_err"]},
         "train_s": out["train_s"], "infer_s_per_design": out["infer_s_per_design"], "screening": out["screening"],
-        "clocks": clk.summary(),
-    }), flush=True)
+        "clocks": clocks,
+    }
 
 
 def main():

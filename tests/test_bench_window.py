@@ -59,3 +59,22 @@ def test_slab_nodes_cover_the_particle_planes_with_their_margins():
     # clipped to the interior planes 1 .. np-2 at the mesh ends
     p = _parts([(1, 1, 0), (1, 1, 10)], m, rng)
     assert bench.slab_nodes(p, m) == 10 * 4 * 3
+
+
+def test_surrogate_line_rates_and_keys():
+    """The surrogate workload's bench line: screened designs/h = 3600 / (inference + fallback x
+    full solve), the full solver's designs/h, the row of the chosen threshold."""
+    out = {"solve_s_per_design": 0.032, "infer_s_per_design": 3e-5, "train_steps": 6000, "train_s": 25.0,
+           "median_err": 0.022, "p90_err": 0.066, "baseline_median_err": 0.9,
+           "screening": [{"threshold": 0.05, "fallback": 0.1, "accepted_median_err": 0.021,
+                          "accepted_p90_err": 0.06, "speedup": 9.9},
+                         {"threshold": 0.1, "fallback": 0.001, "accepted_median_err": 0.022,
+                          "accepted_p90_err": 0.066, "speedup": 500.0}]}
+    line = bench.surrogate_line(out, 16384, 1024, 0.1, {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                                                         "samples": 0})
+    assert line["value"] == 3600.0 / (3e-5 + 0.001 * 0.032)
+    assert line["full_solve_designs_per_hour"] == 3600.0 / 0.032
+    assert line["held_out_psat_error"]["fallback"] == 0.001 and line["speedup_vs_full_solve"] == 500.0
+    assert line["config"]["workload"] == "surrogate-48x48x384" and line["config"]["threshold"] == 0.1
+    for k in ("metric", "unit", "n_gpus", "higher_is_better", "dtype", "clocks"):
+        assert k in line
